@@ -1,0 +1,177 @@
+/*
+ * umcp_gpu.h - C ABI of the GB300 membrane-surface engine.
+ *
+ * Drop-in replacement for the hot path of UMCP's `struct surface`
+ * (src/interp.h:210-552): the Loop limit-surface Helfrich energy and its
+ * gradient, the effective-mass apply and the membrane integrators. Plain C
+ * types only; every call returns a umcp_status and never exits the process
+ * (the reference prints and calls exit(1), e.g. src/grad.C:67-72).
+ *
+ * Threading: a umcp_ctx owns one CUDA stream on one device; calls on a ctx
+ * (and on meshes made from it) are serialised on that stream. Use one ctx
+ * per host thread. Host-pointer calls copy in and out; *_device calls take
+ * device pointers that live on the ctx's device.
+ */
+#ifndef UMCP_GPU_H
+#define UMCP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  UMCP_OK = 0,
+  UMCP_ERR_INVALID = 1,     /* bad argument, malformed mesh or plan */
+  UMCP_ERR_IO = 2,          /* file could not be read or written */
+  UMCP_ERR_CUDA = 3,        /* CUDA runtime error (umcp_last_error has the text) */
+  UMCP_ERR_NONFINITE = 4,   /* NaN/Inf in the energy ("nan en.", src/interpLib.C:3770-3774) */
+  UMCP_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  UMCP_ERR_NOMEM = 6,       /* device memory exhausted or over the admission budget */
+  UMCP_ERR_UNSUPPORTED = 7, /* option the engine does not implement */
+  UMCP_ERR_DIVERGED = 8     /* energy jump above the divergence threshold (src/hd.C:1280-1305) */
+} umcp_status;
+
+typedef enum { UMCP_FP64 = 0, UMCP_FP32_CENTRED = 1 } umcp_precision;
+
+typedef struct umcp_ctx umcp_ctx;
+typedef struct umcp_plan umcp_plan;   /* host-side plan: topology, basis rows, reference state */
+typedef struct umcp_mesh umcp_mesh;   /* device-resident surface built from a plan */
+
+/* Physical parameters, as the reference's input keywords (src/input.C:16-310). */
+typedef struct {
+  double kc;          /* bending modulus, kcal/mol ("kc", default 14) */
+  double KA;          /* per-point area modulus ("KA", default -1 -> 0.215) */
+  double kg;          /* Gaussian modulus ("kg", default 0) */
+  double k_reg;       /* angle regulariser (global k_reg, default 0) */
+  double temperature; /* K ("T", default 298) */
+  int precision;      /* umcp_precision */
+  const char *lipid_directives; /* text holding "lipid library|inner|outer ..." lines, or NULL */
+} umcp_params;
+
+/* Sizes of a plan. */
+typedef struct {
+  int nv;            /* vertices; state vectors have 3*nv+3 doubles (xyz..., alpha_x,y,z) */
+  int n_regular;     /* faces whose lowest-index corner has valence 6 (12 control points, 15 points) */
+  int n_irregular;   /* faces at a valence 5/7 corner (valence+6 control points, 16 points) */
+  int n_lipid_types;
+  double box[9];     /* periodic box vectors PBC_vec, row-major */
+} umcp_plan_info;
+
+/* ---- errors ---------------------------------------------------------- */
+const char *umcp_last_error(void);           /* text of the last failure on this host thread */
+const char *umcp_status_string(umcp_status s);
+
+/* ---- parameters and synthetic meshes (host only) ---------------------- */
+umcp_status umcp_params_default(umcp_params *p);
+/* Replaces src/input.C keyword parsing for the hot-path keys: "kc", "KA",
+ * "kg", "T", "k_reg", "lipid ..." lines; unknown keys are ignored. */
+umcp_status umcp_params_from_input(const char *input_text, umcp_params *p, char *lipid_buf, size_t lipid_buf_len);
+
+/* Icosahedron Loop-subdivided `level` times (original vertices first, so every
+ * valence-5 vertex is its faces' lowest index), radius R, radial N(0,sigma)
+ * noise from Philox(seed, vertex), box 3R; written in the .mesh format
+ * (src/write_structures.C:473-530). */
+umcp_status umcp_mesh_generate_icosphere(int level, double R, double sigma, uint64_t seed, const char *mesh_path);
+/* nx*ny triangular lattice (ny even), spacing a, periodic box, height field
+ * with a q^-4 spectrum of variance kT/(kc*Lx*Ly*q^4) for kc = kc_kT kT. */
+umcp_status umcp_mesh_generate_planar(int nx, int ny, double a, double kc_kT, uint64_t seed, const char *mesh_path);
+
+/* ---- plans (host only) ------------------------------------------------ */
+/* surface::loadLattice + generatePlan + readLipidComposition + setg0 at the
+ * mesh-file positions (src/interpLib.C:1144, 4998; src/lipid_composition.C:47;
+ * src/interpLib.C:2969; order of src/hd.C:158-270). */
+umcp_status umcp_plan_from_file(const char *mesh_path, const umcp_params *p, umcp_plan **out);
+/* surface::setg0(r) (src/interpLib.C:2969-3390): r has 3*nv+3 doubles; the
+ * box scales are ignored, as the reference ignores them there. */
+umcp_status umcp_plan_set_reference(umcp_plan *plan, const double *r);
+umcp_status umcp_plan_info_get(const umcp_plan *plan, umcp_plan_info *info);
+/* Copies the positions the plan was built from (3*nv+3, alpha = 1). */
+umcp_status umcp_plan_positions(const umcp_plan *plan, double *r);
+/* Oriented neighbour rings (after the reference's orientation pass):
+ * valence[nv], ring[sum valence]. */
+umcp_status umcp_plan_rings(const umcp_plan *plan, int *valence, int *ring);
+/* Face tables. kind: 0 regular, 1 irregular. Arrays may be NULL to skip.
+ *   cp[nf*13], img[nf*13*3] (lattice image of each control point),
+ *   valence[nf], g0[nf*npt], rr0[nf*npt], outer[nf*ntypes], inner[nf*ntypes] */
+umcp_status umcp_plan_faces(const umcp_plan *plan, int kind, int *cp, int8_t *img, int *valence, double *g0,
+                            double *rr0, double *outer, double *inner);
+/* Basis rows of a patch type: valence 6 (15 points x 12) or 5/7 (16 points x
+ * valence+6): rows[kind(w,u,v,uu,uv,vv)][pt][cp], weight[pt], u[pt], v[pt]. */
+umcp_status umcp_plan_basis(const umcp_plan *plan, int valence, double *rows, double *weight, double *u, double *v);
+/* Lipid types of the plan: c0[ntypes], apl[ntypes]. */
+umcp_status umcp_plan_lipids(const umcp_plan *plan, double *c0, double *apl);
+void umcp_plan_destroy(umcp_plan *plan);
+
+/* ---- device context and meshes --------------------------------------- */
+umcp_status umcp_ctx_create(int device, umcp_ctx **out);
+void umcp_ctx_destroy(umcp_ctx *ctx);
+umcp_status umcp_ctx_synchronize(umcp_ctx *ctx);
+
+/* Upload a plan; the mesh keeps its own state buffers on the device. */
+umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, const umcp_params *p, umcp_mesh **out);
+void umcp_mesh_destroy(umcp_mesh *mesh);
+umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *p);
+
+/* surface::energy(r, NULL) (src/interpLib.C:4180-4352). terms (may be NULL)
+ * receives {VA, VC, VR}: area, curvature (bending + Gaussian) and angle parts. */
+umcp_status umcp_energy(umcp_mesh *mesh, const double *r, double *E, double *terms);
+/* surface::grad(r, g) (src/grad.C:65): ADDS dE/dr into g (3*nv+3). */
+umcp_status umcp_grad(umcp_mesh *mesh, const double *r, double *g);
+/* Both in one pass: E and g (g accumulated). */
+umcp_status umcp_energy_grad(umcp_mesh *mesh, const double *r, double *E, double *g);
+/* Device-pointer form: d_r, d_g hold 3*nv+3 doubles; d_E one double; g accumulated. */
+umcp_status umcp_energy_grad_device(umcp_mesh *mesh, const double *d_r, double *d_E, double *d_g);
+
+/* ---- effective mass ---------------------------------------------------- */
+/* Install M^-1 as a CSR matrix over vertices (SparseMatrix nzl/nzv rows,
+ * src/sparse.h:4-53). */
+umcp_status umcp_mass_set(umcp_mesh *mesh, int nrow, const int *row_ptr, const int *col, const double *val);
+/* AltSparseCartMatVecIncrScale (src/parallel.C:1028-1075):
+ * out[3i+c] += scale/alpha_c^2 * (scalev ? scalev[c*nrow+i] : 1) * sum_k val[k] in[3 col[k]+c]. */
+umcp_status umcp_mass_apply(umcp_mesh *mesh, const double *in, double *out, const double *scalev, double scale,
+                            const double *alphas);
+umcp_status umcp_mass_apply_device(umcp_mesh *mesh, const double *d_in, double *d_out, const double *d_scalev,
+                                   double scale, const double *alphas);
+
+/* ---- dynamics ---------------------------------------------------------- */
+typedef enum {
+  UMCP_OVERDAMPED_BD = 0, /* r += -(D/kT) g dt + sqrt(2 D dt) xi */
+  UMCP_BD_MEMBRANE = 1,   /* "do_bd_membrane" leapfrog with p reset (src/hd.C:1520-1720,1943) */
+  UMCP_LANGEVIN = 2       /* "do_ld" leapfrog with friction (src/hd.C:1546-1720) */
+} umcp_integrator_kind;
+
+typedef struct {
+  int kind;           /* umcp_integrator_kind */
+  double time_step;   /* "time_step" (s); AKMA_TIME scaling applied inside for kinds 1,2 */
+  double gamma;       /* "gamma_langevin" */
+  double D;           /* kind 0: diffusion coefficient, A^2 per time_step unit */
+  uint64_t seed;      /* Philox key */
+  uint32_t stream;    /* Philox stream id (distinguishes meshes / replicas) */
+  double divergence_threshold; /* energy jump that stops the run (hd.C uses 1e5); <= 0 disables */
+  int use_mass;       /* 1: apply the installed M^-1; 0: identity */
+} umcp_integrator;
+
+/* Run n_steps steps starting at step index `step0` on the mesh's resident
+ * state (set with umcp_state_set). Energies of each step may be returned in
+ * energies[n_steps] (may be NULL). The loop is captured into a CUDA graph
+ * after its first use with the same mesh and n_steps. */
+umcp_status umcp_state_set(umcp_mesh *mesh, const double *r, const double *p);
+umcp_status umcp_state_get(umcp_mesh *mesh, double *r, double *p);
+umcp_status umcp_run(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step0, int n_steps, double *energies);
+/* Same as umcp_run without waiting: queues the steps on the ctx stream and
+ * returns; umcp_ctx_synchronize or a later blocking call observes errors. */
+umcp_status umcp_run_async(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step0, int n_steps);
+/* One step of the integrator on HOST state: copies r (3*nv+3) and p (3*nv,
+ * may be NULL for zero momenta) in, steps once at step index `step`, copies
+ * the new r (and p) back and returns the energy of the pre-step state in *E.
+ * This is the drop-in for one pass of the reference's dynamics loop body
+ * (src/hd.C:1102-1720): energy, gradient, update. */
+umcp_status umcp_step_host(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step, double *r, double *p, double *E);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UMCP_GPU_H */

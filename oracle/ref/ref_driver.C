@@ -1,0 +1,211 @@
+/*
+ * Oracle driver (test infrastructure, never shipped): runs the REFERENCE's own
+ * membrane-surface code, compiled from its sources by oracle/ref/Makefile, and
+ * dumps what it computes so the CPU restatement (oracle/umcp_oracle.c) and
+ * the GPU path can be pinned against it.
+ *
+ * It follows the setup order of the reference's hd.C (src/hd.C:158-270):
+ *   surface::loadLattice -> surface::generatePlan -> readLipidComposition
+ *   -> r = vertex positions, alpha = 1 -> setg0(r)
+ * then fills the serial face partition that setupParallel would build
+ * (src/parallel.C:137) and calls surface::energy(r, NULL) and
+ * surface::grad(r, g) as hd.C does in its dynamics loop (src/hd.C:1128,1240).
+ *
+ * Usage:
+ *   ref_driver dump <mesh> <params> <positions.bin|-> <out_prefix>
+ *   ref_driver time <mesh> <params> <positions.bin|-> <n_calls>
+ *
+ * <params> holds "kc X", "KA X", "kg X", "k_reg X" lines and any
+ * "lipid ..." lines (read by the reference's readLipidComposition).
+ * <positions.bin> holds 3*nv+3 doubles (xyz per vertex, then alpha_x,y,z);
+ * "-" keeps the mesh-file positions. setg0 always uses the mesh-file
+ * positions (as hd.C does), so a positions file evaluates a deformed state.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <strings.h>
+#include <sys/time.h>
+#include "interp.h"
+#include "parallel.h"
+
+extern double kc, KA, kg, k_reg;
+extern double VA, VC, VR, AVC;
+extern int setup_for_parallel;
+
+static void read_params(const char *path)
+{
+	FILE *f = fopen(path, "r");
+	if (!f) { fprintf(stderr, "cannot open params %s\n", path); exit(2); }
+	char line[4096], key[256];
+	double val;
+	while (fgets(line, sizeof line, f)) {
+		if (sscanf(line, "%255s %lf", key, &val) != 2) continue;
+		if (!strcasecmp(key, "kc")) kc = val;
+		else if (!strcasecmp(key, "KA")) KA = val;
+		else if (!strcasecmp(key, "kg")) kg = val;
+		else if (!strcasecmp(key, "k_reg")) k_reg = val;
+	}
+	fclose(f);
+}
+
+static surface *setup(const char *mesh, const char *params, double **r_out)
+{
+	read_params(params);
+	surface *s = (surface *)calloc(1, sizeof(surface));
+	s->surface_id = 0;
+	s->loadLattice(mesh, 0.);
+	fprintf(stderr, "ref_driver: loaded %d vertices\n", s->nv);
+	s->generatePlan();
+	fprintf(stderr, "ref_driver: plan %d regular, %d irregular faces\n", s->nf_faces, s->nf_irr_faces);
+	FILE *pf = fopen(params, "r");
+	s->readLipidComposition(pf);
+	if (pf) fclose(pf);
+	int nv = s->nv;
+	double *r = (double *)calloc(3 * nv + 3, sizeof(double));
+	s->get(r);
+	r[3 * nv + 0] = r[3 * nv + 1] = r[3 * nv + 2] = 1.0;
+	s->setg0(r);
+	fprintf(stderr, "ref_driver: reference state set\n");
+
+	/* Serial face partition: every face on rank 0 (what setupParallel's
+	 * balanced partition reduces to for one process). */
+	setup_for_parallel = 1;
+	par_info.nSurfaces = 1;
+	par_info.my_id = 0;
+	par_info.nprocs = 1;
+	par_info.faces = (int **)malloc(sizeof(int *));
+	par_info.nf = (int *)malloc(sizeof(int));
+	int nfaces = s->nf_faces + s->nf_irr_faces;
+	par_info.faces[0] = (int *)malloc(sizeof(int) * nfaces);
+	for (int f = 0; f < nfaces; f++) par_info.faces[0][f] = f;
+	par_info.nf[0] = nfaces;
+	par_info.nc = 0;
+	*r_out = r;
+	return s;
+}
+
+static void load_positions(const char *path, double *r, int nv)
+{
+	if (!strcmp(path, "-")) return;
+	FILE *f = fopen(path, "rb");
+	if (!f) { fprintf(stderr, "cannot open positions %s\n", path); exit(2); }
+	size_t n = fread(r, sizeof(double), 3 * nv + 3, f);
+	fclose(f);
+	if (n != (size_t)(3 * nv + 3)) { fprintf(stderr, "positions file too short\n"); exit(2); }
+}
+
+static FILE *open_out(const char *prefix, const char *suffix, const char *mode)
+{
+	char name[4096];
+	snprintf(name, sizeof name, "%s.%s", prefix, suffix);
+	FILE *f = fopen(name, mode);
+	if (!f) { fprintf(stderr, "cannot write %s\n", name); exit(2); }
+	return f;
+}
+
+static void dump_formulas(FILE *f, formula *frm, int n)
+{
+	/* Per point: ncoor, tri, cp[ncoor], then doubles: weight, g0, RuRv0,
+	 * r_pbc[3*ncoor], r_w, r_u, r_v, r_uu, r_uv, r_vv [ncoor each]. */
+	for (int i = 0; i < n; i++) {
+		int hdr[2] = {frm[i].ncoor, frm[i].tri};
+		fwrite(hdr, sizeof(int), 2, f);
+		fwrite(frm[i].cp, sizeof(int), frm[i].ncoor, f);
+		double d[3] = {frm[i].weight, frm[i].g0, frm[i].RuRv0};
+		fwrite(d, sizeof(double), 3, f);
+		fwrite(frm[i].r_pbc, sizeof(double), 3 * frm[i].ncoor, f);
+		fwrite(frm[i].r_w, sizeof(double), frm[i].ncoor, f);
+		fwrite(frm[i].r_u, sizeof(double), frm[i].ncoor, f);
+		fwrite(frm[i].r_v, sizeof(double), frm[i].ncoor, f);
+		fwrite(frm[i].r_uu, sizeof(double), frm[i].ncoor, f);
+		fwrite(frm[i].r_uv, sizeof(double), frm[i].ncoor, f);
+		fwrite(frm[i].r_vv, sizeof(double), frm[i].ncoor, f);
+	}
+}
+
+int main(int argc, char **argv)
+{
+	if (argc < 6) {
+		fprintf(stderr, "usage: %s dump|time <mesh> <params> <positions|-> <out_prefix|n_calls>\n", argv[0]);
+		return 2;
+	}
+	double *r = NULL;
+	surface *s = setup(argv[2], argv[3], &r);
+	int nv = s->nv;
+	load_positions(argv[4], r, nv);
+	double *g = (double *)calloc(3 * nv + 3, sizeof(double));
+
+	if (!strcmp(argv[1], "time")) {
+		int ncalls = atoi(argv[5]);
+		struct timeval t0, t1;
+		gettimeofday(&t0, NULL);
+		double esum = 0;
+		for (int c = 0; c < ncalls; c++) {
+			esum += s->energy(r, NULL);
+			memset(g, 0, sizeof(double) * (3 * nv + 3));
+			s->grad(r, g);
+		}
+		gettimeofday(&t1, NULL);
+		double dt = (t1.tv_sec - t0.tv_sec) + 1e-6 * (t1.tv_usec - t0.tv_usec);
+		printf("{\"nv\": %d, \"calls\": %d, \"seconds\": %.6f, \"energy\": %.17e}\n", nv, ncalls, dt, esum / ncalls);
+		return 0;
+	}
+
+	double E = s->energy(r, NULL);
+	double va = VA, vc = VC, vr = VR;
+	s->grad(r, g);
+
+	const char *pre = argv[5];
+	FILE *f = open_out(pre, "energy.txt", "w");
+	fprintf(f, "E %.17e\nVA %.17e\nVC %.17e\nVR %.17e\nnv %d\nnf_faces %d\nnf_irr_faces %d\nnf_g_q_p %d\nnf_irr_pts %d\nnt %d\n",
+	        E, va, vc, vr, nv, s->nf_faces, s->nf_irr_faces, s->nf_g_q_p, s->nf_irr_pts, s->nt);
+	fclose(f);
+
+	f = open_out(pre, "grad.bin", "wb");
+	fwrite(g, sizeof(double), 3 * nv + 3, f);
+	fclose(f);
+
+	f = open_out(pre, "positions.bin", "wb");
+	fwrite(r, sizeof(double), 3 * nv + 3, f);
+	fclose(f);
+
+	/* Per-face energy, in the reference's face numbering. */
+	f = open_out(pre, "face_energy.bin", "wb");
+	for (int fx = 0; fx < s->nf_faces + s->nf_irr_faces; fx++) {
+		double e = s->faceEnergy(fx, r, NULL, 0);
+		fwrite(&e, sizeof(double), 1, f);
+	}
+	fclose(f);
+
+	f = open_out(pre, "plan_reg.bin", "wb");
+	dump_formulas(f, s->theFormulas, s->nf_faces * s->nf_g_q_p);
+	fclose(f);
+	f = open_out(pre, "plan_irr.bin", "wb");
+	dump_formulas(f, s->theIrregularFormulas, s->nf_irr_faces * s->nf_irr_pts);
+	fclose(f);
+
+	/* Triangle compositions (outer, inner leaflet areas per lipid type). */
+	f = open_out(pre, "composition.txt", "w");
+	fprintf(f, "ntypes %d\n", s->bilayerComp.nlipidTypes);
+	for (int x = 0; x < s->bilayerComp.nlipidTypes; x++)
+		fprintf(f, "type %d %s c0 %.17e APL %.17e\n", x, s->bilayerComp.names[x], s->bilayerComp.c0[x], s->bilayerComp.APL[x]);
+	for (int t = 0; t < s->nt; t++) {
+		fprintf(f, "tri %d %d %d %d", t, s->theTriangles[t].ids[0], s->theTriangles[t].ids[1], s->theTriangles[t].ids[2]);
+		for (int x = 0; x < s->bilayerComp.nlipidTypes; x++)
+			fprintf(f, " %.17e %.17e", s->theTriangles[t].composition.outerLeaflet[x], s->theTriangles[t].composition.innerLeaflet[x]);
+		fprintf(f, "\n");
+	}
+	fclose(f);
+
+	/* Final (oriented) neighbour order of every vertex. */
+	f = open_out(pre, "edges.txt", "w");
+	for (int i = 0; i < nv; i++) {
+		fprintf(f, "%d %d", i, s->theVertices[i].valence);
+		for (int e = 0; e < s->theVertices[i].valence; e++) fprintf(f, " %d", s->theVertices[i].edges[e]);
+		fprintf(f, "\n");
+	}
+	fclose(f);
+	printf("E %.17e\n", E);
+	return 0;
+}

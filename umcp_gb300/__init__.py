@@ -1,0 +1,341 @@
+"""GB300 engine for UMCP's membrane-surface hot path.
+
+Python mirror of the reference's `struct surface` call surface over the C ABI
+in include/umcp_gpu.h (ctypes, plain pointers): `Plan` is the host side of
+loadLattice/generatePlan/setg0, `Mesh.energy`/`Mesh.grad` replace
+surface::energy(r, NULL)/surface::grad(r, g) (grad ADDS into g, as the
+reference's does), `Mesh.mass_apply` replaces AltSparseCartMatVecIncrScale
+and `Mesh.run`/`Mesh.step_host` the dynamics loop body of hd.C.
+
+The compute runs only in the CUDA library; if it is missing the import
+fails loudly (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "libumcp_gb300.so"
+
+FP64 = 0
+FP32_CENTRED = 1
+OVERDAMPED_BD = 0
+BD_MEMBRANE = 1
+LANGEVIN = 2
+
+KCAL_MOL_PER_KT_298 = 0.592186663194  # kT at 298 K in kcal/mol (src/hd.C:142)
+
+_STATUS = {
+    0: "ok", 1: "invalid argument", 2: "i/o error", 3: "cuda error", 4: "non-finite energy",
+    5: "device wait timed out", 6: "out of device memory", 7: "unsupported", 8: "diverged",
+}
+
+
+class UmcpError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("kc", C.c_double), ("KA", C.c_double), ("kg", C.c_double), ("k_reg", C.c_double),
+        ("temperature", C.c_double), ("precision", C.c_int), ("lipid_directives", C.c_char_p),
+    ]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [
+        ("nv", C.c_int), ("n_regular", C.c_int), ("n_irregular", C.c_int), ("n_lipid_types", C.c_int),
+        ("box", C.c_double * 9),
+    ]
+
+
+class Integrator(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("time_step", C.c_double), ("gamma", C.c_double), ("D", C.c_double),
+        ("seed", C.c_uint64), ("stream", C.c_uint32), ("divergence_threshold", C.c_double),
+        ("use_mass", C.c_int),
+    ]
+
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_I8 = C.POINTER(C.c_int8)
+_VP = C.c_void_p
+
+# name -> argument types; every function returns umcp_status (int) unless listed in _VOID/_STR.
+_SIGNATURES = {
+    "umcp_params_default": [C.POINTER(Params)],
+    "umcp_params_from_input": [C.c_char_p, C.POINTER(Params), C.c_char_p, C.c_size_t],
+    "umcp_mesh_generate_icosphere": [C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_char_p],
+    "umcp_mesh_generate_planar": [C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_char_p],
+    "umcp_plan_from_file": [C.c_char_p, C.POINTER(Params), C.POINTER(_VP)],
+    "umcp_plan_set_reference": [_VP, _D],
+    "umcp_plan_info_get": [_VP, C.POINTER(PlanInfo)],
+    "umcp_plan_positions": [_VP, _D],
+    "umcp_plan_rings": [_VP, _I, _I],
+    "umcp_plan_faces": [_VP, C.c_int, _I, _I8, _I, _D, _D, _D, _D],
+    "umcp_plan_basis": [_VP, C.c_int, _D, _D, _D, _D],
+    "umcp_plan_lipids": [_VP, _D, _D],
+    "umcp_plan_destroy": [_VP],
+    "umcp_ctx_create": [C.c_int, C.POINTER(_VP)],
+    "umcp_ctx_destroy": [_VP],
+    "umcp_ctx_synchronize": [_VP],
+    "umcp_mesh_create": [_VP, _VP, C.POINTER(Params), C.POINTER(_VP)],
+    "umcp_mesh_destroy": [_VP],
+    "umcp_mesh_set_params": [_VP, C.POINTER(Params)],
+    "umcp_energy": [_VP, _D, _D, _D],
+    "umcp_grad": [_VP, _D, _D],
+    "umcp_energy_grad": [_VP, _D, _D, _D],
+    "umcp_energy_grad_device": [_VP, _VP, _VP, _VP],
+    "umcp_mass_set": [_VP, C.c_int, _I, _I, _D],
+    "umcp_mass_apply": [_VP, _D, _D, _D, C.c_double, _D],
+    "umcp_mass_apply_device": [_VP, _VP, _VP, _VP, C.c_double, _D],
+    "umcp_state_set": [_VP, _D, _D],
+    "umcp_state_get": [_VP, _D, _D],
+    "umcp_run": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int, _D],
+    "umcp_run_async": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int],
+    "umcp_step_host": [_VP, C.POINTER(Integrator), C.c_uint64, _D, _D, _D],
+    "umcp_last_error": [],
+    "umcp_status_string": [C.c_int],
+}
+_VOID = {"umcp_plan_destroy", "umcp_ctx_destroy", "umcp_mesh_destroy"}
+_STR = {"umcp_last_error", "umcp_status_string"}
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """Loads the engine library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"umcp_gb300 engine library missing: {LIB_PATH} (run __graft_entry__.build())")
+        lib = C.CDLL(str(LIB_PATH))
+        for name, args in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = None if name in _VOID else (C.c_char_p if name in _STR else C.c_int)
+        _lib = lib
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGNATURES)
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise UmcpError(status, library().umcp_last_error().decode())
+
+
+def _dp(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_D)
+
+
+def _ip(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_I)
+
+
+def params(kc=14.0, KA=0.215, kg=0.0, k_reg=0.0, temperature=298.0, precision=FP64, lipids: str | None = None) -> Params:
+    p = Params()
+    _check(library().umcp_params_default(C.byref(p)))
+    p.kc, p.KA, p.kg, p.k_reg, p.temperature, p.precision = kc, KA, kg, k_reg, temperature, precision
+    p._lipid_bytes = lipids.encode() if lipids else None  # keep alive
+    p.lipid_directives = p._lipid_bytes
+    return p
+
+
+def kc_from_kT(kc_kT: float, temperature: float = 298.0) -> float:
+    """Bending modulus in kcal/mol for kc given in units of kT (src/hd.C:142-143)."""
+    return kc_kT * KCAL_MOL_PER_KT_298 / 298.0 * temperature
+
+
+def generate_icosphere(path: str | os.PathLike, level: int, R: float, sigma: float, seed: int) -> None:
+    _check(library().umcp_mesh_generate_icosphere(level, R, sigma, seed, str(path).encode()))
+
+
+def generate_planar(path: str | os.PathLike, nx: int, ny: int, a: float, kc_kT: float, seed: int) -> None:
+    _check(library().umcp_mesh_generate_planar(nx, ny, a, kc_kT, seed, str(path).encode()))
+
+
+class Plan:
+    """Host-side plan of one mesh (loadLattice + generatePlan + lipids + setg0)."""
+
+    def __init__(self, mesh_path: str | os.PathLike, prm: Params | None = None):
+        self._h = C.c_void_p()
+        self._prm = prm if prm is not None else params()
+        _check(library().umcp_plan_from_file(str(mesh_path).encode(), C.byref(self._prm), C.byref(self._h)))
+        info = PlanInfo()
+        _check(library().umcp_plan_info_get(self._h, C.byref(info)))
+        self.nv = info.nv
+        self.n_regular = info.n_regular
+        self.n_irregular = info.n_irregular
+        self.n_lipid_types = info.n_lipid_types
+        self.box = np.array(info.box[:], dtype=np.float64).reshape(3, 3)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.umcp_plan_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def positions(self) -> np.ndarray:
+        r = np.zeros(3 * self.nv + 3)
+        _check(library().umcp_plan_positions(self._h, _dp(r)))
+        return r
+
+    def set_reference(self, r: np.ndarray) -> None:
+        _check(library().umcp_plan_set_reference(self._h, _dp(np.ascontiguousarray(r, dtype=np.float64))))
+
+    def rings(self) -> tuple[np.ndarray, np.ndarray]:
+        val = np.zeros(self.nv, dtype=np.int32)
+        _check(library().umcp_plan_rings(self._h, _ip(val), None))
+        ring = np.zeros(int(val.sum()), dtype=np.int32)
+        _check(library().umcp_plan_rings(self._h, None, _ip(ring)))
+        return val, ring
+
+    def faces(self, kind: int) -> dict:
+        nf = self.n_irregular if kind else self.n_regular
+        npt = 16 if kind else 15
+        nt = self.n_lipid_types
+        out = {
+            "cp": np.zeros((nf, 13), dtype=np.int32), "img": np.zeros((nf, 13, 3), dtype=np.int8),
+            "valence": np.zeros(nf, dtype=np.int32), "g0": np.zeros((nf, npt)), "rr0": np.zeros((nf, npt)),
+            "outer": np.zeros((nf, nt)), "inner": np.zeros((nf, nt)),
+        }
+        _check(library().umcp_plan_faces(
+            self._h, kind, _ip(out["cp"]), out["img"].ctypes.data_as(_I8), _ip(out["valence"]), _dp(out["g0"]),
+            _dp(out["rr0"]), _dp(out["outer"]), _dp(out["inner"])))
+        return out
+
+    def basis(self, valence: int) -> dict:
+        npt, ncp = (15, 12) if valence == 6 else (16, valence + 6)
+        rows = np.zeros((6, npt, ncp))
+        w, u, v = np.zeros(npt), np.zeros(npt), np.zeros(npt)
+        _check(library().umcp_plan_basis(self._h, valence, _dp(rows), _dp(w), _dp(u), _dp(v)))
+        return {"rows": rows, "weight": w, "u": u, "v": v}
+
+    def lipids(self) -> tuple[np.ndarray, np.ndarray]:
+        c0, apl = np.zeros(self.n_lipid_types), np.zeros(self.n_lipid_types)
+        _check(library().umcp_plan_lipids(self._h, _dp(c0), _dp(apl)))
+        return c0, apl
+
+
+class Context:
+    """One CUDA device and stream."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        _check(library().umcp_ctx_create(device, C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.umcp_ctx_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self) -> None:
+        _check(library().umcp_ctx_synchronize(self._h))
+
+
+class Mesh:
+    """Device-resident surface; energy/grad mirror surface::energy/grad."""
+
+    def __init__(self, ctx: Context, plan: Plan, prm: Params | None = None):
+        self.ctx = ctx  # keep the context alive
+        self.nv = plan.nv
+        self._prm = prm if prm is not None else plan._prm
+        self._h = C.c_void_p()
+        _check(library().umcp_mesh_create(ctx.handle, plan.handle, C.byref(self._prm), C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.umcp_mesh_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, prm: Params) -> None:
+        self._prm = prm
+        _check(library().umcp_mesh_set_params(self._h, C.byref(prm)))
+
+    def energy(self, r: np.ndarray, terms: bool = False):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        E = C.c_double()
+        t = np.zeros(3)
+        _check(library().umcp_energy(self._h, _dp(r), C.byref(E), _dp(t)))
+        return (E.value, t) if terms else E.value
+
+    def grad(self, r: np.ndarray, g: np.ndarray) -> np.ndarray:
+        """Adds dE/dr into g (3*nv+3), as surface::grad does."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        _check(library().umcp_grad(self._h, _dp(r), _dp(g)))
+        return g
+
+    def energy_grad(self, r: np.ndarray) -> tuple[float, np.ndarray]:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        g = np.zeros(3 * self.nv + 3)
+        E = C.c_double()
+        _check(library().umcp_energy_grad(self._h, _dp(r), C.byref(E), _dp(g)))
+        return E.value, g
+
+    def mass_set(self, row_ptr: np.ndarray, col: np.ndarray, val: np.ndarray) -> None:
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int32)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        val = np.ascontiguousarray(val, dtype=np.float64)
+        _check(library().umcp_mass_set(self._h, len(row_ptr) - 1, _ip(row_ptr), _ip(col), _dp(val)))
+
+    def mass_apply(self, vin: np.ndarray, vout: np.ndarray, scalev: np.ndarray | None = None, scale: float = 1.0,
+                   alphas=(1.0, 1.0, 1.0)) -> np.ndarray:
+        a = np.asarray(alphas, dtype=np.float64)
+        sv = None if scalev is None else np.ascontiguousarray(scalev, dtype=np.float64)
+        _check(library().umcp_mass_apply(self._h, _dp(np.ascontiguousarray(vin, dtype=np.float64)), _dp(vout),
+                                         _dp(sv), scale, _dp(a)))
+        return vout
+
+    def state_set(self, r: np.ndarray, p: np.ndarray | None = None) -> None:
+        _check(library().umcp_state_set(self._h, _dp(np.ascontiguousarray(r, dtype=np.float64)),
+                                        _dp(None if p is None else np.ascontiguousarray(p, dtype=np.float64))))
+
+    def state_get(self) -> tuple[np.ndarray, np.ndarray]:
+        r, p = np.zeros(3 * self.nv + 3), np.zeros(3 * self.nv)
+        _check(library().umcp_state_get(self._h, _dp(r), _dp(p)))
+        return r, p
+
+    def run(self, it: Integrator, step0: int, n_steps: int, energies: bool = True):
+        e = np.zeros(max(n_steps, 1)) if energies else None
+        _check(library().umcp_run(self._h, C.byref(it), step0, n_steps, _dp(e)))
+        return e[:n_steps] if energies else None
+
+    def run_async(self, it: Integrator, step0: int, n_steps: int) -> None:
+        _check(library().umcp_run_async(self._h, C.byref(it), step0, n_steps))
+
+    def step_host(self, it: Integrator, step: int, r: np.ndarray, p: np.ndarray | None = None) -> float:
+        E = C.c_double()
+        _check(library().umcp_step_host(self._h, C.byref(it), step, _dp(r), _dp(p), C.byref(E)))
+        return E.value
+
+
+def integrator(kind=OVERDAMPED_BD, time_step=1.0, gamma=0.0, D=0.0, seed=1, stream=0, divergence_threshold=0.0,
+               use_mass=0) -> Integrator:
+    return Integrator(kind, time_step, gamma, D, seed, stream, divergence_threshold, use_mass)

@@ -1,0 +1,772 @@
+// C ABI of the membrane-surface engine (include/umcp_gpu.h): host plans,
+// device-resident meshes, energy/gradient, effective-mass apply and runs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/umcp_gpu.h"
+#include "launch.h"
+#include "mesh.h"
+#include "plan.h"
+
+using namespace umcp;
+
+static constexpr double kAkmaTime = 1.0 / (0.04888 * 1e-12);  // AKMA_TIME, src/units.h:5
+
+// ------------------------------------------------------------------ errors
+
+static thread_local std::string g_last_error;
+
+static umcp_status fail(umcp_status s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+
+#define UMCP_CUDA(call)                                                                          \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return fail(UMCP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+extern "C" const char *umcp_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char *umcp_status_string(umcp_status s) {
+  switch (s) {
+    case UMCP_OK: return "ok";
+    case UMCP_ERR_INVALID: return "invalid argument";
+    case UMCP_ERR_IO: return "i/o error";
+    case UMCP_ERR_CUDA: return "cuda error";
+    case UMCP_ERR_NONFINITE: return "non-finite energy";
+    case UMCP_ERR_TIMEOUT: return "device wait timed out";
+    case UMCP_ERR_NOMEM: return "out of device memory";
+    case UMCP_ERR_UNSUPPORTED: return "unsupported";
+    case UMCP_ERR_DIVERGED: return "diverged";
+  }
+  return "unknown";
+}
+
+// ------------------------------------------------------------------ params
+
+extern "C" umcp_status umcp_params_default(umcp_params *p) {
+  if (!p) return fail(UMCP_ERR_INVALID, "null params");
+  p->kc = 14.0;      // src/input.C:66
+  p->KA = 0.215;     // src/input.C:64,309-310 (KA -1 resolves to 0.215)
+  p->kg = 0.0;       // src/input.C:67
+  p->k_reg = 0.0;    // src/interpLib.C:87
+  p->temperature = 298.0;  // src/input.C:71
+  p->precision = UMCP_FP64;
+  p->lipid_directives = nullptr;
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_params_from_input(const char *text, umcp_params *p, char *lipid_buf, size_t lipid_len) {
+  if (!text || !p) return fail(UMCP_ERR_INVALID, "null argument");
+  std::istringstream in(text);
+  std::string line, lipids;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::string key;
+    if (!(ls >> key)) continue;
+    std::string lk = key;
+    for (char &c : lk) c = (char)tolower((unsigned char)c);
+    if (lk == "lipid") { lipids += line + "\n"; continue; }
+    double v;
+    if (!(ls >> v)) continue;
+    if (lk == "kc") p->kc = v;
+    else if (lk == "ka") p->KA = (v < 0) ? 0.215 : v;
+    else if (lk == "kg") p->kg = v;
+    else if (lk == "t") p->temperature = v;
+    else if (lk == "k_reg") p->k_reg = v;
+  }
+  if (lipid_buf && lipid_len) {
+    if (lipids.size() + 1 > lipid_len) return fail(UMCP_ERR_INVALID, "lipid buffer too small");
+    memcpy(lipid_buf, lipids.c_str(), lipids.size() + 1);
+    p->lipid_directives = lipid_buf;
+  }
+  return UMCP_OK;
+}
+
+// ------------------------------------------------------------------ mesh generators
+
+extern "C" umcp_status umcp_mesh_generate_icosphere(int level, double R, double sigma, uint64_t seed, const char *path) {
+  if (level < 1 || level > 9 || !(R > 0) || sigma < 0 || !path)
+    return fail(UMCP_ERR_INVALID, "icosphere needs 1 <= level <= 9, R > 0, sigma >= 0");
+  Mesh m;
+  generate_icosphere(level, R, sigma, seed, &m);
+  std::string e = write_mesh(path, m);
+  return e.empty() ? UMCP_OK : fail(UMCP_ERR_IO, e);
+}
+
+extern "C" umcp_status umcp_mesh_generate_planar(int nx, int ny, double a, double kc_kT, uint64_t seed, const char *path) {
+  if (nx < 4 || ny < 4 || !(a > 0) || !(kc_kT > 0) || !path)
+    return fail(UMCP_ERR_INVALID, "planar mesh needs nx, ny >= 4, a > 0, kc > 0");
+  Mesh m;
+  generate_planar(nx, ny, a, kc_kT, seed, &m);
+  std::string e = write_mesh(path, m);
+  return e.empty() ? UMCP_OK : fail(UMCP_ERR_IO, e);
+}
+
+// ------------------------------------------------------------------ plans
+
+struct umcp_plan {
+  Mesh mesh;
+  Plan plan;
+};
+
+extern "C" umcp_status umcp_plan_from_file(const char *mesh_path, const umcp_params *p, umcp_plan **out) {
+  if (!mesh_path || !out) return fail(UMCP_ERR_INVALID, "null argument");
+  auto pl = std::make_unique<umcp_plan>();
+  std::string e = read_mesh(mesh_path, &pl->mesh);
+  if (!e.empty()) return fail(e.find("cannot open") == 0 ? UMCP_ERR_IO : UMCP_ERR_INVALID, e);
+  e = orient(&pl->mesh);
+  if (!e.empty()) return fail(UMCP_ERR_INVALID, e);
+  std::vector<Lipid> lipids;
+  e = parse_lipids((p && p->lipid_directives) ? p->lipid_directives : "", &lipids);
+  if (!e.empty()) return fail(UMCP_ERR_INVALID, e);
+  e = build_plan(pl->mesh, lipids, &pl->plan);
+  if (!e.empty()) return fail(UMCP_ERR_INVALID, e);
+  *out = pl.release();
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_set_reference(umcp_plan *plan, const double *r) {
+  if (!plan || !r) return fail(UMCP_ERR_INVALID, "null argument");
+  set_reference_state(plan->mesh, r, &plan->plan);
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_info_get(const umcp_plan *plan, umcp_plan_info *info) {
+  if (!plan || !info) return fail(UMCP_ERR_INVALID, "null argument");
+  info->nv = plan->mesh.nv;
+  info->n_regular = (int)plan->plan.reg_faces.size();
+  info->n_irregular = (int)plan->plan.irr_faces.size();
+  info->n_lipid_types = plan->plan.ntypes;
+  for (int d = 0; d < 3; ++d)
+    for (int c = 0; c < 3; ++c) info->box[3 * d + c] = plan->mesh.box[d][c];
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_positions(const umcp_plan *plan, double *r) {
+  if (!plan || !r) return fail(UMCP_ERR_INVALID, "null argument");
+  std::copy(plan->mesh.r.begin(), plan->mesh.r.end(), r);
+  r[3 * plan->mesh.nv] = r[3 * plan->mesh.nv + 1] = r[3 * plan->mesh.nv + 2] = 1.0;
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_rings(const umcp_plan *plan, int *valence, int *ring) {
+  if (!plan) return fail(UMCP_ERR_INVALID, "null argument");
+  if (valence) std::copy(plan->mesh.valence.begin(), plan->mesh.valence.end(), valence);
+  if (ring) std::copy(plan->mesh.nbr.begin(), plan->mesh.nbr.end(), ring);
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_faces(const umcp_plan *plan, int kind, int *cp, int8_t *img, int *valence, double *g0,
+                                       double *rr0, double *outer, double *inner) {
+  if (!plan || (kind != 0 && kind != 1)) return fail(UMCP_ERR_INVALID, "bad plan or kind");
+  const Plan &P = plan->plan;
+  const std::vector<Face> &F = kind ? P.irr_faces : P.reg_faces;
+  const int npt = kind ? kIrrPts : kRegPts;
+  for (size_t f = 0; f < F.size(); ++f) {
+    for (int x = 0; x < 13; ++x) {
+      if (cp) cp[f * 13 + x] = (x < F[f].ncp) ? F[f].cp[x] : -1;
+      for (int c = 0; c < 3; ++c)
+        if (img) img[(f * 13 + x) * 3 + c] = (x < F[f].ncp) ? F[f].img[x][c] : 0;
+    }
+    if (valence) valence[f] = F[f].valence;
+  }
+  const std::vector<double> &G0 = kind ? P.irr_g0 : P.reg_g0, &RR = kind ? P.irr_RuRv0 : P.reg_RuRv0;
+  if (g0) std::copy(G0.begin(), G0.end(), g0);
+  if (rr0) std::copy(RR.begin(), RR.end(), rr0);
+  (void)npt;
+  const std::vector<double> &O = kind ? P.irr_outer : P.reg_outer, &I = kind ? P.irr_inner : P.reg_inner;
+  if (outer) std::copy(O.begin(), O.end(), outer);
+  if (inner) std::copy(I.begin(), I.end(), inner);
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_basis(const umcp_plan *plan, int valence, double *rows, double *weight, double *u,
+                                       double *v) {
+  if (!plan) return fail(UMCP_ERR_INVALID, "null plan");
+  PatchBasis tmp;
+  const PatchBasis *B = nullptr;
+  if (valence == 6) B = &plan->plan.regular;
+  else if (valence == 5 || valence == 7) {
+    B = &plan->plan.irregular[valence];
+    if (B->row.empty()) {
+      std::string e = build_irregular_basis(valence, &tmp);
+      if (!e.empty()) return fail(UMCP_ERR_INVALID, e);
+      B = &tmp;
+    }
+  } else
+    return fail(UMCP_ERR_INVALID, "valence must be 5, 6 or 7");
+  if (rows) std::copy(B->row.begin(), B->row.end(), rows);
+  if (weight) std::copy(B->weight.begin(), B->weight.end(), weight);
+  if (u) std::copy(B->u.begin(), B->u.end(), u);
+  if (v) std::copy(B->v.begin(), B->v.end(), v);
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_plan_lipids(const umcp_plan *plan, double *c0, double *apl) {
+  if (!plan) return fail(UMCP_ERR_INVALID, "null plan");
+  for (size_t x = 0; x < plan->plan.lipids.size(); ++x) {
+    if (c0) c0[x] = plan->plan.lipids[x].c0;
+    if (apl) apl[x] = plan->plan.lipids[x].apl;
+  }
+  return UMCP_OK;
+}
+
+extern "C" void umcp_plan_destroy(umcp_plan *plan) { delete plan; }
+
+// ------------------------------------------------------------------ device context
+
+struct umcp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+};
+
+extern "C" umcp_status umcp_ctx_create(int device, umcp_ctx **out) {
+  if (!out) return fail(UMCP_ERR_INVALID, "null out");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(UMCP_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(UMCP_ERR_INVALID, "device index out of range");
+  UMCP_CUDA(cudaSetDevice(device));
+  auto c = std::make_unique<umcp_ctx>();
+  c->device = device;
+  UMCP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  *out = c.release();
+  return UMCP_OK;
+}
+
+extern "C" void umcp_ctx_destroy(umcp_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+extern "C" umcp_status umcp_ctx_synchronize(umcp_ctx *ctx) {
+  if (!ctx) return fail(UMCP_ERR_INVALID, "null ctx");
+  UMCP_CUDA(cudaStreamSynchronize(ctx->stream));
+  return UMCP_OK;
+}
+
+// ------------------------------------------------------------------ device mesh
+
+namespace {
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t alloc(size_t b) {
+    if (p) { cudaFree(p); p = nullptr; }
+    bytes = b;
+    return b ? cudaMalloc(&p, b) : cudaSuccess;
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+struct Group {
+  int ncp = 0, npt = 0, nfaces = 0, face_base = 0, slot_base = 0, irregular = 0;
+  double dudv = 0.5;
+  DevBuf cp, g0, rr0, comp, basis, weight, dest;
+};
+}  // namespace
+
+struct umcp_mesh {
+  umcp_ctx *ctx = nullptr;
+  int nv = 0, nfaces = 0, nslots = 0;
+  int precision = UMCP_FP64;
+  dev::SurfaceParams P{};
+  std::vector<std::unique_ptr<Group>> groups;
+  DevBuf partial, off, terms, seg;
+  DevBuf r, g, p, qdot, E, parts, status, step, runidx;
+  double kT = 0.592186663194;  // kcal/mol at the params' temperature (src/hd.C:142-143)
+  DevBuf energies;
+  size_t energies_cap = 0;
+  double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
+  double *h_stage2 = nullptr; // pinned, 3*nv doubles
+  // effective inverse mass
+  int mrows = 0;
+  DevBuf mrow, mcol, mval, alphas;
+  // graph cache for runs
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  StepArgs graph_args{};
+  int graph_use_mass = -1;
+  double graph_threshold = 0;
+  void *graph_energies = nullptr;
+
+  ~umcp_mesh() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (h_stage) cudaFreeHost(h_stage);
+    if (h_stage2) cudaFreeHost(h_stage2);
+  }
+};
+
+static uint32_t pack_cp(int v, const int8_t img[3]) {
+  int code = (img[0] + 1) + 3 * (img[1] + 1) + 9 * (img[2] + 1);
+  return (uint32_t)v | ((uint32_t)code << dev::kVertexBits);
+}
+
+template <class T>
+static cudaError_t upload(DevBuf &b, const std::vector<T> &h) {
+  cudaError_t e = b.alloc(h.size() * sizeof(T));
+  if (e != cudaSuccess || h.empty()) return e;
+  return cudaMemcpy(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+static constexpr int kGraphChunk = 32;  // steps captured per CUDA graph
+
+static void fill_params(umcp_mesh *m, const umcp_params *p) {
+  m->kT = (5.92186663194E-01 / 298.0) * p->temperature;
+  m->P.kc = p->kc;
+  m->P.KA = p->KA;
+  m->P.kg = p->kg;
+  m->P.k_reg = p->k_reg;
+}
+
+extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, const umcp_params *prm, umcp_mesh **out) {
+  if (!ctx || !plan || !out) return fail(UMCP_ERR_INVALID, "null argument");
+  umcp_params defaults;
+  umcp_params_default(&defaults);
+  if (!prm) prm = &defaults;
+  if (prm->precision != UMCP_FP64 && prm->precision != UMCP_FP32_CENTRED)
+    return fail(UMCP_ERR_INVALID, "unknown precision");
+  UMCP_CUDA(cudaSetDevice(ctx->device));
+  auto m = std::make_unique<umcp_mesh>();
+  m->ctx = ctx;
+  m->precision = prm->precision;
+  const Plan &PL = plan->plan;
+  const Mesh &ME = plan->mesh;
+  m->nv = ME.nv;
+  m->P.nv = ME.nv;
+  for (int d = 0; d < 3; ++d)
+    for (int c = 0; c < 3; ++c) m->P.box[d][c] = ME.box[d][c];
+  fill_params(m.get(), prm);
+
+  // Face groups: regular, then irregular by valence (5, 7).
+  struct Src { const PatchBasis *B; std::vector<int> idx; bool irr; };
+  std::vector<Src> srcs;
+  {
+    Src s{&PL.regular, {}, false};
+    for (size_t f = 0; f < PL.reg_faces.size(); ++f) s.idx.push_back((int)f);
+    srcs.push_back(s);
+    for (int val : {5, 7}) {
+      Src t{&PL.irregular[val], {}, true};
+      for (size_t f = 0; f < PL.irr_faces.size(); ++f)
+        if (PL.irr_faces[f].valence == val) t.idx.push_back((int)f);
+      if (!t.idx.empty()) srcs.push_back(t);
+    }
+  }
+  const int nt = PL.ntypes;
+  std::vector<std::vector<int>> vslots(ME.nv);  // slots touching each vertex, ascending
+  int face_base = 0, slot_base = 0;
+  for (const Src &s : srcs) {
+    auto G = std::make_unique<Group>();
+    const PatchBasis &B = *s.B;
+    G->ncp = B.ncp;
+    G->npt = B.npt;
+    G->nfaces = (int)s.idx.size();
+    G->face_base = face_base;
+    G->slot_base = slot_base;
+    G->irregular = s.irr;
+    G->dudv = s.irr ? 1.0 : 0.5;
+    std::vector<uint32_t> cp((size_t)G->nfaces * G->ncp);
+    std::vector<double> g0((size_t)G->nfaces * G->npt), rr0((size_t)G->nfaces * G->npt), comp((size_t)G->nfaces * 3);
+    for (int q = 0; q < G->nfaces; ++q) {
+      int f = s.idx[q];
+      const Face &F = s.irr ? PL.irr_faces[f] : PL.reg_faces[f];
+      for (int x = 0; x < G->ncp; ++x) {
+        cp[(size_t)q * G->ncp + x] = pack_cp(F.cp[x], F.img[x]);
+        vslots[F.cp[x]].push_back(slot_base + q * G->ncp + x);
+      }
+      const std::vector<double> &G0 = s.irr ? PL.irr_g0 : PL.reg_g0, &RR = s.irr ? PL.irr_RuRv0 : PL.reg_RuRv0;
+      for (int p = 0; p < G->npt; ++p) {
+        g0[(size_t)q * G->npt + p] = G0[(size_t)f * G->npt + p];
+        rr0[(size_t)q * G->npt + p] = RR[(size_t)f * G->npt + p];
+      }
+      const double *O = &(s.irr ? PL.irr_outer : PL.reg_outer)[(size_t)f * nt];
+      const double *I = &(s.irr ? PL.irr_inner : PL.reg_inner)[(size_t)f * nt];
+      composition_coeffs(O, I, PL.lipids, &comp[3 * q], &comp[3 * q + 1], &comp[3 * q + 2]);
+    }
+    // basis rows u,v,uu,uv,vv as [kind][cp][pt]
+    std::vector<double> basis((size_t)5 * G->ncp * G->npt);
+    for (int k = 0; k < 5; ++k)
+      for (int x = 0; x < G->ncp; ++x)
+        for (int p = 0; p < G->npt; ++p) basis[((size_t)k * G->ncp + x) * G->npt + p] = B.at(k + 1, p, x);
+    UMCP_CUDA(upload(G->cp, cp));
+    UMCP_CUDA(upload(G->g0, g0));
+    UMCP_CUDA(upload(G->rr0, rr0));
+    UMCP_CUDA(upload(G->comp, comp));
+    UMCP_CUDA(upload(G->basis, basis));
+    UMCP_CUDA(upload(G->weight, B.weight));
+    face_base += G->nfaces;
+    slot_base += G->nfaces * G->ncp;
+    m->groups.push_back(std::move(G));
+  }
+  m->nfaces = face_base;
+  m->nslots = slot_base;
+  // Vertex-major destination of every (face, control point) slot.
+  std::vector<int> off(ME.nv + 1, 0), dest(slot_base, -1);
+  for (int v = 0; v < ME.nv; ++v) off[v + 1] = off[v] + (int)vslots[v].size();
+  for (int v = 0; v < ME.nv; ++v)
+    for (size_t k = 0; k < vslots[v].size(); ++k) dest[vslots[v][k]] = off[v] + (int)k;
+  for (auto &G : m->groups) {
+    std::vector<int> d(dest.begin() + G->slot_base, dest.begin() + G->slot_base + (size_t)G->nfaces * G->ncp);
+    UMCP_CUDA(upload(G->dest, d));
+  }
+  UMCP_CUDA(upload(m->off, off));
+  std::vector<int> seg = {0, m->nfaces};
+  UMCP_CUDA(upload(m->seg, seg));
+  const size_t elem = (m->precision == UMCP_FP64) ? sizeof(double) : sizeof(float);
+  UMCP_CUDA(m->partial.alloc((size_t)slot_base * 3 * elem));
+  UMCP_CUDA(m->terms.alloc((size_t)m->nfaces * 6 * sizeof(double)));
+  const size_t nst = 3 * (size_t)ME.nv + 3;
+  UMCP_CUDA(m->r.alloc(nst * sizeof(double)));
+  UMCP_CUDA(m->g.alloc(nst * sizeof(double)));
+  UMCP_CUDA(m->p.alloc(3 * (size_t)ME.nv * sizeof(double)));
+  UMCP_CUDA(m->qdot.alloc(3 * (size_t)ME.nv * sizeof(double)));
+  UMCP_CUDA(m->E.alloc(sizeof(double)));
+  UMCP_CUDA(m->parts.alloc(3 * sizeof(double)));
+  UMCP_CUDA(m->status.alloc(sizeof(int)));
+  UMCP_CUDA(m->step.alloc(sizeof(uint64_t)));
+  UMCP_CUDA(m->runidx.alloc(sizeof(uint64_t)));
+  UMCP_CUDA(m->alphas.alloc(3 * sizeof(double)));
+  UMCP_CUDA(cudaMemset(m->p.p, 0, m->p.bytes));
+  UMCP_CUDA(cudaMemset(m->status.p, 0, sizeof(int)));
+  UMCP_CUDA(cudaMallocHost(&m->h_stage, nst * sizeof(double)));
+  UMCP_CUDA(cudaMallocHost(&m->h_stage2, 3 * (size_t)ME.nv * sizeof(double)));
+  // Initial state: the plan's positions, alpha = 1.
+  std::vector<double> r0(nst);
+  std::copy(ME.r.begin(), ME.r.end(), r0.begin());
+  r0[3 * ME.nv] = r0[3 * ME.nv + 1] = r0[3 * ME.nv + 2] = 1.0;
+  UMCP_CUDA(cudaMemcpy(m->r.p, r0.data(), nst * sizeof(double), cudaMemcpyHostToDevice));
+  *out = m.release();
+  return UMCP_OK;
+}
+
+extern "C" void umcp_mesh_destroy(umcp_mesh *mesh) {
+  if (!mesh) return;
+  cudaSetDevice(mesh->ctx->device);
+  cudaStreamSynchronize(mesh->ctx->stream);
+  delete mesh;
+}
+
+extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *p) {
+  if (!mesh || !p) return fail(UMCP_ERR_INVALID, "null argument");
+  fill_params(mesh, p);
+  if (mesh->graph) { cudaGraphExecDestroy(mesh->graph); mesh->graph = nullptr; }
+  return UMCP_OK;
+}
+
+// Queue energy+gradient of state d_r: E -> d_E (and parts), gradient ADDED
+// into d_g (3*nv+3). d_g may be null to skip the gather.
+template <typename T>
+static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g) {
+  cudaStream_t s = m->ctx->stream;
+  for (auto &G : m->groups) {
+    dev::FaceLaunch L;
+    L.nfaces = G->nfaces;
+    L.face_base = G->face_base;
+    L.slot_base = G->slot_base;
+    L.cp = G->cp.as<uint32_t>();
+    L.g0 = G->g0.as<double>();
+    L.rr0 = G->rr0.as<double>();
+    L.comp = G->comp.as<double>();
+    L.basis = G->basis.as<double>();
+    L.weight = G->weight.as<double>();
+    L.dudv = G->dudv;
+    L.irregular = G->irregular;
+    cudaError_t e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->partial.as<T>(),
+                                    m->terms.as<double>(), m->status.as<int>(), 0, s);
+    if (e != cudaSuccess) return e;
+  }
+  if (d_g) {
+    cudaError_t e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), d_g, s);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_reduce_terms(1, m->seg.as<int>(), m->terms.as<double>(), d_E, d_parts, d_g ? d_g + 3 * m->nv : nullptr,
+                             s);
+}
+
+static cudaError_t queue_eg(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g) {
+  return (m->precision == UMCP_FP64) ? queue_energy_grad<double>(m, d_r, d_E, d_parts, d_g)
+                                     : queue_energy_grad<float>(m, d_r, d_E, d_parts, d_g);
+}
+
+static umcp_status check_status(umcp_mesh *m) {
+  int st = 0;
+  UMCP_CUDA(cudaMemcpyAsync(&st, m->status.p, sizeof(int), cudaMemcpyDeviceToHost, m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  if (st & kStatusNonFinite) return fail(UMCP_ERR_NONFINITE, "non-finite energy (the reference stops with \"nan en.\")");
+  if (st & kStatusDiverged) return fail(UMCP_ERR_DIVERGED, "energy rose above the divergence threshold");
+  return UMCP_OK;
+}
+
+static umcp_status host_energy_grad(umcp_mesh *m, const double *r, double *E, double *terms, double *g) {
+  if (!m || !r) return fail(UMCP_ERR_INVALID, "null argument");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t s = m->ctx->stream;
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  memcpy(m->h_stage, r, nst * sizeof(double));
+  UMCP_CUDA(cudaMemcpyAsync(m->r.p, m->h_stage, nst * sizeof(double), cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), s));
+  if (g) UMCP_CUDA(cudaMemsetAsync(m->g.p, 0, nst * sizeof(double), s));
+  UMCP_CUDA(queue_eg(m, m->r.as<double>(), m->E.as<double>(), m->parts.as<double>(), g ? m->g.as<double>() : nullptr));
+  double e_parts[4];
+  UMCP_CUDA(cudaMemcpyAsync(&e_parts[0], m->E.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaMemcpyAsync(&e_parts[1], m->parts.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (g) UMCP_CUDA(cudaMemcpyAsync(m->h_stage, m->g.p, nst * sizeof(double), cudaMemcpyDeviceToHost, s));
+  umcp_status st = check_status(m);  // synchronizes
+  if (E) *E = e_parts[0];
+  if (terms) { terms[0] = e_parts[1]; terms[1] = e_parts[2]; terms[2] = e_parts[3]; }
+  if (g)
+    for (size_t i = 0; i < nst; ++i) g[i] += m->h_stage[i];
+  return st;
+}
+
+extern "C" umcp_status umcp_energy(umcp_mesh *mesh, const double *r, double *E, double *terms) {
+  return host_energy_grad(mesh, r, E, terms, nullptr);
+}
+extern "C" umcp_status umcp_grad(umcp_mesh *mesh, const double *r, double *g) {
+  if (!g) return fail(UMCP_ERR_INVALID, "null gradient");
+  return host_energy_grad(mesh, r, nullptr, nullptr, g);
+}
+extern "C" umcp_status umcp_energy_grad(umcp_mesh *mesh, const double *r, double *E, double *g) {
+  return host_energy_grad(mesh, r, E, nullptr, g);
+}
+
+extern "C" umcp_status umcp_energy_grad_device(umcp_mesh *m, const double *d_r, double *d_E, double *d_g) {
+  if (!m || !d_r) return fail(UMCP_ERR_INVALID, "null argument");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(queue_eg(m, d_r, d_E ? d_E : m->E.as<double>(), m->parts.as<double>(), d_g));
+  return UMCP_OK;
+}
+
+// ------------------------------------------------------------------ effective mass
+
+extern "C" umcp_status umcp_mass_set(umcp_mesh *m, int nrow, const int *row_ptr, const int *col, const double *val) {
+  if (!m || !row_ptr || !col || !val || nrow != m->nv) return fail(UMCP_ERR_INVALID, "mass matrix must have nv rows");
+  int nnz = row_ptr[nrow];
+  for (int i = 0; i < nrow; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return fail(UMCP_ERR_INVALID, "row_ptr not monotone");
+  for (int k = 0; k < nnz; ++k)
+    if (col[k] < 0 || col[k] >= m->nv) return fail(UMCP_ERR_INVALID, "column index out of range");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(upload(m->mrow, std::vector<int>(row_ptr, row_ptr + nrow + 1)));
+  UMCP_CUDA(upload(m->mcol, std::vector<int>(col, col + nnz)));
+  UMCP_CUDA(upload(m->mval, std::vector<double>(val, val + nnz)));
+  m->mrows = nrow;
+  if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_mass_apply_device(umcp_mesh *m, const double *d_in, double *d_out, const double *d_scalev,
+                                              double scale, const double *alphas) {
+  if (!m || !d_in || !d_out) return fail(UMCP_ERR_INVALID, "null argument");
+  if (!m->mrows) return fail(UMCP_ERR_INVALID, "no mass matrix installed");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  double a[3] = {1, 1, 1};
+  if (alphas) { a[0] = alphas[0]; a[1] = alphas[1]; a[2] = alphas[2]; }
+  UMCP_CUDA(cudaMemcpyAsync(m->alphas.p, a, sizeof a, cudaMemcpyHostToDevice, m->ctx->stream));
+  UMCP_CUDA(launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), d_scalev, scale,
+                        m->alphas.as<double>(), d_in, d_out, 1, m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_mass_apply(umcp_mesh *m, const double *in, double *out, const double *scalev, double scale,
+                                       const double *alphas) {
+  if (!m || !in || !out) return fail(UMCP_ERR_INVALID, "null argument");
+  if (!m->mrows) return fail(UMCP_ERR_INVALID, "no mass matrix installed");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t s = m->ctx->stream;
+  const size_t n3 = 3 * (size_t)m->nv;
+  DevBuf din, dout, dsc;
+  UMCP_CUDA(din.alloc(n3 * sizeof(double)));
+  UMCP_CUDA(dout.alloc(n3 * sizeof(double)));
+  UMCP_CUDA(cudaMemcpyAsync(din.p, in, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(cudaMemcpyAsync(dout.p, out, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (scalev) {
+    UMCP_CUDA(dsc.alloc(n3 * sizeof(double)));
+    UMCP_CUDA(cudaMemcpyAsync(dsc.p, scalev, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  double a[3] = {1, 1, 1};
+  if (alphas) { a[0] = alphas[0]; a[1] = alphas[1]; a[2] = alphas[2]; }
+  UMCP_CUDA(cudaMemcpyAsync(m->alphas.p, a, sizeof a, cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(),
+                        scalev ? dsc.as<double>() : nullptr, scale, m->alphas.as<double>(), din.as<double>(),
+                        dout.as<double>(), 1, s));
+  UMCP_CUDA(cudaMemcpyAsync(out, dout.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaStreamSynchronize(s));
+  return UMCP_OK;
+}
+
+// ------------------------------------------------------------------ dynamics
+
+
+extern "C" umcp_status umcp_state_set(umcp_mesh *m, const double *r, const double *p) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  if (r) UMCP_CUDA(cudaMemcpyAsync(m->r.p, r, nst * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
+  if (p) UMCP_CUDA(cudaMemcpyAsync(m->p.p, p, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
+  else UMCP_CUDA(cudaMemsetAsync(m->p.p, 0, (nst - 3) * sizeof(double), m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_state_get(umcp_mesh *m, double *r, double *p) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  if (r) UMCP_CUDA(cudaMemcpyAsync(r, m->r.p, nst * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+  if (p) UMCP_CUDA(cudaMemcpyAsync(p, m->p.p, (nst - 3) * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return UMCP_OK;
+}
+
+static umcp_status make_step_args(umcp_mesh *m, const umcp_integrator *it, StepArgs *a) {
+  if (it->kind < 0 || it->kind > 2) return fail(UMCP_ERR_INVALID, "unknown integrator kind");
+  if (!(it->time_step > 0)) return fail(UMCP_ERR_INVALID, "time_step must be positive");
+  if (it->use_mass && !m->mrows) return fail(UMCP_ERR_INVALID, "use_mass set but no mass matrix installed");
+  if (it->kind == 0 && !(it->D > 0)) return fail(UMCP_ERR_INVALID, "overdamped BD needs D > 0");
+  if (it->kind != 0 && !(it->gamma > 0)) return fail(UMCP_ERR_INVALID, "leapfrog integrators need gamma > 0");
+  *a = StepArgs{};
+  a->kind = it->kind;
+  a->seed = it->seed;
+  a->stream = it->stream;
+  a->gamma = it->gamma;
+  a->AK = kAkmaTime * it->time_step;
+  if (it->kind == 0) {
+    a->mob_dt = it->D * it->time_step / m->kT;
+    a->sigma = std::sqrt(2.0 * it->D * it->time_step);
+  } else {
+    a->sigma = std::sqrt(2.0 * it->gamma * m->kT * a->AK);
+  }
+  return UMCP_OK;
+}
+
+// One step on the resident state: energy+gradient at r(t), then the update.
+static cudaError_t queue_step(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold) {
+  cudaStream_t s = m->ctx->stream;
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  cudaError_t e = cudaMemsetAsync(m->g.p, 0, nst * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  e = queue_eg(m, m->r.as<double>(), m->E.as<double>(), m->parts.as<double>(), m->g.as<double>());
+  if (e != cudaSuccess) return e;
+  e = launch_record_energy(m->E.as<double>(), m->energies.as<double>(), m->runidx.as<uint64_t>(), threshold,
+                           m->status.as<int>(), s);
+  if (e != cudaSuccess) return e;
+  if (a.kind == 0 || !use_mass) {
+    e = launch_step_local(m->nv, a, m->step.as<uint64_t>(), m->r.as<double>(), m->p.as<double>(), m->g.as<double>(),
+                          m->status.as<int>(), s);
+  } else {
+    e = launch_kick(m->nv, a, m->step.as<uint64_t>(), m->p.as<double>(), m->g.as<double>(), m->status.as<int>(), s);
+    if (e == cudaSuccess)
+      e = launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), nullptr, 1.0, nullptr,
+                      m->p.as<double>(), m->qdot.as<double>(), 0, s);
+    if (e == cudaSuccess)
+      e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->status.as<int>(), s);
+  }
+  if (e != cudaSuccess) return e;
+  return launch_advance_step(m->step.as<uint64_t>(), m->runidx.as<uint64_t>(), s);
+}
+
+static bool same_args(const StepArgs &x, const StepArgs &y) { return memcmp(&x, &y, sizeof(StepArgs)) == 0; }
+
+static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t step0, int n_steps) {
+  cudaStream_t s = m->ctx->stream;
+  StepArgs a;
+  umcp_status st = make_step_args(m, it, &a);
+  if (st != UMCP_OK) return st;
+  if ((size_t)n_steps > m->energies_cap) {
+    if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
+    UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
+    m->energies_cap = (size_t)n_steps;
+  }
+  UMCP_CUDA(cudaMemcpyAsync(m->step.p, &step0, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(cudaMemsetAsync(m->runidx.p, 0, sizeof(uint64_t), s));
+  UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), s));
+  const int use_mass = (it->kind != 0 && it->use_mass) ? 1 : 0;
+  const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
+  if (full > 0) {
+    if (m->graph && (!same_args(a, m->graph_args) || m->graph_use_mass != use_mass ||
+                     m->graph_threshold != it->divergence_threshold)) {
+      cudaGraphExecDestroy(m->graph);
+      m->graph = nullptr;
+    }
+    if (!m->graph) {
+      cudaGraph_t g;
+      UMCP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaSuccess;
+      for (int i = 0; i < kGraphChunk && e == cudaSuccess; ++i) e = queue_step(m, a, use_mass, it->divergence_threshold);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e));
+      if (e2 != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+      e = cudaGraphInstantiate(&m->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { m->graph = nullptr; return fail(UMCP_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e)); }
+      m->graph_args = a;
+      m->graph_use_mass = use_mass;
+      m->graph_threshold = it->divergence_threshold;
+    }
+    for (int c = 0; c < full; ++c) UMCP_CUDA(cudaGraphLaunch(m->graph, s));
+  }
+  for (int i = 0; i < rem; ++i) UMCP_CUDA(queue_step(m, a, use_mass, it->divergence_threshold));
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_run(umcp_mesh *m, const umcp_integrator *it, uint64_t step0, int n_steps, double *energies) {
+  if (!m || !it || n_steps < 0) return fail(UMCP_ERR_INVALID, "bad argument");
+  if (n_steps == 0) return UMCP_OK;
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  umcp_status st = run_steps(m, it, step0, n_steps);
+  if (st != UMCP_OK) return st;
+  if (energies)
+    UMCP_CUDA(cudaMemcpyAsync(energies, m->energies.p, (size_t)n_steps * sizeof(double), cudaMemcpyDeviceToHost,
+                              m->ctx->stream));
+  return check_status(m);
+}
+
+extern "C" umcp_status umcp_run_async(umcp_mesh *m, const umcp_integrator *it, uint64_t step0, int n_steps) {
+  if (!m || !it || n_steps < 0) return fail(UMCP_ERR_INVALID, "bad argument");
+  if (n_steps == 0) return UMCP_OK;
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  return run_steps(m, it, step0, n_steps);
+}
+
+extern "C" umcp_status umcp_step_host(umcp_mesh *m, const umcp_integrator *it, uint64_t step, double *r, double *p,
+                                      double *E) {
+  if (!m || !it || !r) return fail(UMCP_ERR_INVALID, "null argument");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t s = m->ctx->stream;
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  memcpy(m->h_stage, r, nst * sizeof(double));
+  UMCP_CUDA(cudaMemcpyAsync(m->r.p, m->h_stage, nst * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (p) {
+    memcpy(m->h_stage2, p, (nst - 3) * sizeof(double));
+    UMCP_CUDA(cudaMemcpyAsync(m->p.p, m->h_stage2, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  umcp_status st = run_steps(m, it, step, 1);
+  if (st != UMCP_OK) return st;
+  double e = 0;
+  UMCP_CUDA(cudaMemcpyAsync(m->h_stage, m->r.p, nst * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (p) UMCP_CUDA(cudaMemcpyAsync(m->h_stage2, m->p.p, (nst - 3) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaMemcpyAsync(&e, m->E.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  st = check_status(m);
+  memcpy(r, m->h_stage, nst * sizeof(double));
+  if (p) memcpy(p, m->h_stage2, (nst - 3) * sizeof(double));
+  if (E) *E = e;
+  return st;
+}

@@ -1,0 +1,124 @@
+// Device kernels of the membrane-surface hot path (sm_103a).
+//
+// face_kernel     one half-warp per face: lanes are quadrature points while
+//                 the five basis contractions and the pointwise energy and
+//                 adjoint are formed, then lanes are control points while the
+//                 adjoint is contracted back onto the one-ring. Writes per-face
+//                 gradient partials and per-face energy terms; no atomics.
+// gather_kernel   per vertex, sums its face partials in a fixed order (CSR of
+//                 (face, slot) references), optionally fused with an
+//                 integrator update.
+// reduce_kernel   per mesh, fixed-order tree sum of the per-face terms.
+//
+// The energy model is the reference's surface::fenergy/ifenergy with
+// FIXED_A and LOCAL_LIPID_ENERGY (src/interpLib.C:3426-3881); the gradient
+// is its exact derivative (src/grad.C:65-942, 6445-7457), written here in
+// closed form: with m = Ru x Rv, W = |m|^2, l = m.Suu, k = m.Suv, n = m.Svv,
+//   H = c1 + c2 = -(l Rv.Rv - 2 k Ru.Rv + n Ru.Ru) / W^(3/2)
+//   K = c1 c2   = (l n - k^2) / W^2 - SAFETY/4
+// which the reference reaches through the shape-operator eigenvalues.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace umcp {
+namespace dev {
+
+constexpr int kVertexBits = 27;  // packed control point: vertex | image_code << 27
+constexpr uint32_t kVertexMask = (1u << kVertexBits) - 1u;
+constexpr double kSafety = 1e-12;  // SAFETY, src/interp.h:14
+
+struct SurfaceParams {
+  double kc, KA, kg, k_reg;
+  double box[3][3];
+  int nv;
+};
+
+// Per-mesh view for a face launch.
+struct FaceLaunch {
+  int nfaces;              // faces in this launch
+  int face_base;           // index of the first face in the mesh's face numbering (for terms)
+  int slot_base;           // first partial slot (in units of 3 values) of face 0
+  const uint32_t *cp;      // [nfaces][ncp] packed control points
+  const double *g0;        // [nfaces][npt]
+  const double *rr0;       // [nfaces][npt]
+  const double *comp;      // [nfaces][3]: P2, Hbar, Pres
+  const double *basis;     // [5][ncp][npt] rows u,v,uu,uv,vv (global, staged to shared)
+  const double *weight;    // [npt]
+  double dudv;
+  int irregular;
+};
+
+template <typename T>
+struct Vec3 {
+  T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ Vec3<T> cross(const Vec3<T> &a, const Vec3<T> &b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename T>
+__device__ __forceinline__ T dot(const Vec3<T> &a, const Vec3<T> &b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// Pointwise energy and adjoint at one quadrature point. Returns energy parts
+// (area, curvature, angle) and writes dE/d{Ru,Rv,Suu,Suv,Svv} into Kb, and
+// the angle-term part of dE/d{Ru,Rv} into Kreg (needed only for the box-scale
+// derivative on irregular faces, src/grad.C:7414-7421).
+template <typename T>
+__device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T rr0, T dudv, T P2, T Hbar, T Pres,
+                                              T kc, T KA, T kg, T k_reg, T *ea, T *ec, T *er, Vec3<T> Kb[5],
+                                              Vec3<T> Kreg[2]) {
+  const Vec3<T> &Ru = K[0], &Rv = K[1], &Suu = K[2], &Suv = K[3], &Svv = K[4];
+  Vec3<T> m = cross(Ru, Rv);
+  T W = dot(m, m);
+  T E11 = dot(Ru, Ru), E12 = dot(Ru, Rv), E22 = dot(Rv, Rv);
+  T l = dot(m, Suu), k = dot(m, Suv), n = dot(m, Svv);
+  T g = sqrt(W);
+  T iW = T(1) / W;
+  T ig3 = iW / g;  // W^-3/2
+  T Tt = l * E22 - T(2) * k * E12 + n * E11;
+  T Q = l * n - k * k;
+  T H = -Tt * ig3;
+  T Kg = Q * iW * iW - T(kSafety * 0.25);
+  T dH = H - Hbar;
+  T sEE = sqrt(E11 * E22);
+  T val = E12 / sEE;
+  T dv = val - rr0;
+  T dg = g - g0;
+  *ec = T(0.25) * kc * w * (P2 * dH * dH + Pres) + dudv * g0 * w * kg * Kg;
+  *ea = dudv * w * KA * dg * dg / g0;
+  *er = k_reg * dv * dv;
+  // adjoints
+  T Hb = T(0.5) * kc * w * P2 * dH;
+  T Kb_ = dudv * g0 * w * kg;
+  T gb = T(2) * dudv * w * KA * dg / g0;
+  T vb = T(2) * k_reg * dv;
+  T Tb = -Hb * ig3;
+  T Qb = Kb_ * iW * iW;
+  T Wb = Hb * T(1.5) * Tt * ig3 * iW - T(2) * Kb_ * Q * iW * iW * iW + gb / (T(2) * g);
+  T lb = Tb * E22 + Qb * n;
+  T kb = T(-2) * Tb * E12 - T(2) * Qb * k;
+  T nb = Tb * E11 + Qb * l;
+  T rE11 = T(-0.5) * vb * val / E11, rE12 = vb / sEE, rE22 = T(-0.5) * vb * val / E22;
+  T E11b = Tb * n + rE11;
+  T E12b = T(-2) * Tb * k + rE12;
+  T E22b = Tb * l + rE22;
+  Kb[2] = {lb * m.x, lb * m.y, lb * m.z};
+  Kb[3] = {kb * m.x, kb * m.y, kb * m.z};
+  Kb[4] = {nb * m.x, nb * m.y, nb * m.z};
+  Vec3<T> mb = {lb * Suu.x + kb * Suv.x + nb * Svv.x + T(2) * Wb * m.x,
+                lb * Suu.y + kb * Suv.y + nb * Svv.y + T(2) * Wb * m.y,
+                lb * Suu.z + kb * Suv.z + nb * Svv.z + T(2) * Wb * m.z};
+  Vec3<T> a = cross(Rv, mb), b = cross(mb, Ru);
+  Kb[0] = {T(2) * E11b * Ru.x + E12b * Rv.x + a.x, T(2) * E11b * Ru.y + E12b * Rv.y + a.y,
+           T(2) * E11b * Ru.z + E12b * Rv.z + a.z};
+  Kb[1] = {T(2) * E22b * Rv.x + E12b * Ru.x + b.x, T(2) * E22b * Rv.y + E12b * Ru.y + b.y,
+           T(2) * E22b * Rv.z + E12b * Ru.z + b.z};
+  Kreg[0] = {T(2) * rE11 * Ru.x + rE12 * Rv.x, T(2) * rE11 * Ru.y + rE12 * Rv.y, T(2) * rE11 * Ru.z + rE12 * Rv.z};
+  Kreg[1] = {T(2) * rE22 * Rv.x + rE12 * Ru.x, T(2) * rE22 * Rv.y + rE12 * Ru.y, T(2) * rE22 * Rv.z + rE12 * Ru.z};
+}
+
+}  // namespace dev
+}  // namespace umcp
