@@ -109,6 +109,9 @@ void umcp_plan_destroy(umcp_plan *plan);
 umcp_status umcp_ctx_create(int device, umcp_ctx **out);
 void umcp_ctx_destroy(umcp_ctx *ctx);
 umcp_status umcp_ctx_synchronize(umcp_ctx *ctx);
+/* The cudaStream_t (as void*) every call on this ctx is queued on, so a
+ * caller can order its own work (timing events, copies) with the engine's. */
+umcp_status umcp_ctx_stream(umcp_ctx *ctx, void **stream);
 
 /* Upload a plan; the mesh keeps its own state buffers on the device. */
 umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, const umcp_params *p, umcp_mesh **out);
@@ -124,6 +127,19 @@ umcp_status umcp_grad(umcp_mesh *mesh, const double *r, double *g);
 umcp_status umcp_energy_grad(umcp_mesh *mesh, const double *r, double *E, double *g);
 /* Device-pointer form: d_r, d_g hold 3*nv+3 doubles; d_E one double; g accumulated. */
 umcp_status umcp_energy_grad_device(umcp_mesh *mesh, const double *d_r, double *d_E, double *d_g);
+/* Queues only the per-face pass (quadrature, pointwise energy and adjoint,
+ * per-face gradient partials) on the mesh's resident state, without the
+ * per-vertex gather or the sums: the unit a roofline measurement times. */
+umcp_status umcp_face_pass(umcp_mesh *mesh);
+
+/* Work sizes of a mesh: faces, quadrature points, gradient partial slots,
+ * and kernels queued per integrator step (with and without a mass matrix). */
+typedef struct {
+  int nv, n_faces, n_points, n_slots;
+  int kernels_per_step, kernels_per_step_mass;
+  int precision;
+} umcp_mesh_info;
+umcp_status umcp_mesh_info_get(const umcp_mesh *mesh, umcp_mesh_info *info);
 
 /* ---- effective mass ---------------------------------------------------- */
 /* Install M^-1 as a CSR matrix over vertices (SparseMatrix nzl/nzv rows,

@@ -53,6 +53,10 @@ def lib() -> C.CDLL:
         L.oracle_energy.restype = C.c_double
         L.oracle_grad.argtypes = [C.POINTER(OracleSurface), _D, _D]
         L.oracle_grad.restype = None
+        L.oracle_energy_faces.argtypes = [C.POINTER(OracleSurface), _D, C.c_int, C.c_int]
+        L.oracle_energy_faces.restype = C.c_double
+        L.oracle_grad_faces.argtypes = [C.POINTER(OracleSurface), _D, _D, C.c_int, C.c_int]
+        L.oracle_grad_faces.restype = None
         L.oracle_sparse_apply.argtypes = [C.c_int, _I, _I, _D, _D, C.c_double, _D, _D, _D]
         L.oracle_sparse_apply.restype = None
         L.oracle_step.argtypes = [C.POINTER(StepParams), C.c_int, _D, _D, _D, _D]
@@ -117,6 +121,17 @@ class Oracle:
         if per_face:
             out.append(fe)
         return out[0] if len(out) == 1 else tuple(out)
+
+    @property
+    def n_faces(self) -> int:
+        return self.s.nreg + self.s.nirr
+
+    def energy_grad_faces(self, r, f0, f1, g):
+        """Energy of faces [f0, f1) and their gradient added into g."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        e = lib().oracle_energy_faces(C.byref(self.s), _d(r), f0, f1)
+        lib().oracle_grad_faces(C.byref(self.s), _d(r), _d(g), f0, f1)
+        return e
 
     def grad(self, r, g=None):
         r = np.ascontiguousarray(r, dtype=np.float64)

@@ -97,11 +97,10 @@ static void contract(const face_view *F, double Xs[][3], int pt, double K[5][3])
 	}
 }
 
-double oracle_energy(const oracle_surface *s, const double *r, double *terms, double *face_e)
+static double energy_range(const oracle_surface *s, const double *r, double *terms, double *face_e, int f0, int f1)
 {
 	double VA = 0, VC = 0, VR = 0, E = 0;
-	const int nfaces = s->nreg + s->nirr;
-	for (int f = 0; f < nfaces; f++) {
+	for (int f = f0; f < f1; f++) {
 		face_view F = face_at(s, f);
 		double X[13][3], Xs[13][3];
 		control_points(s, r, &F, X, Xs);
@@ -139,18 +138,28 @@ double oracle_energy(const oracle_surface *s, const double *r, double *terms, do
 			VR += er; VC += eb; VA += ea;
 			ef += er + eb + ea;
 		}
-		if (face_e) face_e[f] = ef;
+		if (face_e) face_e[f - f0] = ef;
 		E += ef;
 	}
 	if (terms) { terms[0] = VA; terms[1] = VC; terms[2] = VR; }
 	return E;
 }
 
-void oracle_grad(const oracle_surface *s, const double *r, double *gr)
+double oracle_energy(const oracle_surface *s, const double *r, double *terms, double *face_e)
 {
-	const int nv = s->nv, nfaces = s->nreg + s->nirr;
+	return energy_range(s, r, terms, face_e, 0, s->nreg + s->nirr);
+}
+
+double oracle_energy_faces(const oracle_surface *s, const double *r, int f0, int f1)
+{
+	return energy_range(s, r, NULL, NULL, f0, f1);
+}
+
+static void grad_range(const oracle_surface *s, const double *r, double *gr, int f0, int f1)
+{
+	const int nv = s->nv;
 	const double *al = r + 3 * nv;
-	for (int f = 0; f < nfaces; f++) {
+	for (int f = f0; f < f1; f++) {
 		face_view F = face_at(s, f);
 		double X[13][3], Xs[13][3];
 		control_points(s, r, &F, X, Xs);
@@ -251,6 +260,16 @@ void oracle_grad(const oracle_surface *s, const double *r, double *gr)
 			}
 		}
 	}
+}
+
+void oracle_grad(const oracle_surface *s, const double *r, double *gr)
+{
+	grad_range(s, r, gr, 0, s->nreg + s->nirr);
+}
+
+void oracle_grad_faces(const oracle_surface *s, const double *r, double *gr, int f0, int f1)
+{
+	grad_range(s, r, gr, f0, f1);
 }
 
 void oracle_sparse_apply(int nrow, const int *row_ptr, const int *col, const double *val,

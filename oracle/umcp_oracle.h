@@ -52,6 +52,12 @@ double oracle_energy(const oracle_surface *s, const double *r, double *terms, do
  * into g (3*nv+3 entries, last three the box-scale derivatives). */
 void oracle_grad(const oracle_surface *s, const double *r, double *g);
 
+/* The same two passes restricted to faces [f0, f1) (regular faces first,
+ * then irregular), for a face-partitioned run over several processes as the
+ * reference's MPI face partition does (src/parallel.C:137-387). */
+double oracle_energy_faces(const oracle_surface *s, const double *r, int f0, int f1);
+void oracle_grad_faces(const oracle_surface *s, const double *r, double *g, int f0, int f1);
+
 /* AltSparseCartMatVecIncrScale (src/parallel.C:1028-1075) over a row-list
  * matrix in CSR form: out[3*row+c] += scale/alpha_c^2 * (scalev ? scalev[c*nrow+row] : 1)
  *                                     * sum_k val[k] * in[3*col[k]+c]. */

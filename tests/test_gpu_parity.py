@@ -1,0 +1,217 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's own
+outputs (golden fixtures) and against the oracle at larger sizes.
+
+Tolerances (written here, used below):
+  FP64 plain path: energy |dE|/|E| <= 1e-10; gradient max|dg|/max|g| <= 1e-10.
+  FP32 face-centred form: energy |dE|/|E| <= 1e-6; gradient max|dg|/max|g| <= 2e-5.
+  Integrator steps (FP64, same Philox draws as the oracle): positions to 1e-12
+  of the largest coordinate.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import umcp_gb300 as U
+from conftest import golden_cases, load_case, rel_inf
+from oracle import bridge as B
+
+pytestmark = pytest.mark.gpu
+
+E64, G64 = 1e-10, 1e-10
+E32, G32 = 1e-6, 2e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return U.Context(0)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_fp64_energy_and_gradient_match_reference(ctx, name):
+    plan, prm, gold = load_case(name)
+    mesh = U.Mesh(ctx, plan, prm)
+    E, t = mesh.energy(gold["r"], terms=True)
+    assert abs(E - gold["E"]) <= E64 * abs(gold["E"])
+    assert np.allclose(t, [gold["VA"], gold["VC"], gold["VR"]], rtol=0, atol=E64 * abs(gold["E"]))
+    g = np.zeros(3 * plan.nv + 3)
+    mesh.grad(gold["r"], g)
+    assert rel_inf(g[:-3], gold["grad"][:-3]) <= G64
+    assert np.allclose(g[-3:], gold["grad"][-3:], rtol=G64, atol=G64 * np.abs(gold["grad"]).max())
+
+
+def test_grad_accumulates_like_the_reference(ctx):
+    plan, prm, gold = load_case("ico2_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    g = np.ones(3 * plan.nv + 3)
+    mesh.grad(gold["r"], g)
+    assert rel_inf(g - 1.0, gold["grad"]) <= G64
+
+
+@pytest.mark.parametrize("kind,size", [("ico", 5), ("planar", 48)])
+def test_fp64_matches_oracle_at_larger_sizes(ctx, tmp_path, kind, size):
+    path = tmp_path / "m.mesh"
+    if kind == "ico":
+        U.generate_icosphere(path, size, 300.0, 3.0, 77)
+    else:
+        U.generate_planar(path, size, size, 10.0, 20.0, 78)
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, kg=-1.0, k_reg=0.1)
+    plan = U.Plan(path, prm)
+    r = plan.positions()
+    rng = np.random.default_rng(9)
+    r[:-3] += rng.normal(0, 0.2, 3 * plan.nv)
+    r[-3:] = (1.002, 0.999, 1.001)
+    O = B.Oracle(plan, prm)
+    mesh = U.Mesh(ctx, plan, prm)
+    E, g = mesh.energy_grad(r)
+    assert abs(E - O.energy(r)) <= E64 * abs(E)
+    assert rel_inf(g, O.grad(r)) <= G64
+
+
+def test_energy_grad_is_deterministic(ctx):
+    plan, prm, gold = load_case("ico4_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    E1, g1 = mesh.energy_grad(gold["r"])
+    E2, g2 = mesh.energy_grad(gold["r"])
+    assert E1 == E2 and np.array_equal(g1, g2)
+
+
+@pytest.mark.parametrize("name", ["ico4_plain", "planar12_deformed", "ico3_deformed"])
+def test_fp32_centred_form_error_bound(ctx, name):
+    plan, prm, gold = load_case(name, precision=U.FP32_CENTRED)
+    mesh = U.Mesh(ctx, plan, prm)
+    E, g = mesh.energy_grad(gold["r"])
+    assert abs(E - gold["E"]) <= E32 * abs(gold["E"])
+    assert rel_inf(g[:-3], gold["grad"][:-3]) <= G32
+
+
+def test_fp32_centred_form_on_the_planar_benchmark_membrane(ctx, tmp_path):
+    path = tmp_path / "p128.mesh"
+    U.generate_planar(path, 128, 128, 10.0, 20.0, 1002)
+    prm64 = U.params(kc=U.kc_from_kT(20.0), KA=0.215)
+    prm32 = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=U.FP32_CENTRED)
+    plan = U.Plan(path, prm64)
+    r = plan.positions()
+    r[:-3] += np.random.default_rng(4).normal(0, 0.05, 3 * plan.nv)
+    E64_, g64 = U.Mesh(ctx, plan, prm64).energy_grad(r)
+    E32_, g32 = U.Mesh(ctx, plan, prm32).energy_grad(r)
+    assert abs(E32_ - E64_) <= E32 * abs(E64_)
+    assert rel_inf(g32, g64) <= G32
+
+
+def _oracle_run(plan, prm, r, mode, dt, gamma, D, seed, stream, nsteps, mass=None):
+    O = B.Oracle(plan, prm)
+    kT = 0.592186663194 / 298.0 * prm.temperature
+    p = np.zeros(3 * plan.nv)
+    r = r.copy()
+    for s in range(nsteps):
+        g = O.grad(r)
+        xi = B.noise(seed, stream, s, plan.nv)
+        rv = r[:-3].copy()
+        B.step(mode, dt, gamma, kT, D, rv, p, g[:-3], xi, mass=mass)
+        r[:-3] = rv
+    return r, p
+
+
+@pytest.mark.parametrize("kind", [U.OVERDAMPED_BD, U.BD_MEMBRANE, U.LANGEVIN])
+def test_integrator_steps_match_oracle(ctx, kind):
+    plan, prm, gold = load_case("ico3_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    r0 = plan.positions()
+    if kind == U.OVERDAMPED_BD:
+        it = U.integrator(kind, time_step=1.0, D=0.00125, seed=11, stream=3)
+    else:
+        it = U.integrator(kind, time_step=1e-15, gamma=0.001, seed=11, stream=3)
+    mesh.state_set(r0)
+    energies = mesh.run(it, 0, 5)
+    r_gpu, p_gpu = mesh.state_get()
+    r_ref, p_ref = _oracle_run(plan, prm, r0, kind, it.time_step, it.gamma, it.D, 11, 3, 5)
+    assert np.max(np.abs(r_gpu - r_ref)) <= 1e-12 * np.abs(r_ref).max()
+    assert np.max(np.abs(p_gpu - p_ref)) <= 1e-12 * max(np.abs(p_ref).max(), 1e-300)
+    assert abs(energies[0] - B.Oracle(plan, prm).energy(r0)) <= E64 * energies[0]
+
+
+def test_run_graph_chunks_equal_eager_steps(ctx):
+    plan, prm, _ = load_case("ico2_plain")
+    it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.00125, seed=5)
+    a = U.Mesh(ctx, plan, prm)
+    e_a = a.run(it, 0, 70)  # two captured chunks of 32 and 6 eager steps
+    b = U.Mesh(ctx, plan, prm)
+    e_b = np.array([b.run(it, s, 1)[0] for s in range(70)])
+    assert np.array_equal(e_a, e_b)
+    assert np.array_equal(a.state_get()[0], b.state_get()[0])
+
+
+def test_step_host_is_one_run_step(ctx):
+    plan, prm, _ = load_case("ico2_plain")
+    it = U.integrator(U.LANGEVIN, time_step=1e-15, gamma=0.001, seed=8)
+    a = U.Mesh(ctx, plan, prm)
+    r = plan.positions()
+    p = np.zeros(3 * plan.nv)
+    for s in range(3):
+        a.step_host(it, s, r, p)
+    b = U.Mesh(ctx, plan, prm)
+    b.run(it, 0, 3)
+    rb, pb = b.state_get()
+    assert np.array_equal(r, rb) and np.array_equal(p, pb)
+
+
+def _random_mass(nv, seed, fill=0.05):
+    rng = np.random.default_rng(seed)
+    rows, cols, vals = [], [], []
+    for i in range(nv):
+        js = np.unique(np.concatenate([[i], rng.choice(nv, max(1, int(fill * nv)), replace=False)]))
+        rows.append(len(js))
+        cols.extend(js)
+        vals.extend(rng.normal(0, 1, len(js)) + (js == i) * 5.0)
+    row_ptr = np.concatenate([[0], np.cumsum(rows)]).astype(np.int32)
+    return row_ptr, np.array(cols, dtype=np.int32), np.array(vals)
+
+
+def test_mass_apply_matches_oracle(ctx):
+    plan, prm, _ = load_case("ico3_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    rp, cl, vl = _random_mass(plan.nv, 2)
+    mesh.mass_set(rp, cl, vl)
+    rng = np.random.default_rng(1)
+    vin = rng.normal(0, 1, 3 * plan.nv)
+    base = rng.normal(0, 1, 3 * plan.nv)
+    scalev = rng.uniform(0.5, 2.0, 3 * plan.nv)
+    for sv, scale, al in [(None, 1.0, (1, 1, 1)), (scalev, -0.7, (1.01, 0.98, 1.2))]:
+        got = mesh.mass_apply(vin, base.copy(), sv, scale, al)
+        want = B.sparse_apply(rp, cl, vl, vin, base.copy(), sv, scale, al)
+        assert np.max(np.abs(got - want)) <= 1e-13 * np.abs(want).max()
+
+
+def test_leapfrog_with_mass_matches_oracle(ctx):
+    plan, prm, _ = load_case("ico2_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    rp, cl, vl = _random_mass(plan.nv, 5, fill=0.2)
+    vl = np.abs(vl) * 0.01
+    mesh.mass_set(rp, cl, vl)
+    r0 = plan.positions()
+    for kind in (U.BD_MEMBRANE, U.LANGEVIN):
+        it = U.integrator(kind, time_step=1e-15, gamma=0.001, seed=21, stream=1, use_mass=1)
+        mesh.state_set(r0)
+        mesh.run(it, 0, 3)
+        r_gpu, p_gpu = mesh.state_get()
+        r_ref, p_ref = _oracle_run(plan, prm, r0, kind, it.time_step, it.gamma, 0.0, 21, 1, 3, mass=(rp, cl, vl))
+        assert np.max(np.abs(r_gpu - r_ref)) <= 1e-12 * np.abs(r_ref).max()
+
+
+def test_nonfinite_energy_is_reported_and_context_survives(ctx):
+    plan, prm, gold = load_case("ico2_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    r = gold["r"].copy()
+    r[5] = np.nan
+    with pytest.raises(U.UmcpError, match="non-finite"):
+        mesh.energy(r)
+    assert abs(mesh.energy(gold["r"]) - gold["E"]) <= E64 * abs(gold["E"])
+
+
+def test_divergence_stops_the_run(ctx):
+    plan, prm, _ = load_case("ico2_plain")
+    mesh = U.Mesh(ctx, plan, prm)
+    it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=5.0, seed=2, divergence_threshold=10.0)
+    with pytest.raises(U.UmcpError, match="diverged"):
+        mesh.run(it, 0, 40)

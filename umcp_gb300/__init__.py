@@ -55,6 +55,13 @@ class PlanInfo(C.Structure):
     ]
 
 
+class MeshInfo(C.Structure):
+    _fields_ = [
+        ("nv", C.c_int), ("n_faces", C.c_int), ("n_points", C.c_int), ("n_slots", C.c_int),
+        ("kernels_per_step", C.c_int), ("kernels_per_step_mass", C.c_int), ("precision", C.c_int),
+    ]
+
+
 class Integrator(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("time_step", C.c_double), ("gamma", C.c_double), ("D", C.c_double),
@@ -86,6 +93,9 @@ _SIGNATURES = {
     "umcp_ctx_create": [C.c_int, C.POINTER(_VP)],
     "umcp_ctx_destroy": [_VP],
     "umcp_ctx_synchronize": [_VP],
+    "umcp_ctx_stream": [_VP, C.POINTER(_VP)],
+    "umcp_face_pass": [_VP],
+    "umcp_mesh_info_get": [_VP, C.POINTER(MeshInfo)],
     "umcp_mesh_create": [_VP, _VP, C.POINTER(Params), C.POINTER(_VP)],
     "umcp_mesh_destroy": [_VP],
     "umcp_mesh_set_params": [_VP, C.POINTER(Params)],
@@ -255,6 +265,12 @@ class Context:
     def synchronize(self) -> None:
         _check(library().umcp_ctx_synchronize(self._h))
 
+    def stream(self) -> int:
+        """The cudaStream_t every engine call on this context is queued on."""
+        s = C.c_void_p()
+        _check(library().umcp_ctx_stream(self._h, C.byref(s)))
+        return s.value or 0
+
 
 class Mesh:
     """Device-resident surface; energy/grad mirror surface::energy/grad."""
@@ -274,6 +290,14 @@ class Mesh:
     @property
     def handle(self):
         return self._h
+
+    def info(self) -> MeshInfo:
+        i = MeshInfo()
+        _check(library().umcp_mesh_info_get(self._h, C.byref(i)))
+        return i
+
+    def face_pass(self) -> None:
+        _check(library().umcp_face_pass(self._h))
 
     def set_params(self, prm: Params) -> None:
         self._prm = prm

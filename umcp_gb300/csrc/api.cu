@@ -254,6 +254,12 @@ extern "C" void umcp_ctx_destroy(umcp_ctx *ctx) {
   delete ctx;
 }
 
+extern "C" umcp_status umcp_ctx_stream(umcp_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return fail(UMCP_ERR_INVALID, "null argument");
+  *stream = (void *)ctx->stream;
+  return UMCP_OK;
+}
+
 extern "C" umcp_status umcp_ctx_synchronize(umcp_ctx *ctx) {
   if (!ctx) return fail(UMCP_ERR_INVALID, "null ctx");
   UMCP_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -298,16 +304,23 @@ struct umcp_mesh {
   // effective inverse mass
   int mrows = 0;
   DevBuf mrow, mcol, mval, alphas;
-  // graph cache for runs
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
-  StepArgs graph_args{};
-  int graph_use_mass = -1;
-  double graph_threshold = 0;
-  void *graph_energies = nullptr;
+  // captured step sequences, by length (1 and kGraphChunk steps)
+  struct CachedGraph {
+    cudaGraphExec_t exec = nullptr;
+    int steps = 0;
+    StepArgs args{};
+    int use_mass = -1;
+    double threshold = 0;
+  };
+  std::vector<CachedGraph> graphs;
+  void drop_graphs() {
+    for (auto &g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
 
   ~umcp_mesh() {
-    if (graph) cudaGraphExecDestroy(graph);
+    drop_graphs();
     if (h_stage) cudaFreeHost(h_stage);
     if (h_stage2) cudaFreeHost(h_stage2);
   }
@@ -465,14 +478,15 @@ extern "C" void umcp_mesh_destroy(umcp_mesh *mesh) {
 extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *p) {
   if (!mesh || !p) return fail(UMCP_ERR_INVALID, "null argument");
   fill_params(mesh, p);
-  if (mesh->graph) { cudaGraphExecDestroy(mesh->graph); mesh->graph = nullptr; }
+  mesh->drop_graphs();
   return UMCP_OK;
 }
 
 // Queue energy+gradient of state d_r: E -> d_E (and parts), gradient ADDED
 // into d_g (3*nv+3). d_g may be null to skip the gather.
 template <typename T>
-static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g) {
+static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g,
+                                     bool faces_only) {
   cudaStream_t s = m->ctx->stream;
   for (auto &G : m->groups) {
     dev::FaceLaunch L;
@@ -491,6 +505,7 @@ static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_
                                     m->terms.as<double>(), m->status.as<int>(), 0, s);
     if (e != cudaSuccess) return e;
   }
+  if (faces_only) return cudaSuccess;
   if (d_g) {
     cudaError_t e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), d_g, s);
     if (e != cudaSuccess) return e;
@@ -499,9 +514,10 @@ static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_
                              s);
 }
 
-static cudaError_t queue_eg(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g) {
-  return (m->precision == UMCP_FP64) ? queue_energy_grad<double>(m, d_r, d_E, d_parts, d_g)
-                                     : queue_energy_grad<float>(m, d_r, d_E, d_parts, d_g);
+static cudaError_t queue_eg(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g,
+                            bool faces_only = false) {
+  return (m->precision == UMCP_FP64) ? queue_energy_grad<double>(m, d_r, d_E, d_parts, d_g, faces_only)
+                                     : queue_energy_grad<float>(m, d_r, d_E, d_parts, d_g, faces_only);
 }
 
 static umcp_status check_status(umcp_mesh *m) {
@@ -546,6 +562,30 @@ extern "C" umcp_status umcp_energy_grad(umcp_mesh *mesh, const double *r, double
   return host_energy_grad(mesh, r, E, nullptr, g);
 }
 
+extern "C" umcp_status umcp_face_pass(umcp_mesh *m) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(queue_eg(m, m->r.as<double>(), m->E.as<double>(), m->parts.as<double>(), nullptr, /*faces_only=*/true));
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *info) {
+  if (!m || !info) return fail(UMCP_ERR_INVALID, "null argument");
+  info->nv = m->nv;
+  info->n_faces = m->nfaces;
+  int npts = 0;
+  for (auto &G : m->groups) npts += G->nfaces * G->npt;
+  info->n_points = npts;
+  info->n_slots = m->nslots;
+  const int groups = (int)m->groups.size();
+  // face kernels + gather + reduce + record + update + advance; the mass path
+  // replaces the update with kick + spmv + drift.
+  info->kernels_per_step = groups + 5;
+  info->kernels_per_step_mass = groups + 7;
+  info->precision = m->precision;
+  return UMCP_OK;
+}
+
 extern "C" umcp_status umcp_energy_grad_device(umcp_mesh *m, const double *d_r, double *d_E, double *d_g) {
   if (!m || !d_r) return fail(UMCP_ERR_INVALID, "null argument");
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
@@ -567,7 +607,7 @@ extern "C" umcp_status umcp_mass_set(umcp_mesh *m, int nrow, const int *row_ptr,
   UMCP_CUDA(upload(m->mcol, std::vector<int>(col, col + nnz)));
   UMCP_CUDA(upload(m->mval, std::vector<double>(val, val + nnz)));
   m->mrows = nrow;
-  if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
+  m->drop_graphs();
   return UMCP_OK;
 }
 
@@ -685,13 +725,41 @@ static cudaError_t queue_step(umcp_mesh *m, const StepArgs &a, int use_mass, dou
 
 static bool same_args(const StepArgs &x, const StepArgs &y) { return memcmp(&x, &y, sizeof(StepArgs)) == 0; }
 
+static umcp_status graph_for(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold, int steps,
+                             cudaGraphExec_t *out) {
+  for (auto &g : m->graphs)
+    if (g.steps == steps && g.use_mass == use_mass && g.threshold == threshold && same_args(g.args, a)) {
+      *out = g.exec;
+      return UMCP_OK;
+    }
+  cudaStream_t s = m->ctx->stream;
+  cudaGraph_t g;
+  UMCP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < steps && e == cudaSuccess; ++i) e = queue_step(m, a, use_mass, threshold);
+  cudaError_t e2 = cudaStreamEndCapture(s, &g);
+  if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+  umcp_mesh::CachedGraph cg;
+  e = cudaGraphInstantiate(&cg.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e));
+  cg.steps = steps;
+  cg.args = a;
+  cg.use_mass = use_mass;
+  cg.threshold = threshold;
+  m->graphs.push_back(cg);
+  *out = cg.exec;
+  return UMCP_OK;
+}
+
 static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t step0, int n_steps) {
   cudaStream_t s = m->ctx->stream;
   StepArgs a;
   umcp_status st = make_step_args(m, it, &a);
   if (st != UMCP_OK) return st;
   if ((size_t)n_steps > m->energies_cap) {
-    if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
+    m->drop_graphs();  // graphs hold the energies pointer
     UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
     m->energies_cap = (size_t)n_steps;
   }
@@ -701,29 +769,17 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
   const int use_mass = (it->kind != 0 && it->use_mass) ? 1 : 0;
   const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
   if (full > 0) {
-    if (m->graph && (!same_args(a, m->graph_args) || m->graph_use_mass != use_mass ||
-                     m->graph_threshold != it->divergence_threshold)) {
-      cudaGraphExecDestroy(m->graph);
-      m->graph = nullptr;
-    }
-    if (!m->graph) {
-      cudaGraph_t g;
-      UMCP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e = cudaSuccess;
-      for (int i = 0; i < kGraphChunk && e == cudaSuccess; ++i) e = queue_step(m, a, use_mass, it->divergence_threshold);
-      cudaError_t e2 = cudaStreamEndCapture(s, &g);
-      if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e));
-      if (e2 != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
-      e = cudaGraphInstantiate(&m->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) { m->graph = nullptr; return fail(UMCP_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e)); }
-      m->graph_args = a;
-      m->graph_use_mass = use_mass;
-      m->graph_threshold = it->divergence_threshold;
-    }
-    for (int c = 0; c < full; ++c) UMCP_CUDA(cudaGraphLaunch(m->graph, s));
+    cudaGraphExec_t g;
+    st = graph_for(m, a, use_mass, it->divergence_threshold, kGraphChunk, &g);
+    if (st != UMCP_OK) return st;
+    for (int c = 0; c < full; ++c) UMCP_CUDA(cudaGraphLaunch(g, s));
   }
-  for (int i = 0; i < rem; ++i) UMCP_CUDA(queue_step(m, a, use_mass, it->divergence_threshold));
+  if (rem > 0) {
+    cudaGraphExec_t g1;
+    st = graph_for(m, a, use_mass, it->divergence_threshold, 1, &g1);
+    if (st != UMCP_OK) return st;
+    for (int i = 0; i < rem; ++i) UMCP_CUDA(cudaGraphLaunch(g1, s));
+  }
   return UMCP_OK;
 }
 
