@@ -121,7 +121,7 @@ def test_integrator_steps_match_oracle(ctx, kind):
     if kind == U.OVERDAMPED_BD:
         it = U.integrator(kind, time_step=1.0, D=0.00125, seed=11, stream=3)
     else:
-        it = U.integrator(kind, time_step=1e-15, gamma=0.001, seed=11, stream=3)
+        it = U.integrator(kind, time_step=1e-15, gamma=10.0, seed=11, stream=3)
     mesh.state_set(r0)
     energies = mesh.run(it, 0, 5)
     r_gpu, p_gpu = mesh.state_get()
@@ -191,7 +191,7 @@ def test_leapfrog_with_mass_matches_oracle(ctx):
     mesh.mass_set(rp, cl, vl)
     r0 = plan.positions()
     for kind in (U.BD_MEMBRANE, U.LANGEVIN):
-        it = U.integrator(kind, time_step=1e-15, gamma=0.001, seed=21, stream=1, use_mass=1)
+        it = U.integrator(kind, time_step=1e-15, gamma=10.0, seed=21, stream=1, use_mass=1)
         mesh.state_set(r0)
         mesh.run(it, 0, 3)
         r_gpu, p_gpu = mesh.state_get()

@@ -282,9 +282,11 @@ struct DevBuf {
 };
 
 struct Group {
-  int ncp = 0, npt = 0, nfaces = 0, face_base = 0, slot_base = 0, irregular = 0;
+  int ncp = 0, npt = 0, nfaces = 0, slot_base = 0, irregular = 0;
+  int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
   double dudv = 0.5;
   DevBuf cp, g0, rr0, comp, basis, weight, dest;
+  DevBuf g0f, rr0f, compf;  // FP32 copies for the precision form
 };
 }  // namespace
 
@@ -294,13 +296,16 @@ struct umcp_mesh {
   int precision = UMCP_FP64;
   dev::SurfaceParams P{};
   std::vector<std::unique_ptr<Group>> groups;
-  DevBuf partial, off, terms, seg;
-  DevBuf r, g, p, qdot, E, parts, status, step, runidx;
+  DevBuf partial, off, blockpart;
+  int nblocks = 0;
+  DevBuf r, g, p, qdot, E, parts, status, cnt;  // cnt: {first step of the run, run index}
+  DevBuf rhi, rlo;  // FP32 hi/lo pairs of r (precision form)
   double kT = 0.592186663194;  // kcal/mol at the params' temperature (src/hd.C:142-143)
   DevBuf energies;
   size_t energies_cap = 0;
   double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
   double *h_stage2 = nullptr; // pinned, 3*nv doubles
+  uint64_t *h_cnt = nullptr;  // pinned, 2 counters
   // effective inverse mass
   int mrows = 0;
   DevBuf mrow, mcol, mval, alphas;
@@ -323,6 +328,7 @@ struct umcp_mesh {
     drop_graphs();
     if (h_stage) cudaFreeHost(h_stage);
     if (h_stage2) cudaFreeHost(h_stage2);
+    if (h_cnt) cudaFreeHost(h_cnt);
   }
 };
 
@@ -364,7 +370,11 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   m->nv = ME.nv;
   m->P.nv = ME.nv;
   for (int d = 0; d < 3; ++d)
-    for (int c = 0; c < 3; ++c) m->P.box[d][c] = ME.box[d][c];
+    for (int c = 0; c < 3; ++c) {
+      m->P.box[d][c] = ME.box[d][c];
+      m->P.box_hi[d][c] = (float)ME.box[d][c];
+      m->P.box_lo[d][c] = (float)(ME.box[d][c] - (double)m->P.box_hi[d][c]);
+    }
   fill_params(m.get(), prm);
 
   // Face groups: regular, then irregular by valence (5, 7).
@@ -383,14 +393,13 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   }
   const int nt = PL.ntypes;
   std::vector<std::vector<int>> vslots(ME.nv);  // slots touching each vertex, ascending
-  int face_base = 0, slot_base = 0;
+  int face_base = 0, slot_base = 0, block_base = 0;
   for (const Src &s : srcs) {
     auto G = std::make_unique<Group>();
     const PatchBasis &B = *s.B;
     G->ncp = B.ncp;
     G->npt = B.npt;
     G->nfaces = (int)s.idx.size();
-    G->face_base = face_base;
     G->slot_base = slot_base;
     G->irregular = s.irr;
     G->dudv = s.irr ? 1.0 : 0.5;
@@ -412,16 +421,26 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
       const double *I = &(s.irr ? PL.irr_inner : PL.reg_inner)[(size_t)f * nt];
       composition_coeffs(O, I, PL.lipids, &comp[3 * q], &comp[3 * q + 1], &comp[3 * q + 2]);
     }
-    // basis rows u,v,uu,uv,vv as [kind][cp][pt]
-    std::vector<double> basis((size_t)5 * G->ncp * G->npt);
-    for (int k = 0; k < 5; ++k)
-      for (int x = 0; x < G->ncp; ++x)
-        for (int p = 0; p < G->npt; ++p) basis[((size_t)k * G->ncp + x) * G->npt + p] = B.at(k + 1, p, x);
+    // basis rows u,v,uu,uv,vv as [pt][kind][cp], cp padded with zeros to a multiple of 4
+    const int ncpp = (G->ncp + 3) / 4 * 4;
+    std::vector<double> basis((size_t)G->npt * 5 * ncpp, 0.0);
+    for (int p = 0; p < G->npt; ++p)
+      for (int k = 0; k < 5; ++k)
+        for (int x = 0; x < G->ncp; ++x) basis[((size_t)p * 5 + k) * ncpp + x] = B.at(k + 1, p, x);
+    G->nblocks = (prm->precision == UMCP_FP64) ? face_blocks<double>(G->nfaces, G->ncp, G->npt)
+                                               : face_blocks<float>(G->nfaces, G->ncp, G->npt);
+    G->block_base = block_base;
+    block_base += G->nblocks;
     UMCP_CUDA(upload(G->cp, cp));
     UMCP_CUDA(upload(G->g0, g0));
     UMCP_CUDA(upload(G->rr0, rr0));
     UMCP_CUDA(upload(G->comp, comp));
     UMCP_CUDA(upload(G->basis, basis));
+    if (prm->precision == UMCP_FP32_CENTRED) {
+      UMCP_CUDA(upload(G->g0f, std::vector<float>(g0.begin(), g0.end())));
+      UMCP_CUDA(upload(G->rr0f, std::vector<float>(rr0.begin(), rr0.end())));
+      UMCP_CUDA(upload(G->compf, std::vector<float>(comp.begin(), comp.end())));
+    }
     UMCP_CUDA(upload(G->weight, B.weight));
     face_base += G->nfaces;
     slot_base += G->nfaces * G->ncp;
@@ -439,11 +458,11 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     UMCP_CUDA(upload(G->dest, d));
   }
   UMCP_CUDA(upload(m->off, off));
-  std::vector<int> seg = {0, m->nfaces};
-  UMCP_CUDA(upload(m->seg, seg));
+  m->nblocks = block_base;
+  UMCP_CUDA(m->blockpart.alloc((size_t)(block_base > 0 ? block_base : 1) * 6 * sizeof(double)));
+  UMCP_CUDA(cudaMemset(m->blockpart.p, 0, m->blockpart.bytes));
   const size_t elem = (m->precision == UMCP_FP64) ? sizeof(double) : sizeof(float);
   UMCP_CUDA(m->partial.alloc((size_t)slot_base * 3 * elem));
-  UMCP_CUDA(m->terms.alloc((size_t)m->nfaces * 6 * sizeof(double)));
   const size_t nst = 3 * (size_t)ME.nv + 3;
   UMCP_CUDA(m->r.alloc(nst * sizeof(double)));
   UMCP_CUDA(m->g.alloc(nst * sizeof(double)));
@@ -452,18 +471,24 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   UMCP_CUDA(m->E.alloc(sizeof(double)));
   UMCP_CUDA(m->parts.alloc(3 * sizeof(double)));
   UMCP_CUDA(m->status.alloc(sizeof(int)));
-  UMCP_CUDA(m->step.alloc(sizeof(uint64_t)));
-  UMCP_CUDA(m->runidx.alloc(sizeof(uint64_t)));
+  UMCP_CUDA(m->cnt.alloc(2 * sizeof(uint64_t)));
   UMCP_CUDA(m->alphas.alloc(3 * sizeof(double)));
   UMCP_CUDA(cudaMemset(m->p.p, 0, m->p.bytes));
   UMCP_CUDA(cudaMemset(m->status.p, 0, sizeof(int)));
   UMCP_CUDA(cudaMallocHost(&m->h_stage, nst * sizeof(double)));
   UMCP_CUDA(cudaMallocHost(&m->h_stage2, 3 * (size_t)ME.nv * sizeof(double)));
+  UMCP_CUDA(cudaMallocHost(&m->h_cnt, 2 * sizeof(uint64_t)));
   // Initial state: the plan's positions, alpha = 1.
   std::vector<double> r0(nst);
   std::copy(ME.r.begin(), ME.r.end(), r0.begin());
   r0[3 * ME.nv] = r0[3 * ME.nv + 1] = r0[3 * ME.nv + 2] = 1.0;
   UMCP_CUDA(cudaMemcpy(m->r.p, r0.data(), nst * sizeof(double), cudaMemcpyHostToDevice));
+  if (m->precision == UMCP_FP32_CENTRED) {
+    UMCP_CUDA(m->rhi.alloc(3 * (size_t)ME.nv * sizeof(float)));
+    UMCP_CUDA(m->rlo.alloc(3 * (size_t)ME.nv * sizeof(float)));
+    UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), 0));
+    UMCP_CUDA(cudaDeviceSynchronize());
+  }
   *out = m.release();
   return UMCP_OK;
 }
@@ -485,33 +510,47 @@ extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *
 // Queue energy+gradient of state d_r: E -> d_E (and parts), gradient ADDED
 // into d_g (3*nv+3). d_g may be null to skip the gather.
 template <typename T>
-static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g,
-                                     bool faces_only) {
+static cudaError_t queue_faces(umcp_mesh *m, const double *d_r) {
   cudaStream_t s = m->ctx->stream;
   for (auto &G : m->groups) {
     dev::FaceLaunch L;
     L.nfaces = G->nfaces;
-    L.face_base = G->face_base;
-    L.slot_base = G->slot_base;
+    L.block_base = G->block_base;
     L.cp = G->cp.as<uint32_t>();
     L.g0 = G->g0.as<double>();
     L.rr0 = G->rr0.as<double>();
     L.comp = G->comp.as<double>();
+    L.g0f = G->g0f.as<float>();
+    L.rr0f = G->rr0f.as<float>();
+    L.compf = G->compf.as<float>();
     L.basis = G->basis.as<double>();
     L.weight = G->weight.as<double>();
     L.dudv = G->dudv;
     L.irregular = G->irregular;
-    cudaError_t e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->partial.as<T>(),
-                                    m->terms.as<double>(), m->status.as<int>(), 0, s);
+    cudaError_t e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(),
+                                    m->rlo.as<float>(), m->partial.as<T>(), m->blockpart.as<double>(),
+                                    m->status.as<int>(), G->nblocks, s);
     if (e != cudaSuccess) return e;
   }
-  if (faces_only) return cudaSuccess;
-  if (d_g) {
-    cudaError_t e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), d_g, s);
-    if (e != cudaSuccess) return e;
-  }
-  return launch_reduce_terms(1, m->seg.as<int>(), m->terms.as<double>(), d_E, d_parts, d_g ? d_g + 3 * m->nv : nullptr,
-                             s);
+  return cudaSuccess;
+}
+
+// Energy and gradient of state d_r: E -> d_E (parts -> d_parts), gradient
+// ADDED into d_g (3*nv+3) when d_g is given.
+template <typename T>
+static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g,
+                                     bool faces_only) {
+  cudaStream_t s = m->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (sizeof(T) == 4 && !faces_only) e = launch_split_positions(3 * m->nv, d_r, m->rhi.as<float>(), m->rlo.as<float>(), s);
+  if (e != cudaSuccess) return e;
+  e = queue_faces<T>(m, d_r);
+  if (e != cudaSuccess || faces_only) return e;
+  e = launch_finish(m->nblocks, m->blockpart.as<double>(), d_E, d_parts, d_g ? d_g + 3 * m->nv : nullptr, nullptr,
+                    nullptr, 0.0, m->status.as<int>(), s);
+  if (e != cudaSuccess) return e;
+  if (d_g) e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), d_g, s);
+  return e;
 }
 
 static cudaError_t queue_eg(umcp_mesh *m, const double *d_r, double *d_E, double *d_parts, double *d_g,
@@ -578,10 +617,10 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
   info->n_points = npts;
   info->n_slots = m->nslots;
   const int groups = (int)m->groups.size();
-  // face kernels + gather + reduce + record + update + advance; the mass path
-  // replaces the update with kick + spmv + drift.
-  info->kernels_per_step = groups + 5;
-  info->kernels_per_step_mass = groups + 7;
+  // face kernels + finish + fused gather/update; the mass path replaces the
+  // fused kernel with gather + kick + spmv + drift.
+  info->kernels_per_step = groups + 2;
+  info->kernels_per_step_mass = groups + 5;
   info->precision = m->precision;
   return UMCP_OK;
 }
@@ -660,6 +699,9 @@ extern "C" umcp_status umcp_state_set(umcp_mesh *m, const double *r, const doubl
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
   const size_t nst = 3 * (size_t)m->nv + 3;
   if (r) UMCP_CUDA(cudaMemcpyAsync(m->r.p, r, nst * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
+  if (r && m->precision == UMCP_FP32_CENTRED)
+    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(),
+                                     m->ctx->stream));
   if (p) UMCP_CUDA(cudaMemcpyAsync(m->p.p, p, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
   else UMCP_CUDA(cudaMemsetAsync(m->p.p, 0, (nst - 3) * sizeof(double), m->ctx->stream));
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
@@ -697,30 +739,35 @@ static umcp_status make_step_args(umcp_mesh *m, const umcp_integrator *it, StepA
   return UMCP_OK;
 }
 
-// One step on the resident state: energy+gradient at r(t), then the update.
-static cudaError_t queue_step(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold) {
+// One step on the resident state: energy and gradient at r(t), then the update.
+template <typename T>
+static cudaError_t queue_step_t(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold) {
   cudaStream_t s = m->ctx->stream;
-  const size_t nst = 3 * (size_t)m->nv + 3;
-  cudaError_t e = cudaMemsetAsync(m->g.p, 0, nst * sizeof(double), s);
+  cudaError_t e = queue_faces<T>(m, m->r.as<double>());
   if (e != cudaSuccess) return e;
-  e = queue_eg(m, m->r.as<double>(), m->E.as<double>(), m->parts.as<double>(), m->g.as<double>());
+  e = launch_finish(m->nblocks, m->blockpart.as<double>(), m->E.as<double>(), m->parts.as<double>(), nullptr,
+                    m->energies.as<double>(), m->cnt.as<uint64_t>(), threshold, m->status.as<int>(), s);
   if (e != cudaSuccess) return e;
-  e = launch_record_energy(m->E.as<double>(), m->energies.as<double>(), m->runidx.as<uint64_t>(), threshold,
-                           m->status.as<int>(), s);
-  if (e != cudaSuccess) return e;
-  if (a.kind == 0 || !use_mass) {
-    e = launch_step_local(m->nv, a, m->step.as<uint64_t>(), m->r.as<double>(), m->p.as<double>(), m->g.as<double>(),
-                          m->status.as<int>(), s);
-  } else {
-    e = launch_kick(m->nv, a, m->step.as<uint64_t>(), m->p.as<double>(), m->g.as<double>(), m->status.as<int>(), s);
-    if (e == cudaSuccess)
-      e = launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), nullptr, 1.0, nullptr,
-                      m->p.as<double>(), m->qdot.as<double>(), 0, s);
-    if (e == cudaSuccess)
-      e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->status.as<int>(), s);
-  }
-  if (e != cudaSuccess) return e;
-  return launch_advance_step(m->step.as<uint64_t>(), m->runidx.as<uint64_t>(), s);
+  if (a.kind == 0 || !use_mass)
+    return launch_gather_step<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), a, m->cnt.as<uint64_t>(),
+                                 m->r.as<double>(), m->p.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(),
+                                 m->status.as<int>(), s);
+  e = cudaMemsetAsync(m->g.p, 0, 3 * (size_t)m->nv * sizeof(double), s);
+  if (e == cudaSuccess) e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), m->g.as<double>(), s);
+  if (e == cudaSuccess)
+    e = launch_kick(m->nv, a, m->cnt.as<uint64_t>(), m->p.as<double>(), m->g.as<double>(), m->status.as<int>(), s);
+  if (e == cudaSuccess)
+    e = launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), nullptr, 1.0, nullptr,
+                    m->p.as<double>(), m->qdot.as<double>(), 0, s);
+  if (e == cudaSuccess)
+    e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->rhi.as<float>(),
+                     m->rlo.as<float>(), m->status.as<int>(), s);
+  return e;
+}
+
+static cudaError_t queue_step(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold) {
+  return (m->precision == UMCP_FP64) ? queue_step_t<double>(m, a, use_mass, threshold)
+                                     : queue_step_t<float>(m, a, use_mass, threshold);
 }
 
 static bool same_args(const StepArgs &x, const StepArgs &y) { return memcmp(&x, &y, sizeof(StepArgs)) == 0; }
@@ -763,8 +810,11 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
     UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
     m->energies_cap = (size_t)n_steps;
   }
-  UMCP_CUDA(cudaMemcpyAsync(m->step.p, &step0, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-  UMCP_CUDA(cudaMemsetAsync(m->runidx.p, 0, sizeof(uint64_t), s));
+  if (m->precision == UMCP_FP32_CENTRED)
+    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
+  m->h_cnt[0] = step0;
+  m->h_cnt[1] = 0;
+  UMCP_CUDA(cudaMemcpyAsync(m->cnt.p, m->h_cnt, 2 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
   UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), s));
   const int use_mass = (it->kind != 0 && it->use_mass) ? 1 : 0;
   const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;

@@ -1,14 +1,15 @@
 // Device kernels of the membrane-surface hot path (sm_103a).
 //
 // face_kernel     one half-warp per face: lanes are quadrature points while
-//                 the five basis contractions and the pointwise energy and
-//                 adjoint are formed, then lanes are control points while the
-//                 adjoint is contracted back onto the one-ring. Writes per-face
-//                 gradient partials and per-face energy terms; no atomics.
-// gather_kernel   per vertex, sums its face partials in a fixed order (CSR of
-//                 (face, slot) references), optionally fused with an
-//                 integrator update.
-// reduce_kernel   per mesh, fixed-order tree sum of the per-face terms.
+//                 the five basis contractions, the pointwise energy and
+//                 adjoint, and each point's contribution to every control
+//                 point are formed; then lanes are control points while those
+//                 contributions are summed. Writes per-face gradient partials
+//                 and per-block energy sums; no float atomics.
+// gather_kernel   per vertex, sums its face partials in a fixed order
+//                 (vertex-major slots), optionally fused with an integrator
+//                 update.
+// finish_kernel   fixed-order sum of the block partials.
 //
 // The energy model is the reference's surface::fenergy/ifenergy with
 // FIXED_A and LOCAL_LIPID_ENERGY (src/interpLib.C:3426-3881); the gradient
@@ -31,19 +32,20 @@ constexpr double kSafety = 1e-12;  // SAFETY, src/interp.h:14
 struct SurfaceParams {
   double kc, KA, kg, k_reg;
   double box[3][3];
+  float box_hi[3][3], box_lo[3][3];  // box = hi + lo, for the precision form
   int nv;
 };
 
 // Per-mesh view for a face launch.
 struct FaceLaunch {
   int nfaces;              // faces in this launch
-  int face_base;           // index of the first face in the mesh's face numbering (for terms)
-  int slot_base;           // first partial slot (in units of 3 values) of face 0
+  int block_base;          // first block-partial row of this launch
   const uint32_t *cp;      // [nfaces][ncp] packed control points
-  const double *g0;        // [nfaces][npt]
+  const double *g0;        // [nfaces][npt] (plain path)
   const double *rr0;       // [nfaces][npt]
   const double *comp;      // [nfaces][3]: P2, Hbar, Pres
-  const double *basis;     // [5][ncp][npt] rows u,v,uu,uv,vv (global, staged to shared)
+  const float *g0f, *rr0f, *compf;  // the same in FP32 (precision form)
+  const double *basis;     // [npt][5][ncp rounded up to 4] rows u,v,uu,uv,vv (staged to shared)
   const double *weight;    // [npt]
   double dudv;
   int irregular;

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -426,7 +427,10 @@ void generate_planar(int nx, int ny, double a, double kc_kT, uint64_t seed, Mesh
   // of lattice-commensurate q with 0 < |q| <= pi/a, Var(A_q) = 1/(kc_kT Lx Ly q^4).
   const double qmax = M_PI / a;
   int mmax = (int)std::floor(qmax * Lx / (2 * M_PI)), nmax = (int)std::floor(qmax * Ly / (2 * M_PI));
-  std::vector<double> qx, qy, amp, ph;
+  // Separable evaluation: with x = a (i + s/2) (s = row parity) and y = h j,
+  //   z(i,j) = Re sum_n e^{2 pi i n j / ny} F_n(i, s),
+  //   F_n(i, s) = sum_m A_mn e^{i phi_mn} e^{2 pi i m (i + s/2) / nx}.
+  std::vector<std::vector<std::pair<int, std::complex<double>>>> rows(nmax + 1);
   for (int nn = 0; nn <= nmax; ++nn)
     for (int mm = -mmax; mm <= mmax; ++mm) {
       if (nn == 0 && mm <= 0) continue;
@@ -436,15 +440,27 @@ void generate_planar(int nx, int ny, double a, double kc_kT, uint64_t seed, Mesh
       double g0, g1;
       normal_pair(seed, (uint32_t)(mm + 65536), (uint32_t)nn, 1u, &g0, &g1);
       double sd = std::sqrt(1.0 / (kc_kT * Lx * Ly * q2 * q2));
-      qx.push_back(kx); qy.push_back(ky);
-      amp.push_back(sd * g0);
-      ph.push_back(M_PI * (1.0 + std::erf(g1 / std::sqrt(2.0))));  // uniform phase in [0, 2pi)
+      double amp = sd * g0;
+      double ph = M_PI * (1.0 + std::erf(g1 / std::sqrt(2.0)));  // uniform phase in [0, 2pi)
+      rows[nn].push_back({mm, std::polar(amp, ph)});
     }
-  for (int v = 0; v < nv; ++v) {
-    double x = m->r[3 * v], y = m->r[3 * v + 1], z = 0;
-    for (size_t q = 0; q < qx.size(); ++q) z += amp[q] * std::cos(qx[q] * x + qy[q] * y + ph[q]);
-    m->r[3 * v + 2] = z;
+  std::vector<std::complex<double>> F((size_t)2 * nx);
+  std::vector<double> z((size_t)nv, 0.0);
+  for (int nn = 0; nn <= nmax; ++nn) {
+    if (rows[nn].empty()) continue;
+    for (int sp = 0; sp < 2; ++sp)
+      for (int i = 0; i < nx; ++i) {
+        std::complex<double> acc = 0;
+        for (const auto &mc : rows[nn]) acc += mc.second * std::polar(1.0, 2 * M_PI * mc.first * (i + 0.5 * sp) / nx);
+        F[(size_t)sp * nx + i] = acc;
+      }
+    for (int j = 0; j < ny; ++j) {
+      std::complex<double> e = std::polar(1.0, 2 * M_PI * nn * (double)j / ny);
+      const std::complex<double> *Fr = &F[(size_t)(j & 1) * nx];
+      for (int i = 0; i < nx; ++i) z[id(i, j)] += (Fr[i] * e).real();
+    }
   }
+  for (int v = 0; v < nv; ++v) m->r[3 * v + 2] = z[v];
   m->box[0][0] = Lx; m->box[0][1] = 0; m->box[0][2] = 0;
   m->box[1][0] = 0; m->box[1][1] = Ly; m->box[1][2] = 0;
   m->box[2][0] = 0; m->box[2][1] = 0; m->box[2][2] = 1e6;

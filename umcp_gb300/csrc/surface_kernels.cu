@@ -11,181 +11,281 @@
 namespace umcp {
 namespace dev {
 
-constexpr int kThreads = 128;
-constexpr int kHalfWarps = kThreads / 16;
-constexpr int kAdjKinds = 7;  // Ru, Rv, Suu, Suv, Svv adjoints + angle-term part of Ru, Rv
+template <typename T>
+struct alignas(4 * sizeof(T)) Q4 {
+  T x, y, z, w;
+};
 
-// One half-warp (16 lanes) per face. Shared memory per block: the patch's
-// basis rows [kind][cp][pt] (pt fastest, so lanes that differ in pt or in cp
-// hit distinct banks), and per half-warp the face's control points and the
-// adjoints [kind][xyz][pt].
+// FP64 uses half the threads per block so its shared memory stays below the
+// 48 KB static limit.
+template <typename T>
+struct FaceCfg {
+  static constexpr int threads = (sizeof(T) == 8) ? 64 : 128;
+  static constexpr int half_warps = threads / 16;
+  static constexpr int min_blocks = (sizeof(T) == 8) ? 6 : 4;  // caps registers near 128 (FP32) / 168 (FP64)
+};
+
 template <typename T, int NCP, int NPT>
-__global__ void __launch_bounds__(kThreads) face_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P,
-                                                        const double *__restrict__ r, T *__restrict__ partial,
-                                                        double *__restrict__ terms, int *__restrict__ status) {
-  __shared__ T sB[5 * NCP * NPT];
-  __shared__ T sX[kHalfWarps][NCP][3];
-  __shared__ T sK[kHalfWarps][kAdjKinds][3][16];
-  __shared__ T sW[NPT];
+struct FaceSmem {
+  static constexpr int NC4 = (NCP + 3) / 4;  // control points in chunks of four
+  static constexpr int NCPP = NC4 * 4;
+  static constexpr int HW = FaceCfg<T>::half_warps;
+  Q4<T> B[NPT][5][NC4];           // basis rows u,v,uu,uv,vv of point p
+  Q4<T> X[HW][NCPP];              // centred, alpha-scaled control points
+  Q4<T> Tc[HW][NPT][NCPP + 1];    // point p's contribution to each control point (+1 row pad: no bank conflicts)
+  T W[NPT];
+  double red[HW][6];
+};
 
-  for (int i = threadIdx.x; i < 5 * NCP * NPT; i += kThreads) sB[i] = (T)L.basis[i];
-  for (int i = threadIdx.x; i < NPT; i += kThreads) sW[i] = (T)L.weight[i];
+// Error-free sum: s + e == a + b exactly (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Per-half-warp sums of a face's energy terms and dE/dalpha: FP64 in the
+// plain path; FP32 with Kahan compensation in the precision form, which keeps
+// the FP64 pipe out of the face loop.
+template <typename T>
+struct HalfWarpSums;
+template <>
+struct HalfWarpSums<double> {
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  __device__ __forceinline__ void add(int q, double v) { s[q] += v; }
+  __device__ __forceinline__ double get(int q) const { return s[q]; }
+};
+template <>
+struct HalfWarpSums<float> {
+  float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
+  __device__ __forceinline__ void add(int q, float v) {
+    float y = v - c[q], t = s[q] + y;
+    c[q] = (t - s[q]) - y;
+    s[q] = t;
+  }
+  __device__ __forceinline__ double get(int q) const { return (double)s[q] - (double)c[q]; }
+};
+
+template <typename T>
+__device__ __forceinline__ T point_data(const double *d64, const float *d32, size_t i) {
+  if constexpr (sizeof(T) == 8) return d64[i];
+  else return d32[i];
+}
+
+// One half-warp (16 lanes) per face, persistent over faces.
+//  1. lanes = control points: the control point's position relative to the
+//     patch corner (control point 0) in its lattice image, times alpha. The
+//     plain path forms it in FP64; the precision form from FP32 hi/lo pairs
+//     with error-free sums, so the local coordinates carry full FP32
+//     precision even across periodic images.
+//  2. lanes = quadrature points: the five contractions (basis rows held per
+//     point, control points broadcast), pointwise energy and adjoint, and the
+//     adjoint's contribution to every control point (written transposed).
+//  3. lanes = control points: sum the contributions over the points; write the
+//     alpha-scaled gradient partial to its vertex-major slot.
+// Energy terms and dE/dalpha are summed per half-warp, then per block in a
+// fixed order, and written as one block partial (no atomics on floats).
+template <typename T, int NCP, int NPT>
+__global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
+    face_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
+                const float *__restrict__ rhi, const float *__restrict__ rlo, T *__restrict__ partial,
+                double *__restrict__ blockpart, int *__restrict__ status) {
+  using S = FaceSmem<T, NCP, NPT>;
+  constexpr int NC4 = S::NC4, NCPP = S::NCPP, HW = S::HW, NT = FaceCfg<T>::threads;
+  __shared__ S sm;
+
+  {
+    T *b = &sm.B[0][0][0].x;
+    for (int i = threadIdx.x; i < NPT * 5 * NCPP; i += NT) b[i] = (T)L.basis[i];
+    for (int i = threadIdx.x; i < NPT; i += NT) sm.W[i] = (T)L.weight[i];
+    for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
+  }
   __syncthreads();
 
   const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
   const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
-  const double alpha[3] = {r[3 * P.nv], r[3 * P.nv + 1], r[3 * P.nv + 2]};
+  const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
+  const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
   const T kc = (T)P.kc, KA = (T)P.KA, kg = (T)P.kg, k_reg = (T)P.k_reg, dudv = (T)L.dudv;
+  const bool reg_alpha = L.irregular && P.k_reg != 0.0;
+  HalfWarpSums<T> acc;
 
-  for (int f = blockIdx.x * kHalfWarps + hw; f < L.nfaces; f += gridDim.x * kHalfWarps) {
-    // ---- control points: alpha*(r + lattice image), centred on the patch centroid
-    double X[3] = {0, 0, 0}, Xs[3] = {0, 0, 0};
-    if (lane < NCP) {
-      uint32_t packed = L.cp[(size_t)f * NCP + lane];
-      int v = (int)(packed & kVertexMask);
-      int code = (int)(packed >> kVertexBits);
-      int ix = code % 3 - 1, iy = (code / 3) % 3 - 1, iz = code / 9 - 1;
+  for (int f = blockIdx.x * HW + hw; f < L.nfaces; f += gridDim.x * HW) {
+    // ---- 1. control points, relative to the patch corner
+    T xl[3] = {0, 0, 0};
+    {
+      int v = 0, img[3] = {0, 0, 0};
+      if (lane < NCP) {
+        uint32_t packed = L.cp[(size_t)f * NCP + lane];
+        v = (int)(packed & kVertexMask);
+        int code = (int)(packed >> kVertexBits);
+        img[0] = code % 3 - 1; img[1] = (code / 3) % 3 - 1; img[2] = code / 9 - 1;
+      }
+      if constexpr (sizeof(T) == 8) {
+        double X[3] = {0, 0, 0};
+        if (lane < NCP)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        X[c] = r[3 * v + c] + ix * P.box[0][c] + iy * P.box[1][c] + iz * P.box[2][c];
-        Xs[c] = alpha[c] * X[c];
+          for (int c = 0; c < 3; ++c)
+            X[c] = r[3 * (size_t)v + c] + img[0] * P.box[0][c] + img[1] * P.box[1][c] + img[2] * P.box[2][c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double a = __shfl_sync(hmask, X[c], 0, 16);
+          xl[c] = alpha[c] * (X[c] - a);
+        }
+      } else {
+        float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+        if (lane < NCP)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) { hi[c] = rhi[3 * (size_t)v + c]; lo[c] = rlo[3 * (size_t)v + c]; }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float ahi = __shfl_sync(hmask, hi[c], 0, 16), alo = __shfl_sync(hmask, lo[c], 0, 16);
+          // lattice shift hi + lo (each term exact: images are -1, 0 or +1)
+          float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            float t, e;
+            two_sum(sh, (float)img[d] * P.box_hi[d][c], t, e);
+            sh = t;
+            she += e;
+            shl += (float)img[d] * P.box_lo[d][c];
+          }
+          float s1, e1, s2, e2;
+          two_sum(hi[c], sh, s1, e1);
+          two_sum(s1, -ahi, s2, e2);
+          xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((lo[c] - alo) + (she + shl))));
+        }
       }
     }
-    double cen[3] = {Xs[0], Xs[1], Xs[2]}, ucen[3] = {X[0], X[1], X[2]};
-#pragma unroll
-    for (int off = 8; off >= 1; off >>= 1)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        cen[c] += __shfl_xor_sync(hmask, cen[c], off, 16);
-        ucen[c] += __shfl_xor_sync(hmask, ucen[c], off, 16);
-      }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) { cen[c] *= (1.0 / NCP); ucen[c] *= (1.0 / NCP); }
-    if (lane < NCP)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) sX[hw][lane][c] = (T)(Xs[c] - cen[c]);
+    if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
     __syncwarp(hmask);
 
-    // ---- lanes as quadrature points: contractions, energy, adjoint
+    // ---- 2. lanes as quadrature points
     T ea = 0, ec = 0, er = 0;
+    T dreg[3] = {0, 0, 0};
     if (lane < NPT) {
       Vec3<T> K[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) K[k] = {0, 0, 0};
-#pragma unroll
-      for (int x = 0; x < NCP; ++x) {
-        const T px = sX[hw][x][0], py = sX[hw][x][1], pz = sX[hw][x][2];
+#pragma unroll 1
+      for (int c4 = 0; c4 < NC4; ++c4) {
+        const Q4<T> x0 = sm.X[hw][4 * c4], x1 = sm.X[hw][4 * c4 + 1], x2 = sm.X[hw][4 * c4 + 2],
+                    x3 = sm.X[hw][4 * c4 + 3];
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-          const T b = sB[(k * NCP + x) * NPT + lane];
-          K[k].x += b * px;
-          K[k].y += b * py;
-          K[k].z += b * pz;
+          const Q4<T> b = sm.B[lane][k][c4];
+          K[k].x += b.x * x0.x + b.y * x1.x + b.z * x2.x + b.w * x3.x;
+          K[k].y += b.x * x0.y + b.y * x1.y + b.z * x2.y + b.w * x3.y;
+          K[k].z += b.x * x0.z + b.y * x1.z + b.z * x2.z + b.w * x3.z;
         }
       }
       const size_t pi = (size_t)f * NPT + lane;
-      const T g0 = (T)L.g0[pi], rr0 = (T)L.rr0[pi];
-      const T P2 = (T)L.comp[3 * (size_t)f], Hbar = (T)L.comp[3 * (size_t)f + 1], Pres = (T)L.comp[3 * (size_t)f + 2];
+      const T g0 = point_data<T>(L.g0, L.g0f, pi), rr0 = point_data<T>(L.rr0, L.rr0f, pi);
+      const T P2 = point_data<T>(L.comp, L.compf, 3 * (size_t)f), Hbar = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 1),
+              Pres = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 2);
       Vec3<T> Kb[5], Kreg[2];
-      point_adjoint<T>(K, sW[lane], g0, rr0, dudv, P2, Hbar, Pres, kc, KA, kg, k_reg, &ea, &ec, &er, Kb, Kreg);
+      point_adjoint<T>(K, sm.W[lane], g0, rr0, dudv, P2, Hbar, Pres, kc, KA, kg, k_reg, &ea, &ec, &er, Kb, Kreg);
+#pragma unroll 1
+      for (int c4 = 0; c4 < NC4; ++c4) {
+        Q4<T> b[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        sK[hw][k][0][lane] = Kb[k].x;
-        sK[hw][k][1][lane] = Kb[k].y;
-        sK[hw][k][2][lane] = Kb[k].z;
-      }
-      if (L.irregular)
+        for (int k = 0; k < 5; ++k) b[k] = sm.B[lane][k][c4];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          sK[hw][5 + k][0][lane] = Kreg[k].x;
-          sK[hw][5 + k][1][lane] = Kreg[k].y;
-          sK[hw][5 + k][2][lane] = Kreg[k].z;
+        for (int j = 0; j < 4; ++j) {
+          const T bk0 = (&b[0].x)[j], bk1 = (&b[1].x)[j], bk2 = (&b[2].x)[j], bk3 = (&b[3].x)[j],
+                  bk4 = (&b[4].x)[j];
+          Q4<T> t;
+          t.x = bk0 * Kb[0].x + bk1 * Kb[1].x + bk2 * Kb[2].x + bk3 * Kb[3].x + bk4 * Kb[4].x;
+          t.y = bk0 * Kb[0].y + bk1 * Kb[1].y + bk2 * Kb[2].y + bk3 * Kb[3].y + bk4 * Kb[4].y;
+          t.z = bk0 * Kb[0].z + bk1 * Kb[1].z + bk2 * Kb[2].z + bk3 * Kb[3].z + bk4 * Kb[4].z;
+          t.w = T(0);
+          sm.Tc[hw][lane][4 * c4 + j] = t;
+          if (reg_alpha) {
+            // igrad's box-scale derivative takes the angle-term adjoint with
+            // one more alpha factor (src/grad.C:7414-7421).
+            const Q4<T> xx = sm.X[hw][4 * c4 + j];
+            dreg[0] += (bk0 * Kreg[0].x + bk1 * Kreg[1].x) * xx.x;
+            dreg[1] += (bk0 * Kreg[0].y + bk1 * Kreg[1].y) * xx.y;
+            dreg[2] += (bk0 * Kreg[0].z + bk1 * Kreg[1].z) * xx.z;
+          }
         }
+      }
     }
     __syncwarp(hmask);
 
-    // ---- lanes as control points: contract the adjoint back onto the one-ring
-    double da[3] = {0, 0, 0};
+    // ---- 3. lanes as control points
+    T da[3] = {0, 0, 0};
     if (lane < NCP) {
-      T G[3] = {0, 0, 0};
-#pragma unroll 5
-      for (int p = 0; p < NPT; ++p)
+      T G0 = 0, G1 = 0, G2 = 0;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const T b = sB[(k * NCP + lane) * NPT + p];
-          G[0] += b * sK[hw][k][0][p];
-          G[1] += b * sK[hw][k][1][p];
-          G[2] += b * sK[hw][k][2][p];
-        }
+      for (int p = 0; p < NPT; ++p) {
+        const Q4<T> t = sm.Tc[hw][p][lane];
+        G0 += t.x;
+        G1 += t.y;
+        G2 += t.z;
+      }
       const int d = dest[(size_t)f * NCP + lane];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        partial[3 * (size_t)d + c] = (T)(alpha[c] * (double)G[c]);
-        da[c] = (double)G[c] * (X[c] - ucen[c]);
-      }
-      if (L.irregular && P.k_reg != 0.0) {
-        // igrad adds the angle-term adjoint to dE/dalpha with one more alpha
-        // factor (src/grad.C:7414-7421): add (alpha-1) times that part.
-        T Gr[3] = {0, 0, 0};
-        for (int p = 0; p < NPT; ++p)
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            const T b = sB[(k * NCP + lane) * NPT + p];
-            Gr[0] += b * sK[hw][5 + k][0][p];
-            Gr[1] += b * sK[hw][5 + k][1][p];
-            Gr[2] += b * sK[hw][5 + k][2][p];
-          }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) da[c] += (alpha[c] - 1.0) * (double)Gr[c] * (X[c] - ucen[c]);
-      }
+      partial[3 * (size_t)d] = alpha[0] * G0;
+      partial[3 * (size_t)d + 1] = alpha[1] * G1;
+      partial[3 * (size_t)d + 2] = alpha[2] * G2;
+      // dE/dalpha_c = sum_x G_xc (X - X_0)_xc: the patch gradient sums to
+      // zero, so coordinates relative to the corner give the same sum.
+      da[0] = G0 * xl[0] * ialpha[0];
+      da[1] = G1 * xl[1] * ialpha[1];
+      da[2] = G2 * xl[2] * ialpha[2];
     }
-    // ---- per-face sums (fixed butterfly order)
-    double e3[3] = {(double)ea, (double)ec, (double)er};
+    if (reg_alpha)
 #pragma unroll
-    for (int off = 8; off >= 1; off >>= 1) {
+      for (int c = 0; c < 3; ++c) da[c] += (alpha[c] - T(1)) * ialpha[c] * dreg[c];
+    T e3[3] = {ea, ec, er};
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         e3[c] += __shfl_xor_sync(hmask, e3[c], off, 16);
         da[c] += __shfl_xor_sync(hmask, da[c], off, 16);
       }
-    }
-    if (lane == 0) {
-      double *t = terms + 6 * (size_t)(L.face_base + f);
-      t[0] = e3[0]; t[1] = e3[1]; t[2] = e3[2];
-      t[3] = da[0]; t[4] = da[1]; t[5] = da[2];
-      if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
-    }
+    acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+    acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
+    if (lane == 0 && !isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
     __syncwarp(hmask);
   }
-}
-
-template <typename T>
-__global__ void gather_kernel(int nv, const T *__restrict__ partial, const int *__restrict__ off,
-                              double *__restrict__ g) {
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
-    double a0 = 0, a1 = 0, a2 = 0;
-    for (int s = off[v]; s < off[v + 1]; ++s) {
-      a0 += (double)partial[3 * (size_t)s];
-      a1 += (double)partial[3 * (size_t)s + 1];
-      a2 += (double)partial[3 * (size_t)s + 2];
-    }
-    g[3 * (size_t)v] += a0;
-    g[3 * (size_t)v + 1] += a1;
-    g[3 * (size_t)v + 2] += a2;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) sm.red[hw][q] = acc.get(q);
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double s = 0;
+#pragma unroll
+    for (int h = 0; h < HW; ++h) s += sm.red[h][threadIdx.x];
+    blockpart[6 * (size_t)(L.block_base + blockIdx.x) + threadIdx.x] = s;
   }
 }
 
-// One block per mesh; each thread sums a strided subset, then a fixed tree.
-__global__ void reduce_terms_kernel(const int *__restrict__ seg, const double *__restrict__ terms, double *E,
-                                    double *parts, double *galpha) {
+// FP32 hi/lo pairs of the positions for the precision form: r = hi + lo to
+// about 2^-48 relative.
+__global__ void split_positions_kernel(int n, const double *__restrict__ r, float *__restrict__ hi,
+                                       float *__restrict__ lo) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = r[i];
+    const float h = (float)x;
+    hi[i] = h;
+    lo[i] = (float)(x - (double)h);
+  }
+}
+
+// Fixed-order sum of the block partials: E, its three parts, and dE/dalpha
+// (added into galpha). In a run it also records E for this step, flags
+// non-finite or diverging energies, and advances the run index.
+__global__ void finish_kernel(int nblk, const double *__restrict__ blockpart, double *E, double *parts,
+                              double *galpha, double *energies, uint64_t *cnt, double threshold, int *status) {
   __shared__ double red[6][256];
-  const int m = blockIdx.x;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int f = seg[m] + threadIdx.x; f < seg[m + 1]; f += blockDim.x)
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
 #pragma unroll
-    for (int q = 0; q < 6; ++q) acc[q] += terms[6 * (size_t)f + q];
+    for (int q = 0; q < 6; ++q) a[q] += blockpart[6 * (size_t)b + q];
 #pragma unroll
-  for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = acc[q];
+  for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = a[q];
   __syncthreads();
   for (int width = blockDim.x / 2; width > 0; width >>= 1) {
     if ((int)threadIdx.x < width)
@@ -194,9 +294,41 @@ __global__ void reduce_terms_kernel(const int *__restrict__ seg, const double *_
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    if (E) E[m] = red[0][0] + red[1][0] + red[2][0];
-    if (parts) { parts[3 * m] = red[0][0]; parts[3 * m + 1] = red[1][0]; parts[3 * m + 2] = red[2][0]; }
-    if (galpha) { galpha[3 * m] += red[3][0]; galpha[3 * m + 1] += red[4][0]; galpha[3 * m + 2] += red[5][0]; }
+    const double e = red[0][0] + red[1][0] + red[2][0];
+    if (E) E[0] = e;
+    if (parts) { parts[0] = red[0][0]; parts[1] = red[1][0]; parts[2] = red[2][0]; }
+    if (galpha) { galpha[0] += red[3][0]; galpha[1] += red[4][0]; galpha[2] += red[5][0]; }
+    if (!isfinite(e)) atomicOr(status, kStatusNonFinite);
+    if (energies) {
+      const uint64_t idx = cnt[1];
+      energies[idx] = e;
+      if (threshold > 0 && idx > 0 && e - energies[idx - 1] > threshold) atomicOr(status, kStatusDiverged);
+      cnt[1] = idx + 1;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void vertex_gradient(const T *__restrict__ partial, const int *__restrict__ off, int v,
+                                                double gg[3]) {
+  double a0 = 0, a1 = 0, a2 = 0;
+  for (int s = off[v]; s < off[v + 1]; ++s) {
+    a0 += (double)partial[3 * (size_t)s];
+    a1 += (double)partial[3 * (size_t)s + 1];
+    a2 += (double)partial[3 * (size_t)s + 2];
+  }
+  gg[0] = a0; gg[1] = a1; gg[2] = a2;
+}
+
+template <typename T>
+__global__ void gather_kernel(int nv, const T *__restrict__ partial, const int *__restrict__ off,
+                              double *__restrict__ g) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    double gg[3];
+    vertex_gradient(partial, off, v, gg);
+    g[3 * (size_t)v] += gg[0];
+    g[3 * (size_t)v + 1] += gg[1];
+    g[3 * (size_t)v + 2] += gg[2];
   }
 }
 
@@ -230,32 +362,51 @@ __device__ __forceinline__ void kick(const StepArgs &a, const double n[3], doubl
   }
 }
 
-__global__ void step_local_kernel(int nv, StepArgs a, const uint64_t *__restrict__ step, double *__restrict__ r,
-                                  double *__restrict__ p, const double *__restrict__ g, const int *__restrict__ status) {
+// Step index of the current step: the run's first step plus the run index,
+// which finish_kernel has already advanced past this step.
+__device__ __forceinline__ uint64_t current_step(const uint64_t *cnt) { return cnt[0] + cnt[1] - 1; }
+
+// Gather fused with the vertex-local update (overdamped BD, or the leapfrog
+// kinds with identity mass).
+template <typename T>
+__global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const int *__restrict__ off, StepArgs a,
+                                   const uint64_t *__restrict__ cnt, double *__restrict__ r, double *__restrict__ p,
+                                   float *__restrict__ rhi, float *__restrict__ rlo, const int *__restrict__ status) {
   if (*status) return;
-  const uint64_t st = *step;
+  const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
-    double n[3], gg[3] = {g[3 * (size_t)v], g[3 * (size_t)v + 1], g[3 * (size_t)v + 2]};
+    double gg[3], n[3];
+    vertex_gradient(partial, off, v, gg);
     normals3(a.seed, a.stream, st, v, n);
+    double rn[3] = {r[3 * (size_t)v], r[3 * (size_t)v + 1], r[3 * (size_t)v + 2]};
     if (a.kind == 0) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) r[3 * (size_t)v + c] += -a.mob_dt * gg[c] + a.sigma * n[c];
+      for (int c = 0; c < 3; ++c) rn[c] += -a.mob_dt * gg[c] + a.sigma * n[c];
     } else {
       double pp[3] = {p[3 * (size_t)v], p[3 * (size_t)v + 1], p[3 * (size_t)v + 2]};
       kick(a, n, pp, gg);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        r[3 * (size_t)v + c] += pp[c] * a.AK;  // identity M^-1
+        rn[c] += pp[c] * a.AK;  // identity M^-1
         p[3 * (size_t)v + c] = (a.kind == 1) ? 0.0 : pp[c];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      r[3 * (size_t)v + c] = rn[c];
+      if (rhi) {
+        const float h = (float)rn[c];
+        rhi[3 * (size_t)v + c] = h;
+        rlo[3 * (size_t)v + c] = (float)(rn[c] - (double)h);
       }
     }
   }
 }
 
-__global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ step, double *__restrict__ p,
+__global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ cnt, double *__restrict__ p,
                             const double *__restrict__ g, const int *__restrict__ status) {
   if (*status) return;
-  const uint64_t st = *step;
+  const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
     double n[3], gg[3] = {g[3 * (size_t)v], g[3 * (size_t)v + 1], g[3 * (size_t)v + 2]};
     normals3(a.seed, a.stream, st, v, n);
@@ -267,11 +418,18 @@ __global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ ste
 }
 
 __global__ void drift_kernel(int nv, StepArgs a, double *__restrict__ r, double *__restrict__ p,
-                             const double *__restrict__ qdot, const int *__restrict__ status) {
+                             const double *__restrict__ qdot, float *__restrict__ rhi, float *__restrict__ rlo,
+                             const int *__restrict__ status) {
   if (*status) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nv; i += gridDim.x * blockDim.x) {
-    r[i] += qdot[i] * a.AK;
+    const double x = r[i] + qdot[i] * a.AK;
+    r[i] = x;
     if (a.kind == 1) p[i] = 0.0;
+    if (rhi) {
+      const float h = (float)x;
+      rhi[i] = h;
+      rlo[i] = (float)(x - (double)h);
+    }
   }
 }
 
@@ -319,20 +477,6 @@ __global__ void spmv_kernel(int nrow, const int *__restrict__ row_ptr, const int
   }
 }
 
-__global__ void record_energy_kernel(const double *E, double *energies, const uint64_t *runidx, double threshold,
-                                     int *status) {
-  const uint64_t idx = *runidx;
-  const double e = E[0];
-  if (energies) energies[idx] = e;
-  if (!isfinite(e)) atomicOr(status, kStatusNonFinite);
-  if (threshold > 0 && idx > 0 && energies && e - energies[idx - 1] > threshold) atomicOr(status, kStatusDiverged);
-}
-
-__global__ void advance_step_kernel(uint64_t *step, uint64_t *runidx) {
-  *step += 1;
-  *runidx += 1;
-}
-
 }  // namespace dev
 
 static int grid_for(int n, int per_block) {
@@ -340,25 +484,68 @@ static int grid_for(int n, int per_block) {
   return g < 1 ? 1 : g;
 }
 
+template <typename T, int NCP, int NPT>
+static int face_grid_size(int nfaces) {
+  // Persistent grid: as many blocks as fit on the device at once (a fixed
+  // number, so the face-to-block assignment and the sums' order are fixed).
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_kernel<T, NCP, NPT>,
+                                                  dev::FaceCfg<T>::threads, 0);
+    cached = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  int need = grid_for(nfaces, dev::FaceCfg<T>::half_warps);
+  return need < cached ? need : cached;
+}
+
+template <typename T>
+int face_blocks(int nfaces, int ncp, int npt) {
+  if (nfaces <= 0) return 0;
+  if (ncp == 12 && npt == 15) return face_grid_size<T, 12, 15>(nfaces);
+  if (ncp == 11 && npt == 16) return face_grid_size<T, 11, 16>(nfaces);
+  if (ncp == 13 && npt == 16) return face_grid_size<T, 13, 16>(nfaces);
+  return 0;
+}
+template int face_blocks<double>(int, int, int);
+template int face_blocks<float>(int, int, int);
+
 template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
-                         const double *r, T *partial, double *terms, int *status, int grid, cudaStream_t s) {
+                         const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
+                         int *status, int grid, cudaStream_t s) {
   if (L.nfaces <= 0) return cudaSuccess;
-  if (grid <= 0) grid = grid_for(L.nfaces, dev::kHalfWarps);
+  constexpr int NT = dev::FaceCfg<T>::threads;
   if (ncp == 12 && npt == 15)
-    dev::face_kernel<T, 12, 15><<<grid, dev::kThreads, 0, s>>>(L, dest, P, r, partial, terms, status);
+    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
   else if (ncp == 11 && npt == 16)
-    dev::face_kernel<T, 11, 16><<<grid, dev::kThreads, 0, s>>>(L, dest, P, r, partial, terms, status);
+    dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
   else if (ncp == 13 && npt == 16)
-    dev::face_kernel<T, 13, 16><<<grid, dev::kThreads, 0, s>>>(L, dest, P, r, partial, terms, status);
+    dev::face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 template cudaError_t launch_faces<double>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
-                                          const double *, double *, double *, int *, int, cudaStream_t);
+                                          const double *, const float *, const float *, double *, double *, int *,
+                                          int, cudaStream_t);
 template cudaError_t launch_faces<float>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
-                                         const double *, float *, double *, int *, int, cudaStream_t);
+                                         const double *, const float *, const float *, float *, double *, int *, int,
+                                         cudaStream_t);
+
+cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  dev::split_positions_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, r, hi, lo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish(int nblk, const double *blockpart, double *E, double *parts, double *galpha,
+                          double *energies, uint64_t *cnt, double threshold, int *status, cudaStream_t s) {
+  dev::finish_kernel<<<1, 256, 0, s>>>(nblk, blockpart, E, parts, galpha, energies, cnt, threshold, status);
+  return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_gather(int nv, const T *partial, const int *off, double *g, cudaStream_t s) {
@@ -369,25 +556,25 @@ cudaError_t launch_gather(int nv, const T *partial, const int *off, double *g, c
 template cudaError_t launch_gather<double>(int, const double *, const int *, double *, cudaStream_t);
 template cudaError_t launch_gather<float>(int, const float *, const int *, double *, cudaStream_t);
 
-cudaError_t launch_reduce_terms(int nmesh, const int *seg, const double *terms, double *E, double *parts,
-                                double *galpha, cudaStream_t s) {
-  dev::reduce_terms_kernel<<<nmesh, 256, 0, s>>>(seg, terms, E, parts, galpha);
+template <typename T>
+cudaError_t launch_gather_step(int nv, const T *partial, const int *off, const StepArgs &a, const uint64_t *cnt,
+                               double *r, double *p, float *rhi, float *rlo, const int *status, cudaStream_t s) {
+  dev::gather_step_kernel<T><<<grid_for(nv, 256), 256, 0, s>>>(nv, partial, off, a, cnt, r, p, rhi, rlo, status);
   return cudaGetLastError();
 }
+template cudaError_t launch_gather_step<double>(int, const double *, const int *, const StepArgs &, const uint64_t *,
+                                                double *, double *, float *, float *, const int *, cudaStream_t);
+template cudaError_t launch_gather_step<float>(int, const float *, const int *, const StepArgs &, const uint64_t *,
+                                               double *, double *, float *, float *, const int *, cudaStream_t);
 
-cudaError_t launch_step_local(int nv, const StepArgs &a, const uint64_t *step, double *r, double *p, const double *g,
-                              const int *status, cudaStream_t s) {
-  dev::step_local_kernel<<<grid_for(nv, 256), 256, 0, s>>>(nv, a, step, r, p, g, status);
-  return cudaGetLastError();
-}
-cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *step, double *p, const double *g, const int *status,
+cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *cnt, double *p, const double *g, const int *status,
                         cudaStream_t s) {
-  dev::kick_kernel<<<grid_for(nv, 256), 256, 0, s>>>(nv, a, step, p, g, status);
+  dev::kick_kernel<<<grid_for(nv, 256), 256, 0, s>>>(nv, a, cnt, p, g, status);
   return cudaGetLastError();
 }
-cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, const int *status,
-                         cudaStream_t s) {
-  dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, status);
+cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, float *rhi, float *rlo,
+                         const int *status, cudaStream_t s) {
+  dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, rhi, rlo, status);
   return cudaGetLastError();
 }
 cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const double *val, const double *scalev,
@@ -399,15 +586,6 @@ cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const doub
   if (grid > 152 * 16) grid = 152 * 16;
   dev::spmv_kernel<<<grid, 32 * warps_per_block, 0, s>>>(nrow, row_ptr, col, val, scalev, scale, alphas, in, out,
                                                         accumulate);
-  return cudaGetLastError();
-}
-cudaError_t launch_record_energy(const double *E, double *energies, const uint64_t *runidx, double threshold,
-                                 int *status, cudaStream_t s) {
-  dev::record_energy_kernel<<<1, 1, 0, s>>>(E, energies, runidx, threshold, status);
-  return cudaGetLastError();
-}
-cudaError_t launch_advance_step(uint64_t *step, uint64_t *runidx, cudaStream_t s) {
-  dev::advance_step_kernel<<<1, 1, 0, s>>>(step, runidx);
   return cudaGetLastError();
 }
 
