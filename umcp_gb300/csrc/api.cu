@@ -300,6 +300,9 @@ struct umcp_mesh {
   int nblocks = 0;
   DevBuf r, g, p, qdot, E, parts, status, cnt;  // cnt: {first step of the run, run index}
   DevBuf rhi, rlo;  // FP32 hi/lo pairs of r (precision form)
+  DevBuf r_eval;    // staging for host-pointer energy/gradient calls (keeps the resident state)
+  DevBuf done;      // finished-block counter of the face pass
+  bool split_valid = false;  // rhi/rlo hold the resident state r
   double kT = 0.592186663194;  // kcal/mol at the params' temperature (src/hd.C:142-143)
   DevBuf energies;
   size_t energies_cap = 0;
@@ -472,6 +475,9 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   UMCP_CUDA(m->parts.alloc(3 * sizeof(double)));
   UMCP_CUDA(m->status.alloc(sizeof(int)));
   UMCP_CUDA(m->cnt.alloc(2 * sizeof(uint64_t)));
+  UMCP_CUDA(m->r_eval.alloc(nst * sizeof(double)));
+  UMCP_CUDA(m->done.alloc(sizeof(unsigned)));
+  UMCP_CUDA(cudaMemset(m->done.p, 0, sizeof(unsigned)));
   UMCP_CUDA(m->alphas.alloc(3 * sizeof(double)));
   UMCP_CUDA(cudaMemset(m->p.p, 0, m->p.bytes));
   UMCP_CUDA(cudaMemset(m->status.p, 0, sizeof(int)));
@@ -488,6 +494,7 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     UMCP_CUDA(m->rlo.alloc(3 * (size_t)ME.nv * sizeof(float)));
     UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), 0));
     UMCP_CUDA(cudaDeviceSynchronize());
+    m->split_valid = true;
   }
   *out = m.release();
   return UMCP_OK;
@@ -510,9 +517,12 @@ extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *
 // Queue energy+gradient of state d_r: E -> d_E (and parts), gradient ADDED
 // into d_g (3*nv+3). d_g may be null to skip the gather.
 template <typename T>
-static cudaError_t queue_faces(umcp_mesh *m, const double *d_r) {
+static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs *fin) {
   cudaStream_t s = m->ctx->stream;
-  for (auto &G : m->groups) {
+  FinishArgs none{};
+  for (size_t gi = 0; gi < m->groups.size(); ++gi) {
+    auto &G = m->groups[gi];
+    const bool last = (gi + 1 == m->groups.size());
     dev::FaceLaunch L;
     L.nfaces = G->nfaces;
     L.block_base = G->block_base;
@@ -529,7 +539,7 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r) {
     L.irregular = G->irregular;
     cudaError_t e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(),
                                     m->rlo.as<float>(), m->partial.as<T>(), m->blockpart.as<double>(),
-                                    m->status.as<int>(), G->nblocks, s);
+                                    m->status.as<int>(), G->nblocks, (last && fin) ? *fin : none, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -542,12 +552,20 @@ static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_
                                      bool faces_only) {
   cudaStream_t s = m->ctx->stream;
   cudaError_t e = cudaSuccess;
-  if (sizeof(T) == 4 && !faces_only) e = launch_split_positions(3 * m->nv, d_r, m->rhi.as<float>(), m->rlo.as<float>(), s);
+  if (faces_only) {
+    if (sizeof(T) == 4 && !m->split_valid)
+      e = launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s);
+    m->split_valid = true;
+    return e == cudaSuccess ? queue_faces<T>(m, m->r.as<double>(), nullptr) : e;
+  }
+  if (sizeof(T) == 4) {
+    e = launch_split_positions(3 * m->nv, d_r, m->rhi.as<float>(), m->rlo.as<float>(), s);
+    m->split_valid = (d_r == m->r.as<double>());
+  }
   if (e != cudaSuccess) return e;
-  e = queue_faces<T>(m, d_r);
-  if (e != cudaSuccess || faces_only) return e;
-  e = launch_finish(m->nblocks, m->blockpart.as<double>(), d_E, d_parts, d_g ? d_g + 3 * m->nv : nullptr, nullptr,
-                    nullptr, 0.0, m->status.as<int>(), s);
+  FinishArgs fin{m->nblocks, d_E, d_parts, d_g ? d_g + 3 * m->nv : nullptr, nullptr, nullptr, 0.0,
+                 m->status.as<int>(), m->done.as<unsigned>()};
+  e = queue_faces<T>(m, d_r, &fin);
   if (e != cudaSuccess) return e;
   if (d_g) e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), d_g, s);
   return e;
@@ -574,10 +592,11 @@ static umcp_status host_energy_grad(umcp_mesh *m, const double *r, double *E, do
   cudaStream_t s = m->ctx->stream;
   const size_t nst = 3 * (size_t)m->nv + 3;
   memcpy(m->h_stage, r, nst * sizeof(double));
-  UMCP_CUDA(cudaMemcpyAsync(m->r.p, m->h_stage, nst * sizeof(double), cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(cudaMemcpyAsync(m->r_eval.p, m->h_stage, nst * sizeof(double), cudaMemcpyHostToDevice, s));
   UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), s));
   if (g) UMCP_CUDA(cudaMemsetAsync(m->g.p, 0, nst * sizeof(double), s));
-  UMCP_CUDA(queue_eg(m, m->r.as<double>(), m->E.as<double>(), m->parts.as<double>(), g ? m->g.as<double>() : nullptr));
+  UMCP_CUDA(queue_eg(m, m->r_eval.as<double>(), m->E.as<double>(), m->parts.as<double>(),
+                     g ? m->g.as<double>() : nullptr));
   double e_parts[4];
   UMCP_CUDA(cudaMemcpyAsync(&e_parts[0], m->E.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   UMCP_CUDA(cudaMemcpyAsync(&e_parts[1], m->parts.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -617,9 +636,9 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
   info->n_points = npts;
   info->n_slots = m->nslots;
   const int groups = (int)m->groups.size();
-  // face kernels + finish + fused gather/update; the mass path replaces the
-  // fused kernel with gather + kick + spmv + drift.
-  info->kernels_per_step = groups + 2;
+  // face kernels (the last one also sums the energy) + fused gather/update;
+  // the mass path replaces the fused kernel with memset + gather + kick + spmv + drift.
+  info->kernels_per_step = groups + 1;
   info->kernels_per_step_mass = groups + 5;
   info->precision = m->precision;
   return UMCP_OK;
@@ -699,9 +718,11 @@ extern "C" umcp_status umcp_state_set(umcp_mesh *m, const double *r, const doubl
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
   const size_t nst = 3 * (size_t)m->nv + 3;
   if (r) UMCP_CUDA(cudaMemcpyAsync(m->r.p, r, nst * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
-  if (r && m->precision == UMCP_FP32_CENTRED)
+  if (r && m->precision == UMCP_FP32_CENTRED) {
     UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(),
                                      m->ctx->stream));
+    m->split_valid = true;
+  }
   if (p) UMCP_CUDA(cudaMemcpyAsync(m->p.p, p, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
   else UMCP_CUDA(cudaMemsetAsync(m->p.p, 0, (nst - 3) * sizeof(double), m->ctx->stream));
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
@@ -743,10 +764,9 @@ static umcp_status make_step_args(umcp_mesh *m, const umcp_integrator *it, StepA
 template <typename T>
 static cudaError_t queue_step_t(umcp_mesh *m, const StepArgs &a, int use_mass, double threshold) {
   cudaStream_t s = m->ctx->stream;
-  cudaError_t e = queue_faces<T>(m, m->r.as<double>());
-  if (e != cudaSuccess) return e;
-  e = launch_finish(m->nblocks, m->blockpart.as<double>(), m->E.as<double>(), m->parts.as<double>(), nullptr,
-                    m->energies.as<double>(), m->cnt.as<uint64_t>(), threshold, m->status.as<int>(), s);
+  FinishArgs fin{m->nblocks, m->E.as<double>(), m->parts.as<double>(), nullptr, m->energies.as<double>(),
+                 m->cnt.as<uint64_t>(), threshold, m->status.as<int>(), m->done.as<unsigned>()};
+  cudaError_t e = queue_faces<T>(m, m->r.as<double>(), &fin);
   if (e != cudaSuccess) return e;
   if (a.kind == 0 || !use_mass)
     return launch_gather_step<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), a, m->cnt.as<uint64_t>(),
@@ -810,8 +830,9 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
     UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
     m->energies_cap = (size_t)n_steps;
   }
-  if (m->precision == UMCP_FP32_CENTRED)
+  if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
     UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
+  m->split_valid = true;  // every step rewrites the pairs of the new positions
   m->h_cnt[0] = step0;
   m->h_cnt[1] = 0;
   UMCP_CUDA(cudaMemcpyAsync(m->cnt.p, m->h_cnt, 2 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));

@@ -11,6 +11,19 @@ namespace umcp {
 // Status bits written by kernels into the mesh's device status word.
 enum : int { kStatusNonFinite = 1, kStatusDiverged = 2 };
 
+// Where and how the block partials of a face pass are summed (see
+// launch_finish). done: device counter of finished blocks, zero between
+// launches; when non-null, the last block of that face launch does the sum.
+struct FinishArgs {
+  int nblk;            // block-partial rows to sum (all face launches of the mesh)
+  double *E, *parts, *galpha;
+  double *energies;    // run only: energies[cnt[1]] = E, cnt[1] += 1
+  uint64_t *cnt;
+  double threshold;    // energy rise that flags divergence (<= 0: off)
+  int *status;
+  unsigned *done;
+};
+
 // Persistent grid of the face pass for one patch type (fixed per device and
 // face count, so the order of every sum is fixed).
 template <typename T>
@@ -25,16 +38,15 @@ int face_blocks(int nfaces, int ncp, int npt);
 template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
                          const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
-                         int *status, int grid, cudaStream_t s);
+                         int *status, int grid, const FinishArgs &fin, cudaStream_t s);
 
 // hi[i] + lo[i] = r[i] to about 2^-48 relative (the precision form's positions).
 cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s);
 
-// Fixed-order sum of nblk block partials: E, parts (3), galpha (+= 3). With
+// Fixed-order sum of F.nblk block partials: E, parts (3), galpha (+= 3). With
 // energies/cnt given (a run): energies[cnt[1]] = E, divergence and non-finite
 // flags (src/hd.C:1280-1305), cnt[1] += 1.
-cudaError_t launch_finish(int nblk, const double *blockpart, double *E, double *parts, double *galpha,
-                          double *energies, uint64_t *cnt, double threshold, int *status, cudaStream_t s);
+cudaError_t launch_finish(const FinishArgs &F, const double *blockpart, cudaStream_t s);
 
 // Per vertex: g[3v+c] += sum of its partial slots [off[v], off[v+1]).
 template <typename T>

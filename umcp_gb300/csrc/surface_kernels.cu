@@ -66,6 +66,40 @@ struct HalfWarpSums<float> {
   __device__ __forceinline__ double get(int q) const { return (double)s[q] - (double)c[q]; }
 };
 
+// Fixed-order sum of the block partials, done by one block: thread t sums
+// rows t, t+NT, ..., then a shared-memory tree. Writes E, its parts and
+// dE/dalpha; in a run also records E, flags non-finite or diverging energies
+// (src/hd.C:1280-1305) and advances the run index.
+template <int NT>
+__device__ void finish_sums(const FinishArgs &F, const double *__restrict__ blockpart, double (*red)[NT]) {
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < F.nblk; b += NT)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) a[q] += __ldcg(&blockpart[6 * (size_t)b + q]);
+#pragma unroll
+  for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = a[q];
+  __syncthreads();
+  for (int width = NT / 2; width > 0; width >>= 1) {
+    if ((int)threadIdx.x < width)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + width];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double e = red[0][0] + red[1][0] + red[2][0];
+    if (F.E) F.E[0] = e;
+    if (F.parts) { F.parts[0] = red[0][0]; F.parts[1] = red[1][0]; F.parts[2] = red[2][0]; }
+    if (F.galpha) { F.galpha[0] += red[3][0]; F.galpha[1] += red[4][0]; F.galpha[2] += red[5][0]; }
+    if (!isfinite(e)) atomicOr(F.status, kStatusNonFinite);
+    if (F.energies) {
+      const uint64_t idx = F.cnt[1];
+      F.energies[idx] = e;
+      if (F.threshold > 0 && idx > 0 && e - F.energies[idx - 1] > F.threshold) atomicOr(F.status, kStatusDiverged);
+      F.cnt[1] = idx + 1;
+    }
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T point_data(const double *d64, const float *d32, size_t i) {
   if constexpr (sizeof(T) == 8) return d64[i];
@@ -89,7 +123,7 @@ template <typename T, int NCP, int NPT>
 __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     face_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
                 const float *__restrict__ rhi, const float *__restrict__ rlo, T *__restrict__ partial,
-                double *__restrict__ blockpart, int *__restrict__ status) {
+                double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
   using S = FaceSmem<T, NCP, NPT>;
   constexpr int NC4 = S::NC4, NCPP = S::NCPP, HW = S::HW, NT = FaceCfg<T>::threads;
   __shared__ S sm;
@@ -110,51 +144,78 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
   const bool reg_alpha = L.irregular && P.k_reg != 0.0;
   HalfWarpSums<T> acc;
 
-  for (int f = blockIdx.x * HW + hw; f < L.nfaces; f += gridDim.x * HW) {
+  // Global data of a face, loaded one face ahead (control-point indices two
+  // ahead) so the loads are in flight while the previous face computes.
+  struct Ahead {
+    int img[3] = {0, 0, 0};
+    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};  // precision form
+    double X[3] = {0, 0, 0};                     // plain path (image position)
+    T g0 = 1, rr0 = 0, P2 = 0, Hbar = 0, Pres = 0;
+    int dest = 0;
+  };
+  const int stride = gridDim.x * HW;
+  auto load_cp = [&](int f) -> uint32_t {
+    return (f < L.nfaces && lane < NCP) ? __ldg(&L.cp[(size_t)f * NCP + lane]) : 0u;
+  };
+  auto load_ahead = [&](int f, uint32_t packed, Ahead &a) {
+    if (f >= L.nfaces) return;
+    if (lane < NCP) {
+      const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+      a.img[0] = code % 3 - 1; a.img[1] = (code / 3) % 3 - 1; a.img[2] = code / 9 - 1;
+      if constexpr (sizeof(T) == 8) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          a.X[c] = r[3 * (size_t)v + c] + a.img[0] * P.box[0][c] + a.img[1] * P.box[1][c] + a.img[2] * P.box[2][c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { a.hi[c] = rhi[3 * (size_t)v + c]; a.lo[c] = rlo[3 * (size_t)v + c]; }
+      }
+      a.dest = __ldg(&dest[(size_t)f * NCP + lane]);
+    }
+    if (lane < NPT) {
+      const size_t pi = (size_t)f * NPT + lane;
+      a.g0 = point_data<T>(L.g0, L.g0f, pi);
+      a.rr0 = point_data<T>(L.rr0, L.rr0f, pi);
+    }
+    a.P2 = point_data<T>(L.comp, L.compf, 3 * (size_t)f);
+    a.Hbar = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 1);
+    a.Pres = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 2);
+  };
+  int f = blockIdx.x * HW + hw;
+  Ahead cur, nxt;
+  uint32_t cp_next = load_cp(f + stride);
+  load_ahead(f, load_cp(f), cur);
+
+  for (; f < L.nfaces; f += stride) {
+    const uint32_t cp_after = load_cp(f + 2 * stride);
+    load_ahead(f + stride, cp_next, nxt);
+    cp_next = cp_after;
     // ---- 1. control points, relative to the patch corner
     T xl[3] = {0, 0, 0};
-    {
-      int v = 0, img[3] = {0, 0, 0};
-      if (lane < NCP) {
-        uint32_t packed = L.cp[(size_t)f * NCP + lane];
-        v = (int)(packed & kVertexMask);
-        int code = (int)(packed >> kVertexBits);
-        img[0] = code % 3 - 1; img[1] = (code / 3) % 3 - 1; img[2] = code / 9 - 1;
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double a = __shfl_sync(hmask, cur.X[c], 0, 16);
+        xl[c] = alpha[c] * (cur.X[c] - a);
       }
-      if constexpr (sizeof(T) == 8) {
-        double X[3] = {0, 0, 0};
-        if (lane < NCP)
+    } else {
 #pragma unroll
-          for (int c = 0; c < 3; ++c)
-            X[c] = r[3 * (size_t)v + c] + img[0] * P.box[0][c] + img[1] * P.box[1][c] + img[2] * P.box[2][c];
+      for (int c = 0; c < 3; ++c) {
+        const float ahi = __shfl_sync(hmask, cur.hi[c], 0, 16), alo = __shfl_sync(hmask, cur.lo[c], 0, 16);
+        // lattice shift hi + lo (each term exact: images are -1, 0 or +1)
+        float sh = 0.f, she = 0.f, shl = 0.f;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const double a = __shfl_sync(hmask, X[c], 0, 16);
-          xl[c] = alpha[c] * (X[c] - a);
+        for (int d = 0; d < 3; ++d) {
+          float t, e;
+          two_sum(sh, (float)cur.img[d] * P.box_hi[d][c], t, e);
+          sh = t;
+          she += e;
+          shl += (float)cur.img[d] * P.box_lo[d][c];
         }
-      } else {
-        float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
-        if (lane < NCP)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) { hi[c] = rhi[3 * (size_t)v + c]; lo[c] = rlo[3 * (size_t)v + c]; }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float ahi = __shfl_sync(hmask, hi[c], 0, 16), alo = __shfl_sync(hmask, lo[c], 0, 16);
-          // lattice shift hi + lo (each term exact: images are -1, 0 or +1)
-          float sh = 0.f, she = 0.f, shl = 0.f;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            float t, e;
-            two_sum(sh, (float)img[d] * P.box_hi[d][c], t, e);
-            sh = t;
-            she += e;
-            shl += (float)img[d] * P.box_lo[d][c];
-          }
-          float s1, e1, s2, e2;
-          two_sum(hi[c], sh, s1, e1);
-          two_sum(s1, -ahi, s2, e2);
-          xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((lo[c] - alo) + (she + shl))));
-        }
+        float s1, e1, s2, e2;
+        two_sum(cur.hi[c], sh, s1, e1);
+        two_sum(s1, -ahi, s2, e2);
+        xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl))));
       }
     }
     if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
@@ -179,12 +240,9 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
           K[k].z += b.x * x0.z + b.y * x1.z + b.z * x2.z + b.w * x3.z;
         }
       }
-      const size_t pi = (size_t)f * NPT + lane;
-      const T g0 = point_data<T>(L.g0, L.g0f, pi), rr0 = point_data<T>(L.rr0, L.rr0f, pi);
-      const T P2 = point_data<T>(L.comp, L.compf, 3 * (size_t)f), Hbar = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 1),
-              Pres = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 2);
       Vec3<T> Kb[5], Kreg[2];
-      point_adjoint<T>(K, sm.W[lane], g0, rr0, dudv, P2, Hbar, Pres, kc, KA, kg, k_reg, &ea, &ec, &er, Kb, Kreg);
+      point_adjoint<T>(K, sm.W[lane], cur.g0, cur.rr0, dudv, cur.P2, cur.Hbar, cur.Pres, kc, KA, kg, k_reg, &ea, &ec,
+                       &er, Kb, Kreg);
 #pragma unroll 1
       for (int c4 = 0; c4 < NC4; ++c4) {
         Q4<T> b[5];
@@ -224,7 +282,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
         G1 += t.y;
         G2 += t.z;
       }
-      const int d = dest[(size_t)f * NCP + lane];
+      const int d = cur.dest;
       partial[3 * (size_t)d] = alpha[0] * G0;
       partial[3 * (size_t)d + 1] = alpha[1] * G1;
       partial[3 * (size_t)d + 2] = alpha[2] * G2;
@@ -248,6 +306,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
     acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
     if (lane == 0 && !isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
+    cur = nxt;
     __syncwarp(hmask);
   }
   if (lane == 0)
@@ -259,6 +318,21 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
 #pragma unroll
     for (int h = 0; h < HW; ++h) s += sm.red[h][threadIdx.x];
     blockpart[6 * (size_t)(L.block_base + blockIdx.x) + threadIdx.x] = s;
+  }
+  if (fin.done) {
+    // The last block of the mesh's last face launch to finish sums all block
+    // partials (the order of that sum does not depend on which block it is).
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      static_assert(sizeof(sm.Tc) >= sizeof(double) * 6 * NT, "finish scratch must fit in the transpose buffer");
+      finish_sums<NT>(fin, blockpart, reinterpret_cast<double(*)[NT]>(&sm.Tc[0][0][0]));
+      if (threadIdx.x == 0) *fin.done = 0u;
+    }
   }
 }
 
@@ -274,50 +348,38 @@ __global__ void split_positions_kernel(int n, const double *__restrict__ r, floa
   }
 }
 
-// Fixed-order sum of the block partials: E, its three parts, and dE/dalpha
-// (added into galpha). In a run it also records E for this step, flags
-// non-finite or diverging energies, and advances the run index.
-__global__ void finish_kernel(int nblk, const double *__restrict__ blockpart, double *E, double *parts,
-                              double *galpha, double *energies, uint64_t *cnt, double threshold, int *status) {
+// Stand-alone form of the block-partial sum (used when the face launches do
+// not finish themselves).
+__global__ void finish_kernel(FinishArgs F, const double *__restrict__ blockpart) {
   __shared__ double red[6][256];
-  double a[6] = {0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-#pragma unroll
-    for (int q = 0; q < 6; ++q) a[q] += blockpart[6 * (size_t)b + q];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) red[q][threadIdx.x] = a[q];
-  __syncthreads();
-  for (int width = blockDim.x / 2; width > 0; width >>= 1) {
-    if ((int)threadIdx.x < width)
-#pragma unroll
-      for (int q = 0; q < 6; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + width];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const double e = red[0][0] + red[1][0] + red[2][0];
-    if (E) E[0] = e;
-    if (parts) { parts[0] = red[0][0]; parts[1] = red[1][0]; parts[2] = red[2][0]; }
-    if (galpha) { galpha[0] += red[3][0]; galpha[1] += red[4][0]; galpha[2] += red[5][0]; }
-    if (!isfinite(e)) atomicOr(status, kStatusNonFinite);
-    if (energies) {
-      const uint64_t idx = cnt[1];
-      energies[idx] = e;
-      if (threshold > 0 && idx > 0 && e - energies[idx - 1] > threshold) atomicOr(status, kStatusDiverged);
-      cnt[1] = idx + 1;
-    }
-  }
+  finish_sums<256>(F, blockpart, red);
 }
 
+// Sum of a vertex's gradient partials in slot order: FP64 in the plain path,
+// FP32 with Kahan compensation in the precision form.
 template <typename T>
 __device__ __forceinline__ void vertex_gradient(const T *__restrict__ partial, const int *__restrict__ off, int v,
                                                 double gg[3]) {
-  double a0 = 0, a1 = 0, a2 = 0;
-  for (int s = off[v]; s < off[v + 1]; ++s) {
-    a0 += (double)partial[3 * (size_t)s];
-    a1 += (double)partial[3 * (size_t)s + 1];
-    a2 += (double)partial[3 * (size_t)s + 2];
+  if constexpr (sizeof(T) == 8) {
+    double a0 = 0, a1 = 0, a2 = 0;
+    for (int s = off[v]; s < off[v + 1]; ++s) {
+      a0 += partial[3 * (size_t)s];
+      a1 += partial[3 * (size_t)s + 1];
+      a2 += partial[3 * (size_t)s + 2];
+    }
+    gg[0] = a0; gg[1] = a1; gg[2] = a2;
+  } else {
+    float s3[3] = {0, 0, 0}, c3[3] = {0, 0, 0};
+    for (int s = off[v]; s < off[v + 1]; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float y = partial[3 * (size_t)s + c] - c3[c], t = s3[c] + y;
+        c3[c] = (t - s3[c]) - y;
+        s3[c] = t;
+      }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gg[c] = (double)s3[c] - (double)c3[c];
   }
-  gg[0] = a0; gg[1] = a1; gg[2] = a2;
 }
 
 template <typename T>
@@ -330,6 +392,22 @@ __global__ void gather_kernel(int nv, const T *__restrict__ partial, const int *
     g[3 * (size_t)v + 1] += gg[1];
     g[3 * (size_t)v + 2] += gg[2];
   }
+}
+
+// Three unit normals per vertex from two Philox draws (Box-Muller). The
+// plain path transforms in FP64 (bit-for-bit the oracle's draws up to libm
+// rounding); the precision form in FP32 from 24-bit uniforms.
+__device__ __forceinline__ void normals3_f32(uint64_t seed, uint32_t stream, uint64_t step, int v, double n[3]) {
+  philox_out o = philox4x32_10((uint32_t)v, (uint32_t)step, (uint32_t)(step >> 32), stream, (uint32_t)seed,
+                               (uint32_t)(seed >> 32));
+  const float k = 1.0f / 16777216.0f;
+  float u1 = ((float)(o.v[0] >> 8) + 0.5f) * k, u2 = ((float)(o.v[1] >> 8) + 0.5f) * k;
+  float u3 = ((float)(o.v[2] >> 8) + 0.5f) * k, u4 = ((float)(o.v[3] >> 8) + 0.5f) * k;
+  float rad = sqrtf(-2.0f * logf(u1)), sn, cs;
+  sincospif(2.0f * u2, &sn, &cs);
+  n[0] = rad * cs;
+  n[1] = rad * sn;
+  n[2] = sqrtf(-2.0f * logf(u3)) * cospif(2.0f * u4);
 }
 
 __device__ __forceinline__ void normals3(uint64_t seed, uint32_t stream, uint64_t step, int v, double n[3]) {
@@ -377,7 +455,8 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
     double gg[3], n[3];
     vertex_gradient(partial, off, v, gg);
-    normals3(a.seed, a.stream, st, v, n);
+    if constexpr (sizeof(T) == 8) normals3(a.seed, a.stream, st, v, n);
+    else normals3_f32(a.seed, a.stream, st, v, n);
     double rn[3] = {r[3 * (size_t)v], r[3 * (size_t)v + 1], r[3 * (size_t)v + 2]};
     if (a.kind == 0) {
 #pragma unroll
@@ -515,25 +594,25 @@ template int face_blocks<float>(int, int, int);
 template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
                          const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
-                         int *status, int grid, cudaStream_t s) {
+                         int *status, int grid, const FinishArgs &fin, cudaStream_t s) {
   if (L.nfaces <= 0) return cudaSuccess;
   constexpr int NT = dev::FaceCfg<T>::threads;
   if (ncp == 12 && npt == 15)
-    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
+    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
   else if (ncp == 11 && npt == 16)
-    dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
+    dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
   else if (ncp == 13 && npt == 16)
-    dev::face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status);
+    dev::face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 template cudaError_t launch_faces<double>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
                                           const double *, const float *, const float *, double *, double *, int *,
-                                          int, cudaStream_t);
+                                          int, const FinishArgs &, cudaStream_t);
 template cudaError_t launch_faces<float>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
                                          const double *, const float *, const float *, float *, double *, int *, int,
-                                         cudaStream_t);
+                                         const FinishArgs &, cudaStream_t);
 
 cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
@@ -541,9 +620,8 @@ cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo,
   return cudaGetLastError();
 }
 
-cudaError_t launch_finish(int nblk, const double *blockpart, double *E, double *parts, double *galpha,
-                          double *energies, uint64_t *cnt, double threshold, int *status, cudaStream_t s) {
-  dev::finish_kernel<<<1, 256, 0, s>>>(nblk, blockpart, E, parts, galpha, energies, cnt, threshold, status);
+cudaError_t launch_finish(const FinishArgs &F, const double *blockpart, cudaStream_t s) {
+  dev::finish_kernel<<<1, 256, 0, s>>>(F, blockpart);
   return cudaGetLastError();
 }
 
