@@ -127,6 +127,22 @@ umcp_status umcp_grad(umcp_mesh *mesh, const double *r, double *g);
 umcp_status umcp_energy_grad(umcp_mesh *mesh, const double *r, double *E, double *g);
 /* Device-pointer form: d_r, d_g hold 3*nv+3 doubles; d_E one double; g accumulated. */
 umcp_status umcp_energy_grad_device(umcp_mesh *mesh, const double *d_r, double *d_E, double *d_g);
+/* Energy and gradient with NO device allocation at call time. This entry
+ * point has no counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc when they need the energy (inside another
+ * framework's CUDA-graph capture, or under a device-memory budget owned by
+ * another runtime). Same inputs and outputs as umcp_energy_grad_device (the
+ * mesh's plan tables, made at set-up, plus the caller's d_r, d_E, d_g; g is
+ * accumulated); every scratch buffer lives in one 32 MiB file-scope device
+ * array that each GPU loading the library holds until exit. Meshes whose
+ * scratch exceeds 32 MiB (about 110,000 faces in FP64, 200,000 in the FP32
+ * form) are rejected with UMCP_ERR_NOMEM. The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture. All calls on one device share that
+ * device's array and it keeps the last call's contents: calls whose work
+ * overlaps on the GPU (e.g. from two streams) race. Queued on the mesh's ctx
+ * stream; returns without waiting. */
+umcp_status umcp_energy_grad_static(umcp_mesh *mesh, const double *d_r, double *d_E, double *d_g);
 /* Queues only the per-face pass (quadrature, pointwise energy and adjoint,
  * per-face gradient partials) on the mesh's resident state, without the
  * per-vertex gather or the sums: the unit a roofline measurement times. */

@@ -103,6 +103,7 @@ _SIGNATURES = {
     "umcp_grad": [_VP, _D, _D],
     "umcp_energy_grad": [_VP, _D, _D, _D],
     "umcp_energy_grad_device": [_VP, _VP, _VP, _VP],
+    "umcp_energy_grad_static": [_VP, _VP, _VP, _VP],
     "umcp_mass_set": [_VP, C.c_int, _I, _I, _D],
     "umcp_mass_apply": [_VP, _D, _D, _D, C.c_double, _D],
     "umcp_mass_apply_device": [_VP, _VP, _VP, _VP, C.c_double, _D],
@@ -322,6 +323,15 @@ class Mesh:
         E = C.c_double()
         _check(library().umcp_energy_grad(self._h, _dp(r), C.byref(E), _dp(g)))
         return E.value, g
+
+    def energy_grad_device(self, d_r: int, d_E: int, d_g: int) -> None:
+        """Device-pointer energy+gradient (g accumulated), queued on the ctx stream."""
+        _check(library().umcp_energy_grad_device(self._h, C.c_void_p(d_r), C.c_void_p(d_E), C.c_void_p(d_g)))
+
+    def energy_grad_static(self, d_r: int, d_E: int, d_g: int) -> None:
+        """As energy_grad_device, with all scratch in the library's static device
+        array instead of the mesh's own buffers (no allocation at call time)."""
+        _check(library().umcp_energy_grad_static(self._h, C.c_void_p(d_r), C.c_void_p(d_E), C.c_void_p(d_g)))
 
     def mass_set(self, row_ptr: np.ndarray, col: np.ndarray, val: np.ndarray) -> None:
         row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int32)

@@ -897,3 +897,88 @@ extern "C" umcp_status umcp_step_host(umcp_mesh *m, const umcp_integrator *it, u
   if (E) *E = e;
   return st;
 }
+
+// ------------------------------------------------------------------ energy+gradient without allocation
+//
+// For callers that must not allocate device memory at call time: code that
+// runs inside someone else's stream capture (where cudaMalloc is not allowed),
+// or that lives under a fixed device-memory budget owned by another runtime.
+// The mesh's plan tables (made earlier, at set-up) are the inputs, the
+// caller's d_r/d_E/d_g the state and outputs; all scratch of the face pass
+// (gradient partials, block sums, the finished-block counter, the status
+// word and the FP32 position pairs) lives in this file-scope array, which
+// every GPU that loads the library holds until the process exits.
+
+static constexpr size_t kStaticScratchBytes = (size_t)32 << 20;  // 32 MiB per device
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+static void *g_static_scratch_addr[128];  // device address of the array, per device (host-side)
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, double *d_E, double *d_g) {
+  if (!m || !d_r || !d_E) return fail(UMCP_ERR_INVALID, "null argument");
+  const int dev = m->ctx->device;
+  if (dev < 0 || dev >= 128) return fail(UMCP_ERR_INVALID, "device index out of range for the static scratch table");
+  UMCP_CUDA(cudaSetDevice(dev));
+  // Host code cannot use the array's name as a device address; look the
+  // address up once per device, with that device current.
+  if (!g_static_scratch_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(UMCP_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
+    g_static_scratch_addr[dev] = p;
+  }
+  unsigned char *base = (unsigned char *)g_static_scratch_addr[dev];
+  const bool fp32 = (m->precision == UMCP_FP32_CENTRED);
+  const size_t esize = fp32 ? sizeof(float) : sizeof(double);
+  // layout: [status, done] | block partials | gradient partials | FP32 position pairs
+  const size_t off_flags = 0, off_block = 256;
+  const size_t off_partial = off_block + align256((size_t)m->nblocks * 6 * sizeof(double));
+  const size_t off_hi = off_partial + align256((size_t)m->nslots * 3 * esize);
+  const size_t off_lo = off_hi + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
+  const size_t need = off_lo + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
+  if (need > kStaticScratchBytes)
+    return fail(UMCP_ERR_NOMEM, "mesh needs " + std::to_string(need) + " bytes of scratch; the static area holds " +
+                                    std::to_string(kStaticScratchBytes) + " bytes");
+  int *status = (int *)(base + off_flags);
+  unsigned *done = (unsigned *)(base + off_flags + sizeof(int));
+  double *blockpart = (double *)(base + off_block);
+  float *rhi = fp32 ? (float *)(base + off_hi) : nullptr, *rlo = fp32 ? (float *)(base + off_lo) : nullptr;
+  cudaStream_t s = m->ctx->stream;
+  // The array keeps the previous call's contents: the status word and the
+  // finished-block counter must start at zero.
+  UMCP_CUDA(cudaMemsetAsync(base + off_flags, 0, 256, s));
+  if (fp32) UMCP_CUDA(launch_split_positions(3 * m->nv, d_r, rhi, rlo, s));
+  FinishArgs fin{m->nblocks, d_E, nullptr, d_g ? d_g + 3 * m->nv : nullptr, nullptr, nullptr, 0.0, status, done};
+  FinishArgs none{};
+  for (size_t gi = 0; gi < m->groups.size(); ++gi) {
+    auto &G = m->groups[gi];
+    dev::FaceLaunch L;
+    L.nfaces = G->nfaces;
+    L.block_base = G->block_base;
+    L.cp = G->cp.as<uint32_t>();
+    L.g0 = G->g0.as<double>();
+    L.rr0 = G->rr0.as<double>();
+    L.comp = G->comp.as<double>();
+    L.g0f = G->g0f.as<float>();
+    L.rr0f = G->rr0f.as<float>();
+    L.compf = G->compf.as<float>();
+    L.basis = G->basis.as<double>();
+    L.weight = G->weight.as<double>();
+    L.dudv = G->dudv;
+    L.irregular = G->irregular;
+    const FinishArgs &f = (gi + 1 == m->groups.size()) ? fin : none;
+    cudaError_t e = fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
+                                               (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
+                         : launch_faces<double>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
+                                                (double *)(base + off_partial), blockpart, status, G->nblocks, f, s);
+    if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("face pass: ") + cudaGetErrorString(e));
+  }
+  if (d_g) {
+    cudaError_t e = fp32 ? launch_gather<float>(m->nv, (float *)(base + off_partial), m->off.as<int>(), d_g, s)
+                         : launch_gather<double>(m->nv, (double *)(base + off_partial), m->off.as<int>(), d_g, s);
+    if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("gather: ") + cudaGetErrorString(e));
+  }
+  return UMCP_OK;
+}
