@@ -49,6 +49,11 @@ WORKLOAD = {
 METRIC = "BD vertex-steps/s"
 L2_BYTES = 129 * 1024 * 1024
 KT298 = 0.592186663194
+# DRAM bytes per face of one face pass, from the ncu capture of the 512x512
+# membrane (dram__bytes_read.sum + dram__bytes_write.sum = 166.76 MB over
+# 524,288 faces); the benchmark's pass is scaled from it by its face count.
+FACE_PASS_DRAM_BYTES_PER_FACE = 166.757e6 / 524288
+SM_COUNT, FP32_LANES_PER_SM = 152, 128
 
 
 def parse_args():
@@ -293,6 +298,7 @@ def engine_arm(args) -> None:
     e2e_val = info.nv * n_e2e * world / e2e_s
 
     clocks = clk.summary()
+    fp32_peak = SM_COUNT * FP32_LANES_PER_SM * 2 * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 1e12
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_port_sample(mesh_path, U.params(kc=prm.kc, KA=prm.KA, precision=U.FP64), args.cpu_seconds)
@@ -308,10 +314,15 @@ def engine_arm(args) -> None:
             "e2e": {"value": e2e_val, "unit": "vertex-steps/s", "h2d_bytes_per_step": 8 * (3 * info.nv + 3),
                     "d2h_bytes_per_step": 8 * (3 * info.nv + 3) + 8},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": FACE_PASS_DRAM_BYTES_PER_FACE * info.n_faces,
                          "kernel": "face_kernel (per-face pass)", "launch_ms": face_ms,
                          "algorithmic_bytes_per_launch": byts, "peak_source": peaks["source"],
-                         "fp32_tflops": flops / (face_ms / 1e3) / 1e12},
+                         "compute": {"fp32_tflops": flops / (face_ms / 1e3) / 1e12,
+                                     "fp32_simt_peak_tflops": fp32_peak,
+                                     "frac": flops / (face_ms / 1e3) / 1e12 / fp32_peak,
+                                     "peak_note": "nominal FP32 SIMT rate at the sampled SM clock: "
+                                                  "152 SMs x 128 lanes x 2 flop x clock"}},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": info.kernels_per_step * K,
