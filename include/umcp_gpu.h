@@ -107,6 +107,8 @@ void umcp_plan_destroy(umcp_plan *plan);
 
 /* ---- device context and meshes --------------------------------------- */
 umcp_status umcp_ctx_create(int device, umcp_ctx **out);
+/* Drops the caller's reference: the context (and its stream) lives on until
+ * the last mesh or batch created on it is destroyed. */
 void umcp_ctx_destroy(umcp_ctx *ctx);
 umcp_status umcp_ctx_synchronize(umcp_ctx *ctx);
 /* The cudaStream_t (as void*) every call on this ctx is queued on, so a
@@ -202,6 +204,54 @@ umcp_status umcp_run_async(umcp_mesh *mesh, const umcp_integrator *it, uint64_t 
  * This is the drop-in for one pass of the reference's dynamics loop body
  * (src/hd.C:1102-1720): energy, gradient, update. */
 umcp_status umcp_step_host(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step, double *r, double *p, double *E);
+/* Energies recorded by the mesh's latest run (umcp_run, umcp_run_async or a
+ * batch job): the first n of them. Synchronizes the context stream. */
+umcp_status umcp_mesh_energies(umcp_mesh *mesh, double *energies, int64_t n);
+
+/* ---- Batches: many meshes of one context advanced together.
+ * No counterpart in the reference, which runs one surface per process
+ * (src/hd.C:1102-1720 is the loop each job replaces). A job is a mesh with an
+ * integrator, a first step index and a step count; it behaves as
+ * umcp_run(mesh, it, step0, n_steps) would, on the mesh's resident state,
+ * and its trajectory does not depend on the other jobs. Each step launches
+ * one face kernel per patch type over all jobs, one per-job energy sum and
+ * one fused gather + update. */
+typedef struct umcp_batch umcp_batch;
+typedef struct {
+  int tile_faces;     /* faces per tile (one block's unit of work); 0: chosen by timing at the first run */
+  int blocks_per_sm;  /* cap on the persistent face grid; 0: the occupancy limit */
+} umcp_batch_opts;
+typedef struct {
+  int n_jobs;
+  long long n_vertices, n_faces;   /* summed over the jobs */
+  int n_tiles[3];                  /* face tiles: regular, irregular valence 5, valence 7 */
+  int face_grid[3];                /* blocks of each face launch */
+  int n_vertex_tiles;
+  int tile_faces;
+  int kernels_per_step;
+  double tuned_face_ms;            /* the tile timing's best face-pass time (ms), 0 when not tuned */
+} umcp_batch_info;
+/* precision: umcp_precision of every job's mesh. opts may be NULL. */
+umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umcp_batch_opts *opts, umcp_batch **out);
+/* Waits for the batch's work; its meshes stay valid and leave the batch. */
+void umcp_batch_destroy(umcp_batch *batch);
+/* Adds a job. The mesh must belong to the batch's context, have the batch's
+ * precision and be in no other batch; it->use_mass must be 0. The job's run
+ * starts (counters, status) at the next umcp_batch_run. Destroying the mesh
+ * removes the job. */
+umcp_status umcp_batch_add(umcp_batch *batch, umcp_mesh *mesh, const umcp_integrator *it, uint64_t step0,
+                           int64_t n_steps);
+/* Removes the job of mesh (waits for the batch's queued work first). */
+umcp_status umcp_batch_remove(umcp_batch *batch, umcp_mesh *mesh);
+/* Queues n_steps steps on the context stream. A job that has done its step
+ * count, or stopped on a non-finite or diverging energy, takes no more steps. */
+umcp_status umcp_batch_run(umcp_batch *batch, int n_steps);
+/* Steps done and status (umcp_status: OK, NONFINITE or DIVERGED) of every
+ * job, in the order they were added (removed jobs leave no gap). Waits for
+ * the batch's queued work. Either array may be NULL. */
+umcp_status umcp_batch_poll(umcp_batch *batch, int64_t *steps_done, int *job_status);
+umcp_status umcp_batch_job(umcp_batch *batch, const umcp_mesh *mesh, int64_t *steps_done, int *job_status);
+umcp_status umcp_batch_info_get(const umcp_batch *batch, umcp_batch_info *info);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,150 @@
+"""Batches: every job of a batch follows the trajectory its mesh takes when
+run alone (umcp_run with the same integrator, first step and step count).
+
+Positions and momenta are compared bit for bit: the per-face and per-vertex
+arithmetic of the batch is the single-mesh path's, and the gradient partials
+are summed per vertex in the same slot order. Energies are sums over tiles
+instead of over the single-mesh grid's blocks, so they agree to rounding:
+1e-12 relative in FP64, 1e-6 in the FP32 precision form.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import umcp_gb300 as U
+from conftest import load_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["ico2_plain", "ico3_deformed", "planar12_deformed", "ico2_lipids"]
+E_TOL = {U.FP64: 1e-12, U.FP32_CENTRED: 1e-6}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return U.Context(0)
+
+
+def _integrators():
+    return [
+        U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.00125, seed=7, stream=1),
+        U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.002, seed=7, stream=2),
+        U.integrator(U.LANGEVIN, time_step=1e-15, gamma=10.0, seed=9, stream=3),
+        U.integrator(U.BD_MEMBRANE, time_step=1e-15, gamma=10.0, seed=9, stream=4),
+    ]
+
+
+def _mesh(ctx, name, precision):
+    plan, prm, _ = load_case(name, precision)
+    return U.Mesh(ctx, plan, prm)
+
+
+def _alone(ctx, name, precision, it, step0, n):
+    m = _mesh(ctx, name, precision)
+    e = m.run(it, step0, n)
+    r, p = m.state_get()
+    return r, p, e
+
+
+def _check_job(mesh, ref, n, precision):
+    r, p = mesh.state_get()
+    assert np.array_equal(r, ref[0])
+    assert np.array_equal(p, ref[1])
+    e = mesh.energies(n)
+    assert np.max(np.abs(e - ref[2][:n]) / np.abs(ref[2][:n])) <= E_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [U.FP64, U.FP32_CENTRED])
+def test_batch_jobs_equal_their_alone_runs(ctx, precision):
+    its = _integrators()
+    batch = U.Batch(ctx, precision)
+    meshes = []
+    for k, name in enumerate(CASES):
+        m = _mesh(ctx, name, precision)
+        batch.add(m, its[k], 100 * k, 70)
+        meshes.append(m)
+    batch.run(70)  # two captured 32-step chunks and 6 single steps
+    done, st = batch.poll()
+    assert list(done) == [70] * len(CASES) and list(st) == [0] * len(CASES)
+    info = batch.info()
+    assert info.n_jobs == len(CASES) and info.tile_faces > 0 and info.tuned_face_ms > 0
+    assert info.kernels_per_step == 4  # regular and valence-5 faces, reduce, gather + update
+    for k, name in enumerate(CASES):
+        _check_job(meshes[k], _alone(ctx, name, precision, its[k], 100 * k, 70), 70, precision)
+
+
+def test_each_job_stops_at_its_own_step_count(ctx):
+    its = _integrators()
+    counts = [5, 37, 64, 0]
+    batch = U.Batch(ctx, U.FP64)
+    meshes = []
+    for k, name in enumerate(CASES):
+        m = _mesh(ctx, name, U.FP64)
+        batch.add(m, its[k], 0, counts[k])
+        meshes.append(m)
+    batch.run(40)
+    batch.run(40)
+    done, _ = batch.poll()
+    assert list(done) == counts
+    for k, name in enumerate(CASES):
+        if counts[k]:
+            _check_job(meshes[k], _alone(ctx, name, U.FP64, its[k], 0, counts[k]), counts[k], U.FP64)
+
+
+def test_tile_size_does_not_change_trajectories(ctx):
+    it = _integrators()[0]
+    finals = []
+    for tf in (4, 36, 512):
+        batch = U.Batch(ctx, U.FP32_CENTRED, tile_faces=tf)
+        m = _mesh(ctx, "ico3_deformed", U.FP32_CENTRED)
+        batch.add(m, it, 0, 33)
+        batch.run(33)
+        assert batch.info().tile_faces == tf
+        finals.append(m.state_get()[0])
+    assert np.array_equal(finals[0], finals[1]) and np.array_equal(finals[0], finals[2])
+
+
+def test_jobs_join_and_leave_between_runs(ctx):
+    its = _integrators()
+    batch = U.Batch(ctx, U.FP64, tile_faces=32)
+    a = _mesh(ctx, "ico2_plain", U.FP64)
+    b = _mesh(ctx, "ico3_deformed", U.FP64)
+    batch.add(a, its[0], 0, 60)
+    batch.add(b, its[1], 0, 60)
+    batch.run(20)
+    c = _mesh(ctx, "planar12_deformed", U.FP64)
+    batch.add(c, its[2], 5, 30)  # starts at the next run
+    batch.remove(b)
+    batch.run(40)
+    assert batch.job(a) == (60, 0) and batch.job(c) == (30, 0)
+    assert list(batch.poll()[0]) == [60, 30]
+    _check_job(a, _alone(ctx, "ico2_plain", U.FP64, its[0], 0, 60), 60, U.FP64)
+    _check_job(c, _alone(ctx, "planar12_deformed", U.FP64, its[2], 5, 30), 30, U.FP64)
+    rb, _, _ = _alone(ctx, "ico3_deformed", U.FP64, its[1], 0, 20)
+    assert np.array_equal(b.state_get()[0], rb)  # b kept the state of its 20 batched steps
+    del c  # destroying a job's mesh removes the job
+    batch.run(3)
+    assert batch.info().n_jobs == 1
+
+
+def test_a_diverging_job_stops_alone(ctx):
+    its = _integrators()
+    wild = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=5.0, seed=2, divergence_threshold=10.0)
+    batch = U.Batch(ctx, U.FP64)
+    calm = _mesh(ctx, "ico3_deformed", U.FP64)
+    bad = _mesh(ctx, "ico2_plain", U.FP64)
+    batch.add(calm, its[0], 0, 40)
+    batch.add(bad, wild, 0, 40)
+    batch.run(40)
+    done, st = batch.poll()
+    assert done[0] == 40 and st[0] == 0
+    assert st[1] == U.ERR_DIVERGED and 0 < done[1] < 40
+    _check_job(calm, _alone(ctx, "ico3_deformed", U.FP64, its[0], 0, 40), 40, U.FP64)
+    alone = _mesh(ctx, "ico2_plain", U.FP64)
+    with pytest.raises(U.UmcpError, match="diverged"):
+        alone.run(wild, 0, 40)
+    # the flagged step records its energy and moves nothing, alone or batched
+    assert np.array_equal(bad.state_get()[0], alone.state_get()[0])
+    k = int(done[1])
+    assert np.max(np.abs(bad.energies(k) - alone.energies(k)) / np.abs(alone.energies(k))) <= E_TOL[U.FP64]

@@ -27,6 +27,9 @@ OVERDAMPED_BD = 0
 BD_MEMBRANE = 1
 LANGEVIN = 2
 
+ERR_NONFINITE = 4
+ERR_DIVERGED = 8
+
 KCAL_MOL_PER_KT_298 = 0.592186663194  # kT at 298 K in kcal/mol (src/hd.C:142)
 
 _STATUS = {
@@ -70,8 +73,21 @@ class Integrator(C.Structure):
     ]
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("tile_faces", C.c_int), ("blocks_per_sm", C.c_int)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("n_jobs", C.c_int), ("n_vertices", C.c_longlong), ("n_faces", C.c_longlong),
+        ("n_tiles", C.c_int * 3), ("face_grid", C.c_int * 3), ("n_vertex_tiles", C.c_int),
+        ("tile_faces", C.c_int), ("kernels_per_step", C.c_int), ("tuned_face_ms", C.c_double),
+    ]
+
+
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
+_I64 = C.POINTER(C.c_int64)
 _I8 = C.POINTER(C.c_int8)
 _VP = C.c_void_p
 
@@ -112,10 +128,19 @@ _SIGNATURES = {
     "umcp_run": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int, _D],
     "umcp_run_async": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int],
     "umcp_step_host": [_VP, C.POINTER(Integrator), C.c_uint64, _D, _D, _D],
+    "umcp_mesh_energies": [_VP, _D, C.c_int64],
+    "umcp_batch_create": [_VP, C.c_int, C.POINTER(BatchOpts), C.POINTER(_VP)],
+    "umcp_batch_destroy": [_VP],
+    "umcp_batch_add": [_VP, _VP, C.POINTER(Integrator), C.c_uint64, C.c_int64],
+    "umcp_batch_remove": [_VP, _VP],
+    "umcp_batch_run": [_VP, C.c_int],
+    "umcp_batch_poll": [_VP, _I64, _I],
+    "umcp_batch_job": [_VP, _VP, _I64, _I],
+    "umcp_batch_info_get": [_VP, C.POINTER(BatchInfo)],
     "umcp_last_error": [],
     "umcp_status_string": [C.c_int],
 }
-_VOID = {"umcp_plan_destroy", "umcp_ctx_destroy", "umcp_mesh_destroy"}
+_VOID = {"umcp_plan_destroy", "umcp_ctx_destroy", "umcp_mesh_destroy", "umcp_batch_destroy"}
 _STR = {"umcp_last_error", "umcp_status_string"}
 
 _lib = None
@@ -368,6 +393,59 @@ class Mesh:
         E = C.c_double()
         _check(library().umcp_step_host(self._h, C.byref(it), step, _dp(r), _dp(p), C.byref(E)))
         return E.value
+
+    def energies(self, n: int) -> np.ndarray:
+        """The first n energies recorded by the latest run or batch job."""
+        e = np.zeros(max(n, 1))
+        _check(library().umcp_mesh_energies(self._h, _dp(e), n))
+        return e[:n]
+
+
+class Batch:
+    """Many meshes of one context advanced together (umcp_batch_*). Each job
+    behaves as Mesh.run(it, step0, n_steps) on its own mesh."""
+
+    def __init__(self, ctx: Context, precision: int = FP64, tile_faces: int = 0, blocks_per_sm: int = 0):
+        self.ctx = ctx  # keep the context alive; a job's mesh leaves the batch when it is destroyed
+        self._h = C.c_void_p()
+        opts = BatchOpts(tile_faces, blocks_per_sm)
+        _check(library().umcp_batch_create(ctx.handle, precision, C.byref(opts), C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.umcp_batch_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def add(self, mesh: Mesh, it: Integrator, step0: int, n_steps: int) -> None:
+        _check(library().umcp_batch_add(self._h, mesh.handle, C.byref(it), step0, n_steps))
+
+    def remove(self, mesh: Mesh) -> None:
+        _check(library().umcp_batch_remove(self._h, mesh.handle))
+
+    def run(self, n_steps: int) -> None:
+        _check(library().umcp_batch_run(self._h, n_steps))
+
+    def poll(self) -> tuple[np.ndarray, np.ndarray]:
+        """(steps done, status) of every job, in add order."""
+        n = self.info().n_jobs
+        done = np.zeros(max(n, 1), dtype=np.int64)
+        st = np.zeros(max(n, 1), dtype=np.int32)
+        _check(library().umcp_batch_poll(self._h, done.ctypes.data_as(_I64), st.ctypes.data_as(_I)))
+        return done[:n], st[:n]
+
+    def job(self, mesh: Mesh) -> tuple[int, int]:
+        done, st = C.c_int64(), C.c_int()
+        _check(library().umcp_batch_job(self._h, mesh.handle, C.byref(done), C.byref(st)))
+        return done.value, st.value
+
+    def info(self) -> BatchInfo:
+        i = BatchInfo()
+        _check(library().umcp_batch_info_get(self._h, C.byref(i)))
+        return i
 
 
 def integrator(kind=OVERDAMPED_BD, time_step=1.0, gamma=0.0, D=0.0, seed=1, stream=0, divergence_threshold=0.0,

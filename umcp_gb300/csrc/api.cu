@@ -16,6 +16,7 @@
 #include "launch.h"
 #include "mesh.h"
 #include "plan.h"
+#include "engine.h"
 
 using namespace umcp;
 
@@ -25,17 +26,12 @@ static constexpr double kAkmaTime = 1.0 / (0.04888 * 1e-12);  // AKMA_TIME, src/
 
 static thread_local std::string g_last_error;
 
-static umcp_status fail(umcp_status s, const std::string &msg) {
+umcp_status umcp::set_error(umcp_status s, const std::string &msg) {
   g_last_error = msg;
   return s;
 }
 
-#define UMCP_CUDA(call)                                                                          \
-  do {                                                                                           \
-    cudaError_t e_ = (call);                                                                     \
-    if (e_ != cudaSuccess)                                                                       \
-      return fail(UMCP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
-  } while (0)
+static umcp_status fail(umcp_status s, const std::string &msg) { return umcp::set_error(s, msg); }
 
 extern "C" const char *umcp_last_error(void) { return g_last_error.c_str(); }
 
@@ -228,10 +224,6 @@ extern "C" void umcp_plan_destroy(umcp_plan *plan) { delete plan; }
 
 // ------------------------------------------------------------------ device context
 
-struct umcp_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-};
 
 extern "C" umcp_status umcp_ctx_create(int device, umcp_ctx **out) {
   if (!out) return fail(UMCP_ERR_INVALID, "null out");
@@ -248,10 +240,7 @@ extern "C" umcp_status umcp_ctx_create(int device, umcp_ctx **out) {
 }
 
 extern "C" void umcp_ctx_destroy(umcp_ctx *ctx) {
-  if (!ctx) return;
-  cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  if (ctx) ctx_release(ctx);  // the stream goes when the last mesh or batch on it does
 }
 
 extern "C" umcp_status umcp_ctx_stream(umcp_ctx *ctx, void **stream) {
@@ -268,86 +257,6 @@ extern "C" umcp_status umcp_ctx_synchronize(umcp_ctx *ctx) {
 
 // ------------------------------------------------------------------ device mesh
 
-namespace {
-struct DevBuf {
-  void *p = nullptr;
-  size_t bytes = 0;
-  ~DevBuf() { if (p) cudaFree(p); }
-  cudaError_t alloc(size_t b) {
-    if (p) { cudaFree(p); p = nullptr; }
-    bytes = b;
-    return b ? cudaMalloc(&p, b) : cudaSuccess;
-  }
-  template <class T> T *as() const { return (T *)p; }
-};
-
-struct Group {
-  int ncp = 0, npt = 0, nfaces = 0, slot_base = 0, irregular = 0;
-  int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
-  double dudv = 0.5;
-  DevBuf cp, g0, rr0, comp, basis, weight, dest;
-  DevBuf g0f, rr0f, compf;  // FP32 copies for the precision form
-};
-}  // namespace
-
-struct umcp_mesh {
-  umcp_ctx *ctx = nullptr;
-  int nv = 0, nfaces = 0, nslots = 0;
-  int precision = UMCP_FP64;
-  dev::SurfaceParams P{};
-  std::vector<std::unique_ptr<Group>> groups;
-  DevBuf partial, off, blockpart;
-  int nblocks = 0;
-  DevBuf r, g, p, qdot, E, parts, status, cnt;  // cnt: {first step of the run, run index}
-  DevBuf rhi, rlo;  // FP32 hi/lo pairs of r (precision form)
-  DevBuf r_eval;    // staging for host-pointer energy/gradient calls (keeps the resident state)
-  DevBuf done;      // finished-block counter of the face pass
-  bool split_valid = false;  // rhi/rlo hold the resident state r
-  double kT = 0.592186663194;  // kcal/mol at the params' temperature (src/hd.C:142-143)
-  DevBuf energies;
-  size_t energies_cap = 0;
-  double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
-  double *h_stage2 = nullptr; // pinned, 3*nv doubles
-  uint64_t *h_cnt = nullptr;  // pinned, 2 counters
-  // effective inverse mass
-  int mrows = 0;
-  DevBuf mrow, mcol, mval, alphas;
-  // captured step sequences, by length (1 and kGraphChunk steps)
-  struct CachedGraph {
-    cudaGraphExec_t exec = nullptr;
-    int steps = 0;
-    StepArgs args{};
-    int use_mass = -1;
-    double threshold = 0;
-  };
-  std::vector<CachedGraph> graphs;
-  void drop_graphs() {
-    for (auto &g : graphs)
-      if (g.exec) cudaGraphExecDestroy(g.exec);
-    graphs.clear();
-  }
-
-  ~umcp_mesh() {
-    drop_graphs();
-    if (h_stage) cudaFreeHost(h_stage);
-    if (h_stage2) cudaFreeHost(h_stage2);
-    if (h_cnt) cudaFreeHost(h_cnt);
-  }
-};
-
-static uint32_t pack_cp(int v, const int8_t img[3]) {
-  int code = (img[0] + 1) + 3 * (img[1] + 1) + 9 * (img[2] + 1);
-  return (uint32_t)v | ((uint32_t)code << dev::kVertexBits);
-}
-
-template <class T>
-static cudaError_t upload(DevBuf &b, const std::vector<T> &h) {
-  cudaError_t e = b.alloc(h.size() * sizeof(T));
-  if (e != cudaSuccess || h.empty()) return e;
-  return cudaMemcpy(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
-}
-
-static constexpr int kGraphChunk = 32;  // steps captured per CUDA graph
 
 static void fill_params(umcp_mesh *m, const umcp_params *p) {
   m->kT = (5.92186663194E-01 / 298.0) * p->temperature;
@@ -497,6 +406,7 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     m->split_valid = true;
   }
   *out = m.release();
+  ctx_retain(ctx);
   return UMCP_OK;
 }
 
@@ -504,13 +414,17 @@ extern "C" void umcp_mesh_destroy(umcp_mesh *mesh) {
   if (!mesh) return;
   cudaSetDevice(mesh->ctx->device);
   cudaStreamSynchronize(mesh->ctx->stream);
+  if (mesh->batch) batch_forget_mesh(mesh->batch, mesh);
+  umcp_ctx *ctx = mesh->ctx;
   delete mesh;
+  ctx_release(ctx);
 }
 
 extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *p) {
   if (!mesh || !p) return fail(UMCP_ERR_INVALID, "null argument");
   fill_params(mesh, p);
   mesh->drop_graphs();
+  if (mesh->batch) batch_mesh_changed(mesh->batch);  // its job entry holds the parameters
   return UMCP_OK;
 }
 
@@ -739,7 +653,18 @@ extern "C" umcp_status umcp_state_get(umcp_mesh *m, double *r, double *p) {
   return UMCP_OK;
 }
 
-static umcp_status make_step_args(umcp_mesh *m, const umcp_integrator *it, StepArgs *a) {
+extern "C" umcp_status umcp_mesh_energies(umcp_mesh *m, double *energies, int64_t n) {
+  if (!m || (n > 0 && !energies) || n < 0) return fail(UMCP_ERR_INVALID, "bad argument");
+  if ((size_t)n > m->energies_cap) return fail(UMCP_ERR_INVALID, "more energies asked for than the run records");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  if (n > 0)
+    UMCP_CUDA(cudaMemcpyAsync(energies, m->energies.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                              m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return UMCP_OK;
+}
+
+umcp_status umcp::make_step_args(const umcp_mesh *m, const umcp_integrator *it, StepArgs *a) {
   if (it->kind < 0 || it->kind > 2) return fail(UMCP_ERR_INVALID, "unknown integrator kind");
   if (!(it->time_step > 0)) return fail(UMCP_ERR_INVALID, "time_step must be positive");
   if (it->use_mass && !m->mrows) return fail(UMCP_ERR_INVALID, "use_mass set but no mass matrix installed");
@@ -829,6 +754,7 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
     m->drop_graphs();  // graphs hold the energies pointer
     UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
     m->energies_cap = (size_t)n_steps;
+    if (m->batch) batch_mesh_changed(m->batch);  // so does its batch job entry
   }
   if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
     UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));

@@ -1,0 +1,139 @@
+// Internal definitions shared by the engine's translation units (not part
+// of the ABI): device buffers, the context and device mesh objects, and the
+// error helper every entry point reports through.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/umcp_gpu.h"
+#include "launch.h"
+
+namespace umcp {
+
+// Records the text umcp_last_error() returns on this host thread; returns s.
+umcp_status set_error(umcp_status s, const std::string &msg);
+
+constexpr int kGraphChunk = 32;  // steps captured per CUDA graph
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t alloc(size_t b) {
+    if (p) { cudaFree(p); p = nullptr; }
+    bytes = b;
+    return b ? cudaMalloc(&p, b) : cudaSuccess;
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+struct Group {
+  int ncp = 0, npt = 0, nfaces = 0, slot_base = 0, irregular = 0;
+  int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
+  double dudv = 0.5;
+  DevBuf cp, g0, rr0, comp, basis, weight, dest;
+  DevBuf g0f, rr0f, compf;  // FP32 copies for the precision form
+};
+}  // namespace umcp
+
+struct umcp_batch;
+
+// Reference-counted: meshes and batches hold the context, so it outlives
+// them whatever order they are destroyed in.
+struct umcp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int refs = 1;  // the creator's reference plus one per live mesh or batch
+};
+
+namespace umcp {
+inline umcp_ctx *ctx_retain(umcp_ctx *c) {
+  ++c->refs;
+  return c;
+}
+inline void ctx_release(umcp_ctx *c) {
+  if (--c->refs > 0) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+}  // namespace umcp
+
+struct umcp_mesh {
+  umcp_ctx *ctx = nullptr;
+  int nv = 0, nfaces = 0, nslots = 0;
+  int precision = UMCP_FP64;
+  umcp::dev::SurfaceParams P{};
+  std::vector<std::unique_ptr<umcp::Group>> groups;
+  umcp::DevBuf partial, off, blockpart;
+  int nblocks = 0;
+  umcp::DevBuf r, g, p, qdot, E, parts, status, cnt;  // cnt: {first step of the run, run index}
+  umcp::DevBuf rhi, rlo;  // FP32 hi/lo pairs of r (precision form)
+  umcp::DevBuf r_eval;    // staging for host-pointer energy/gradient calls (keeps the resident state)
+  umcp::DevBuf done;      // finished-block counter of the face pass
+  bool split_valid = false;  // rhi/rlo hold the resident state r
+  double kT = 0.592186663194;  // kcal/mol at the params' temperature (src/hd.C:142-143)
+  umcp::DevBuf energies;
+  size_t energies_cap = 0;
+  umcp_batch *batch = nullptr;  // the batch this mesh is a job of, if any
+  double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
+  double *h_stage2 = nullptr; // pinned, 3*nv doubles
+  uint64_t *h_cnt = nullptr;  // pinned, 2 counters
+  // effective inverse mass
+  int mrows = 0;
+  umcp::DevBuf mrow, mcol, mval, alphas;
+  // captured step sequences, by length (1 and kGraphChunk steps)
+  struct CachedGraph {
+    cudaGraphExec_t exec = nullptr;
+    int steps = 0;
+    umcp::StepArgs args{};
+    int use_mass = -1;
+    double threshold = 0;
+  };
+  std::vector<CachedGraph> graphs;
+  void drop_graphs() {
+    for (auto &g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
+
+  ~umcp_mesh() {
+    drop_graphs();
+    if (h_stage) cudaFreeHost(h_stage);
+    if (h_stage2) cudaFreeHost(h_stage2);
+    if (h_cnt) cudaFreeHost(h_cnt);
+  }
+};
+
+namespace umcp {
+
+// Integrator settings of a run on mesh m (validates it).
+umcp_status make_step_args(const umcp_mesh *m, const umcp_integrator *it, StepArgs *a);
+// A batch drops a job whose mesh is being destroyed (waits for its stream
+// first); a batch rebuilds its tables after a job's mesh changed.
+void batch_forget_mesh(umcp_batch *b, umcp_mesh *m);
+void batch_mesh_changed(umcp_batch *b);
+
+inline uint32_t pack_cp(int v, const int8_t img[3]) {
+  int code = (img[0] + 1) + 3 * (img[1] + 1) + 9 * (img[2] + 1);
+  return (uint32_t)v | ((uint32_t)code << dev::kVertexBits);
+}
+
+template <class T>
+inline cudaError_t upload(DevBuf &b, const std::vector<T> &h) {
+  cudaError_t e = b.alloc(h.size() * sizeof(T));
+  if (e != cudaSuccess || h.empty()) return e;
+  return cudaMemcpy(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+}  // namespace umcp
+
+#define UMCP_CUDA(call)                                                                          \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return umcp::set_error(UMCP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)

@@ -51,6 +51,26 @@ struct FaceLaunch {
   int irregular;
 };
 
+// FP64 uses half the threads per block so its shared memory stays below the
+// 48 KB static limit.
+template <typename T>
+struct FaceCfg {
+  static constexpr int threads = (sizeof(T) == 8) ? 64 : 128;
+  static constexpr int half_warps = threads / 16;
+  static constexpr int min_blocks = (sizeof(T) == 8) ? 6 : 4;  // caps registers near 128 (FP32) / 168 (FP64)
+};
+
+// Where one face group's data and its mesh's state live.
+struct FaceSrc {
+  const uint32_t *cp;
+  const double *g0, *rr0, *comp;
+  const float *g0f, *rr0f, *compf;
+  const int *dest;
+  const double *r;
+  const float *rhi, *rlo;
+  int nfaces;
+};
+
 template <typename T>
 struct Vec3 {
   T x, y, z;

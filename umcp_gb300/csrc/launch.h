@@ -75,6 +75,60 @@ cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *cnt, double *
 cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, float *rhi, float *rlo,
                          const int *status, cudaStream_t s);
 
+// One mesh of a batch (device pointers into the mesh's own buffers). The
+// face kernel stages the leading part, BatchFaceJob, in shared memory.
+struct BatchFaceJob {
+  dev::FaceSrc src[3];     // patch types: regular, irregular valence 5, irregular valence 7
+  dev::SurfaceParams P;
+  void *partial;           // the mesh's gradient-partial slots
+  uint64_t *cnt;           // {first step of the run, steps done}
+  uint64_t limit;          // steps in the run
+  int *status;
+  int pad;
+};
+struct BatchJob {
+  BatchFaceJob f;
+  const int *off;          // vertex slot offsets
+  double *r, *p;           // state
+  float *rhi, *rlo;        // FP32 hi/lo pairs of r (precision form), else NULL
+  double *E, *parts;       // energy (and parts) of the latest step
+  double *energies;        // the run's recorded energies, indexed by steps done
+  double threshold;        // energy rise that flags divergence (<= 0: off)
+  StepArgs a;              // the job's integrator
+};
+// Faces [first, first+count) of one patch type of one job, or vertices
+// [first, first+count) of one job.
+struct BatchTile {
+  int job, first, count;
+};
+// Layout of the batch's device count array.
+enum : int { kCountTiles = 0, kCountTileBase = 3, kCountJobs = 6, kCountVertexTiles = 7, kCountWords = 8 };
+constexpr int kVertexTile = 256;  // vertices per vertex tile (one thread each)
+
+// Face launch of patch type `group` over its tiles (counts[group] of them,
+// from counts[3 + group] in tiles); tile_sums[3 * global tile] receives each
+// tile's energy terms. Persistent grid; tiles of stopped or finished jobs are
+// skipped.
+template <typename T>
+cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile *tiles, const int *counts,
+                               const double *basis, const double *weight, int ncp, int npt, double dudv,
+                               int irregular, double *tile_sums, int grid, cudaStream_t s);
+// Per job: tile sums in listed order (tile_idx[tile_off[j] .. tile_off[j+1])),
+// energy record, flags, steps done; live[j] and prog[j] = {done, status}.
+cudaError_t launch_batch_reduce(const BatchJob *jobs, const int *counts, int max_jobs, const int *tile_off,
+                                const int *tile_idx, const double *tile_sums, int *live, unsigned long long *prog,
+                                cudaStream_t s);
+// Gather fused with the update, for live jobs (kinds 0, and 1/2 with identity mass).
+template <typename T>
+cudaError_t launch_batch_gather_step(const BatchJob *jobs, const BatchTile *vtiles, const int *counts,
+                                     const int *live, int grid, cudaStream_t s);
+// Run start of the jobs with start[j] != 0: counters {step0[j], 0}, status 0, hi/lo split.
+cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const int *start,
+                               const unsigned long long *step0, int grid, cudaStream_t s);
+// Device-filling grid of a batch face launch for a patch type.
+template <typename T>
+int batch_face_blocks(int ncp, int npt);
+
 // out[3i+c] (+)= scale/alpha_c^2 * (scalev ? scalev[c*nrow+i] : 1) * sum_k val[k] in[3 col[k]+c].
 // accumulate=0 overwrites out. alphas: device pointer to 3 doubles (or NULL = 1).
 cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const double *val, const double *scalev,

@@ -16,15 +16,6 @@ struct alignas(4 * sizeof(T)) Q4 {
   T x, y, z, w;
 };
 
-// FP64 uses half the threads per block so its shared memory stays below the
-// 48 KB static limit.
-template <typename T>
-struct FaceCfg {
-  static constexpr int threads = (sizeof(T) == 8) ? 64 : 128;
-  static constexpr int half_warps = threads / 16;
-  static constexpr int min_blocks = (sizeof(T) == 8) ? 6 : 4;  // caps registers near 128 (FP32) / 168 (FP64)
-};
-
 template <typename T, int NCP, int NPT>
 struct FaceSmem {
   static constexpr int NC4 = (NCP + 3) / 4;  // control points in chunks of four
@@ -106,7 +97,61 @@ __device__ __forceinline__ T point_data(const double *d64, const float *d32, siz
   else return d32[i];
 }
 
-// One half-warp (16 lanes) per face, persistent over faces.
+// Global data of one face, loaded one face ahead (control-point indices two
+// ahead) so the loads are in flight while the previous face computes.
+template <typename T>
+struct FaceAhead {
+  int img[3] = {0, 0, 0};
+  float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};  // precision form
+  double X[3] = {0, 0, 0};                     // plain path (image position)
+  T g0 = 1, rr0 = 0, P2 = 0, Hbar = 0, Pres = 0;
+  int dest = 0;
+};
+
+// Faces at or past end are not loaded.
+template <int NCP>
+__device__ __forceinline__ uint32_t load_cp(const FaceSrc &S, int f, int end, int lane) {
+  return (f >= 0 && f < end && lane < NCP) ? __ldg(&S.cp[(size_t)f * NCP + lane]) : 0u;
+}
+
+template <typename T, int NCP, int NPT>
+__device__ __forceinline__ void load_ahead(const FaceSrc &S, const SurfaceParams &P, int f, int end, uint32_t packed,
+                                           int lane, FaceAhead<T> &a) {
+  if (f < 0 || f >= end) return;
+  if (lane < NCP) {
+    const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+    a.img[0] = code % 3 - 1; a.img[1] = (code / 3) % 3 - 1; a.img[2] = code / 9 - 1;
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        a.X[c] = S.r[3 * (size_t)v + c] + a.img[0] * P.box[0][c] + a.img[1] * P.box[1][c] + a.img[2] * P.box[2][c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { a.hi[c] = S.rhi[3 * (size_t)v + c]; a.lo[c] = S.rlo[3 * (size_t)v + c]; }
+    }
+    a.dest = __ldg(&S.dest[(size_t)f * NCP + lane]);
+  }
+  if (lane < NPT) {
+    const size_t pi = (size_t)f * NPT + lane;
+    a.g0 = point_data<T>(S.g0, S.g0f, pi);
+    a.rr0 = point_data<T>(S.rr0, S.rr0f, pi);
+  }
+  a.P2 = point_data<T>(S.comp, S.compf, 3 * (size_t)f);
+  a.Hbar = point_data<T>(S.comp, S.compf, 3 * (size_t)f + 1);
+  a.Pres = point_data<T>(S.comp, S.compf, 3 * (size_t)f + 2);
+}
+
+// Stage the block's copy of the patch type's basis rows and weights.
+template <typename T, int NCP, int NPT, int NT>
+__device__ __forceinline__ void stage_basis(FaceSmem<T, NCP, NPT> &sm, const double *basis, const double *weight) {
+  constexpr int NCPP = FaceSmem<T, NCP, NPT>::NCPP, HW = FaceSmem<T, NCP, NPT>::HW;
+  T *b = &sm.B[0][0][0].x;
+  for (int i = threadIdx.x; i < NPT * 5 * NCPP; i += NT) b[i] = (T)basis[i];
+  for (int i = threadIdx.x; i < NPT; i += NT) sm.W[i] = (T)weight[i];
+  for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
+}
+
+// Energy, adjoint and gradient partials of one face by one half-warp:
 //  1. lanes = control points: the control point's position relative to the
 //     patch corner (control point 0) in its lattice image, times alpha. The
 //     plain path forms it in FP64; the precision form from FP32 hi/lo pairs
@@ -117,6 +162,130 @@ __device__ __forceinline__ T point_data(const double *d64, const float *d32, siz
 //     adjoint's contribution to every control point (written transposed).
 //  3. lanes = control points: sum the contributions over the points; write the
 //     alpha-scaled gradient partial to its vertex-major slot.
+// Returns the face's energy terms and dE/dalpha summed over the half-warp.
+template <typename T, int NCP, int NPT>
+__device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, int lane, unsigned hmask,
+                                             const FaceAhead<T> &cur, const SurfaceParams &P, const T alpha[3],
+                                             const T ialpha[3], T dudv, bool reg_alpha, T *__restrict__ partial,
+                                             T e3[3], T da[3]) {
+  constexpr int NC4 = FaceSmem<T, NCP, NPT>::NC4;
+  const T kc = (T)P.kc, KA = (T)P.KA, kg = (T)P.kg, k_reg = (T)P.k_reg;
+  // ---- 1. control points, relative to the patch corner
+  T xl[3] = {0, 0, 0};
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double a = __shfl_sync(hmask, cur.X[c], 0, 16);
+      xl[c] = alpha[c] * (cur.X[c] - a);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float ahi = __shfl_sync(hmask, cur.hi[c], 0, 16), alo = __shfl_sync(hmask, cur.lo[c], 0, 16);
+      // lattice shift hi + lo (each term exact: images are -1, 0 or +1)
+      float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float t, e;
+        two_sum(sh, (float)cur.img[d] * P.box_hi[d][c], t, e);
+        sh = t;
+        she += e;
+        shl += (float)cur.img[d] * P.box_lo[d][c];
+      }
+      float s1, e1, s2, e2;
+      two_sum(cur.hi[c], sh, s1, e1);
+      two_sum(s1, -ahi, s2, e2);
+      xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl))));
+    }
+  }
+  if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
+  __syncwarp(hmask);
+
+  // ---- 2. lanes as quadrature points
+  T ea = 0, ec = 0, er = 0;
+  T dreg[3] = {0, 0, 0};
+  if (lane < NPT) {
+    Vec3<T> K[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) K[k] = {0, 0, 0};
+#pragma unroll 1
+    for (int c4 = 0; c4 < NC4; ++c4) {
+      const Q4<T> x0 = sm.X[hw][4 * c4], x1 = sm.X[hw][4 * c4 + 1], x2 = sm.X[hw][4 * c4 + 2],
+                  x3 = sm.X[hw][4 * c4 + 3];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Q4<T> b = sm.B[lane][k][c4];
+        K[k].x += b.x * x0.x + b.y * x1.x + b.z * x2.x + b.w * x3.x;
+        K[k].y += b.x * x0.y + b.y * x1.y + b.z * x2.y + b.w * x3.y;
+        K[k].z += b.x * x0.z + b.y * x1.z + b.z * x2.z + b.w * x3.z;
+      }
+    }
+    Vec3<T> Kb[5], Kreg[2];
+    point_adjoint<T>(K, sm.W[lane], cur.g0, cur.rr0, dudv, cur.P2, cur.Hbar, cur.Pres, kc, KA, kg, k_reg, &ea, &ec,
+                     &er, Kb, Kreg);
+#pragma unroll 1
+    for (int c4 = 0; c4 < NC4; ++c4) {
+      Q4<T> b[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) b[k] = sm.B[lane][k][c4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const T bk0 = (&b[0].x)[j], bk1 = (&b[1].x)[j], bk2 = (&b[2].x)[j], bk3 = (&b[3].x)[j],
+                bk4 = (&b[4].x)[j];
+        Q4<T> t;
+        t.x = bk0 * Kb[0].x + bk1 * Kb[1].x + bk2 * Kb[2].x + bk3 * Kb[3].x + bk4 * Kb[4].x;
+        t.y = bk0 * Kb[0].y + bk1 * Kb[1].y + bk2 * Kb[2].y + bk3 * Kb[3].y + bk4 * Kb[4].y;
+        t.z = bk0 * Kb[0].z + bk1 * Kb[1].z + bk2 * Kb[2].z + bk3 * Kb[3].z + bk4 * Kb[4].z;
+        t.w = T(0);
+        sm.Tc[hw][lane][4 * c4 + j] = t;
+        if (reg_alpha) {
+          // igrad's box-scale derivative takes the angle-term adjoint with
+          // one more alpha factor (src/grad.C:7414-7421).
+          const Q4<T> xx = sm.X[hw][4 * c4 + j];
+          dreg[0] += (bk0 * Kreg[0].x + bk1 * Kreg[1].x) * xx.x;
+          dreg[1] += (bk0 * Kreg[0].y + bk1 * Kreg[1].y) * xx.y;
+          dreg[2] += (bk0 * Kreg[0].z + bk1 * Kreg[1].z) * xx.z;
+        }
+      }
+    }
+  }
+  __syncwarp(hmask);
+
+  // ---- 3. lanes as control points
+  da[0] = da[1] = da[2] = 0;
+  if (lane < NCP) {
+    T G0 = 0, G1 = 0, G2 = 0;
+#pragma unroll
+    for (int p = 0; p < NPT; ++p) {
+      const Q4<T> t = sm.Tc[hw][p][lane];
+      G0 += t.x;
+      G1 += t.y;
+      G2 += t.z;
+    }
+    const int d = cur.dest;
+    partial[3 * (size_t)d] = alpha[0] * G0;
+    partial[3 * (size_t)d + 1] = alpha[1] * G1;
+    partial[3 * (size_t)d + 2] = alpha[2] * G2;
+    // dE/dalpha_c = sum_x G_xc (X - X_0)_xc: the patch gradient sums to
+    // zero, so coordinates relative to the corner give the same sum.
+    da[0] = G0 * xl[0] * ialpha[0];
+    da[1] = G1 * xl[1] * ialpha[1];
+    da[2] = G2 * xl[2] * ialpha[2];
+  }
+  if (reg_alpha)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) da[c] += (alpha[c] - T(1)) * ialpha[c] * dreg[c];
+  e3[0] = ea; e3[1] = ec; e3[2] = er;
+#pragma unroll
+  for (int off = 8; off >= 1; off >>= 1)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      e3[c] += __shfl_xor_sync(hmask, e3[c], off, 16);
+      da[c] += __shfl_xor_sync(hmask, da[c], off, 16);
+    }
+}
+
+// Single mesh: one half-warp per face, persistent over the mesh's faces.
 // Energy terms and dE/dalpha are summed per half-warp, then per block in a
 // fixed order, and written as one block partial (no atomics on floats).
 template <typename T, int NCP, int NPT>
@@ -125,184 +294,33 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
                 const float *__restrict__ rhi, const float *__restrict__ rlo, T *__restrict__ partial,
                 double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
   using S = FaceSmem<T, NCP, NPT>;
-  constexpr int NC4 = S::NC4, NCPP = S::NCPP, HW = S::HW, NT = FaceCfg<T>::threads;
+  constexpr int HW = S::HW, NT = FaceCfg<T>::threads;
   __shared__ S sm;
-
-  {
-    T *b = &sm.B[0][0][0].x;
-    for (int i = threadIdx.x; i < NPT * 5 * NCPP; i += NT) b[i] = (T)L.basis[i];
-    for (int i = threadIdx.x; i < NPT; i += NT) sm.W[i] = (T)L.weight[i];
-    for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
-  }
+  stage_basis<T, NCP, NPT, NT>(sm, L.basis, L.weight);
   __syncthreads();
 
   const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
   const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
   const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
   const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
-  const T kc = (T)P.kc, KA = (T)P.KA, kg = (T)P.kg, k_reg = (T)P.k_reg, dudv = (T)L.dudv;
+  const T dudv = (T)L.dudv;
   const bool reg_alpha = L.irregular && P.k_reg != 0.0;
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
   HalfWarpSums<T> acc;
 
-  // Global data of a face, loaded one face ahead (control-point indices two
-  // ahead) so the loads are in flight while the previous face computes.
-  struct Ahead {
-    int img[3] = {0, 0, 0};
-    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};  // precision form
-    double X[3] = {0, 0, 0};                     // plain path (image position)
-    T g0 = 1, rr0 = 0, P2 = 0, Hbar = 0, Pres = 0;
-    int dest = 0;
-  };
   const int stride = gridDim.x * HW;
-  auto load_cp = [&](int f) -> uint32_t {
-    return (f < L.nfaces && lane < NCP) ? __ldg(&L.cp[(size_t)f * NCP + lane]) : 0u;
-  };
-  auto load_ahead = [&](int f, uint32_t packed, Ahead &a) {
-    if (f >= L.nfaces) return;
-    if (lane < NCP) {
-      const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
-      a.img[0] = code % 3 - 1; a.img[1] = (code / 3) % 3 - 1; a.img[2] = code / 9 - 1;
-      if constexpr (sizeof(T) == 8) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          a.X[c] = r[3 * (size_t)v + c] + a.img[0] * P.box[0][c] + a.img[1] * P.box[1][c] + a.img[2] * P.box[2][c];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { a.hi[c] = rhi[3 * (size_t)v + c]; a.lo[c] = rlo[3 * (size_t)v + c]; }
-      }
-      a.dest = __ldg(&dest[(size_t)f * NCP + lane]);
-    }
-    if (lane < NPT) {
-      const size_t pi = (size_t)f * NPT + lane;
-      a.g0 = point_data<T>(L.g0, L.g0f, pi);
-      a.rr0 = point_data<T>(L.rr0, L.rr0f, pi);
-    }
-    a.P2 = point_data<T>(L.comp, L.compf, 3 * (size_t)f);
-    a.Hbar = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 1);
-    a.Pres = point_data<T>(L.comp, L.compf, 3 * (size_t)f + 2);
-  };
   int f = blockIdx.x * HW + hw;
-  Ahead cur, nxt;
-  uint32_t cp_next = load_cp(f + stride);
-  load_ahead(f, load_cp(f), cur);
+  FaceAhead<T> cur, nxt;
+  const int end = L.nfaces;
+  uint32_t cp_next = load_cp<NCP>(src, f + stride, end, lane);
+  load_ahead<T, NCP, NPT>(src, P, f, end, load_cp<NCP>(src, f, end, lane), lane, cur);
 
-  for (; f < L.nfaces; f += stride) {
-    const uint32_t cp_after = load_cp(f + 2 * stride);
-    load_ahead(f + stride, cp_next, nxt);
+  for (; f < end; f += stride) {
+    const uint32_t cp_after = load_cp<NCP>(src, f + 2 * stride, end, lane);
+    load_ahead<T, NCP, NPT>(src, P, f + stride, end, cp_next, lane, nxt);
     cp_next = cp_after;
-    // ---- 1. control points, relative to the patch corner
-    T xl[3] = {0, 0, 0};
-    if constexpr (sizeof(T) == 8) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const double a = __shfl_sync(hmask, cur.X[c], 0, 16);
-        xl[c] = alpha[c] * (cur.X[c] - a);
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float ahi = __shfl_sync(hmask, cur.hi[c], 0, 16), alo = __shfl_sync(hmask, cur.lo[c], 0, 16);
-        // lattice shift hi + lo (each term exact: images are -1, 0 or +1)
-        float sh = 0.f, she = 0.f, shl = 0.f;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          float t, e;
-          two_sum(sh, (float)cur.img[d] * P.box_hi[d][c], t, e);
-          sh = t;
-          she += e;
-          shl += (float)cur.img[d] * P.box_lo[d][c];
-        }
-        float s1, e1, s2, e2;
-        two_sum(cur.hi[c], sh, s1, e1);
-        two_sum(s1, -ahi, s2, e2);
-        xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl))));
-      }
-    }
-    if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
-    __syncwarp(hmask);
-
-    // ---- 2. lanes as quadrature points
-    T ea = 0, ec = 0, er = 0;
-    T dreg[3] = {0, 0, 0};
-    if (lane < NPT) {
-      Vec3<T> K[5];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) K[k] = {0, 0, 0};
-#pragma unroll 1
-      for (int c4 = 0; c4 < NC4; ++c4) {
-        const Q4<T> x0 = sm.X[hw][4 * c4], x1 = sm.X[hw][4 * c4 + 1], x2 = sm.X[hw][4 * c4 + 2],
-                    x3 = sm.X[hw][4 * c4 + 3];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          const Q4<T> b = sm.B[lane][k][c4];
-          K[k].x += b.x * x0.x + b.y * x1.x + b.z * x2.x + b.w * x3.x;
-          K[k].y += b.x * x0.y + b.y * x1.y + b.z * x2.y + b.w * x3.y;
-          K[k].z += b.x * x0.z + b.y * x1.z + b.z * x2.z + b.w * x3.z;
-        }
-      }
-      Vec3<T> Kb[5], Kreg[2];
-      point_adjoint<T>(K, sm.W[lane], cur.g0, cur.rr0, dudv, cur.P2, cur.Hbar, cur.Pres, kc, KA, kg, k_reg, &ea, &ec,
-                       &er, Kb, Kreg);
-#pragma unroll 1
-      for (int c4 = 0; c4 < NC4; ++c4) {
-        Q4<T> b[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) b[k] = sm.B[lane][k][c4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const T bk0 = (&b[0].x)[j], bk1 = (&b[1].x)[j], bk2 = (&b[2].x)[j], bk3 = (&b[3].x)[j],
-                  bk4 = (&b[4].x)[j];
-          Q4<T> t;
-          t.x = bk0 * Kb[0].x + bk1 * Kb[1].x + bk2 * Kb[2].x + bk3 * Kb[3].x + bk4 * Kb[4].x;
-          t.y = bk0 * Kb[0].y + bk1 * Kb[1].y + bk2 * Kb[2].y + bk3 * Kb[3].y + bk4 * Kb[4].y;
-          t.z = bk0 * Kb[0].z + bk1 * Kb[1].z + bk2 * Kb[2].z + bk3 * Kb[3].z + bk4 * Kb[4].z;
-          t.w = T(0);
-          sm.Tc[hw][lane][4 * c4 + j] = t;
-          if (reg_alpha) {
-            // igrad's box-scale derivative takes the angle-term adjoint with
-            // one more alpha factor (src/grad.C:7414-7421).
-            const Q4<T> xx = sm.X[hw][4 * c4 + j];
-            dreg[0] += (bk0 * Kreg[0].x + bk1 * Kreg[1].x) * xx.x;
-            dreg[1] += (bk0 * Kreg[0].y + bk1 * Kreg[1].y) * xx.y;
-            dreg[2] += (bk0 * Kreg[0].z + bk1 * Kreg[1].z) * xx.z;
-          }
-        }
-      }
-    }
-    __syncwarp(hmask);
-
-    // ---- 3. lanes as control points
-    T da[3] = {0, 0, 0};
-    if (lane < NCP) {
-      T G0 = 0, G1 = 0, G2 = 0;
-#pragma unroll
-      for (int p = 0; p < NPT; ++p) {
-        const Q4<T> t = sm.Tc[hw][p][lane];
-        G0 += t.x;
-        G1 += t.y;
-        G2 += t.z;
-      }
-      const int d = cur.dest;
-      partial[3 * (size_t)d] = alpha[0] * G0;
-      partial[3 * (size_t)d + 1] = alpha[1] * G1;
-      partial[3 * (size_t)d + 2] = alpha[2] * G2;
-      // dE/dalpha_c = sum_x G_xc (X - X_0)_xc: the patch gradient sums to
-      // zero, so coordinates relative to the corner give the same sum.
-      da[0] = G0 * xl[0] * ialpha[0];
-      da[1] = G1 * xl[1] * ialpha[1];
-      da[2] = G2 * xl[2] * ialpha[2];
-    }
-    if (reg_alpha)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) da[c] += (alpha[c] - T(1)) * ialpha[c] * dreg[c];
-    T e3[3] = {ea, ec, er};
-#pragma unroll
-    for (int off = 8; off >= 1; off >>= 1)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        e3[c] += __shfl_xor_sync(hmask, e3[c], off, 16);
-        da[c] += __shfl_xor_sync(hmask, da[c], off, 16);
-      }
+    T e3[3], da[3];
+    face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, dudv, reg_alpha, partial, e3, da);
     acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
     acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
     if (lane == 0 && !isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
@@ -427,17 +445,38 @@ __device__ __forceinline__ void normals3(uint64_t seed, uint32_t stream, uint64_
 }
 
 // Momentum update of the reference leapfrog (src/hd.C:1546-1693), one vertex.
+// Every product and sum is rounded on its own (no fused multiply-add), in the
+// reference's order of operations, so each kernel that uses it rounds alike.
 __device__ __forceinline__ void kick(const StepArgs &a, const double n[3], double pp[3], const double gg[3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     double q = pp[c];
-    if (a.kind == 2) q -= a.gamma * a.AK * q;
-    q += -gg[c] * a.AK * 0.5;
-    if (a.kind == 1) q += (1.0 / a.gamma) * a.sigma * n[c] / a.AK;
-    else q += a.sigma * n[c];
-    q += -gg[c] * a.AK * 0.5;
+    if (a.kind == 2) q = __dsub_rn(q, __dmul_rn(__dmul_rn(a.gamma, a.AK), q));  // friction
+    const double half = __dmul_rn(__dmul_rn(-gg[c], a.AK), 0.5);                 // half kick
+    q = __dadd_rn(q, half);
+    if (a.kind == 1)
+      q = __dadd_rn(q, __ddiv_rn(__dmul_rn(__dmul_rn(__ddiv_rn(1.0, a.gamma), a.sigma), n[c]), a.AK));
+    else
+      q = __dadd_rn(q, __dmul_rn(a.sigma, n[c]));
+    q = __dadd_rn(q, half);
     pp[c] = q;
   }
+}
+
+// The vertex-local update of one step with identity mass: overdamped BD
+// (r += -(D dt/kT) g + sqrt(2 D dt) xi), or the leapfrog kick followed by
+// r += p AK (p reset for BD). Rounded as kick() is.
+__device__ __forceinline__ void vertex_update(const StepArgs &a, const double gg[3], const double n[3], double rn[3],
+                                              double pp[3]) {
+  if (a.kind == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      rn[c] = __dadd_rn(rn[c], __dadd_rn(__dmul_rn(-a.mob_dt, gg[c]), __dmul_rn(a.sigma, n[c])));
+    return;
+  }
+  kick(a, n, pp, gg);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) rn[c] = __dadd_rn(rn[c], __dmul_rn(pp[c], a.AK));
 }
 
 // Step index of the current step: the run's first step plus the run index,
@@ -458,18 +497,14 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
     if constexpr (sizeof(T) == 8) normals3(a.seed, a.stream, st, v, n);
     else normals3_f32(a.seed, a.stream, st, v, n);
     double rn[3] = {r[3 * (size_t)v], r[3 * (size_t)v + 1], r[3 * (size_t)v + 2]};
-    if (a.kind == 0) {
+    double pp[3] = {0, 0, 0};
+    if (a.kind != 0)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) rn[c] += -a.mob_dt * gg[c] + a.sigma * n[c];
-    } else {
-      double pp[3] = {p[3 * (size_t)v], p[3 * (size_t)v + 1], p[3 * (size_t)v + 2]};
-      kick(a, n, pp, gg);
+      for (int c = 0; c < 3; ++c) pp[c] = p[3 * (size_t)v + c];
+    vertex_update(a, gg, n, rn, pp);
+    if (a.kind != 0)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        rn[c] += pp[c] * a.AK;  // identity M^-1
-        p[3 * (size_t)v + c] = (a.kind == 1) ? 0.0 : pp[c];
-      }
-    }
+      for (int c = 0; c < 3; ++c) p[3 * (size_t)v + c] = (a.kind == 1) ? 0.0 : pp[c];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       r[3 * (size_t)v + c] = rn[c];
@@ -501,13 +536,202 @@ __global__ void drift_kernel(int nv, StepArgs a, double *__restrict__ r, double 
                              const int *__restrict__ status) {
   if (*status) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nv; i += gridDim.x * blockDim.x) {
-    const double x = r[i] + qdot[i] * a.AK;
+    const double x = __dadd_rn(r[i], __dmul_rn(qdot[i], a.AK));
     r[i] = x;
     if (a.kind == 1) p[i] = 0.0;
     if (rhi) {
       const float h = (float)x;
       rhi[i] = h;
       rlo[i] = (float)(x - (double)h);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- batches
+//
+// Many meshes advance together. A tile is a run of up to tile_faces faces of
+// one patch type of one mesh (tiles never straddle meshes); a block takes
+// tiles in turn and sums each tile's energy terms in a fixed order, and each
+// mesh sums its own tiles in listed order. Every mesh keeps its own state,
+// noise stream, step counter and step limit, so a mesh's trajectory does not
+// depend on what else is in the batch. Tile and job counts are read from
+// device memory, so a captured step stays valid when the membership changes.
+
+// A job takes the step when it has neither stopped nor reached its limit.
+__device__ __forceinline__ bool job_active(const BatchFaceJob &J) { return !*J.status && J.cnt[1] < J.limit; }
+
+template <typename T, int NCP, int NPT>
+__global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
+    batch_face_kernel(const BatchJob *__restrict__ jobs, int group, const BatchTile *__restrict__ tiles,
+                      const int *__restrict__ counts, const double *__restrict__ basis,
+                      const double *__restrict__ weight, double dudv_d, int irregular,
+                      double *__restrict__ tile_sums) {
+  using S = FaceSmem<T, NCP, NPT>;
+  constexpr int HW = S::HW, NT = FaceCfg<T>::threads;
+  __shared__ S sm;
+  __shared__ BatchFaceJob sj;
+  __shared__ int s_active;
+  const int ntiles = counts[group], tile_base = counts[3 + group];
+  if ((int)blockIdx.x >= ntiles) return;
+  stage_basis<T, NCP, NPT, NT>(sm, basis, weight);
+  const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  const T dudv = (T)dudv_d;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tile = tiles[tile_base + t];
+    __syncthreads();  // the previous tile's readers of sj and sm.red are done
+    {
+      const int *src = reinterpret_cast<const int *>(&jobs[tile.job].f);
+      int *dst = reinterpret_cast<int *>(&sj);
+      for (int i = threadIdx.x; i < (int)(sizeof(BatchFaceJob) / sizeof(int)); i += NT) dst[i] = src[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_active = job_active(sj);  // one read for the whole block
+    __syncthreads();
+    HalfWarpSums<T> acc;
+    if (s_active) {
+      const FaceSrc &src = sj.src[group];
+      const SurfaceParams &P = sj.P;
+      const double *r = src.r;
+      const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
+      const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
+      const bool reg_alpha = irregular && P.k_reg != 0.0;
+      const int end = tile.first + tile.count;
+      int f = tile.first + hw;
+      FaceAhead<T> cur, nxt;
+      uint32_t cp_next = load_cp<NCP>(src, f + HW, end, lane);
+      load_ahead<T, NCP, NPT>(src, P, f, end, load_cp<NCP>(src, f, end, lane), lane, cur);
+      for (; f < end; f += HW) {
+        const uint32_t cp_after = load_cp<NCP>(src, f + 2 * HW, end, lane);
+        load_ahead<T, NCP, NPT>(src, P, f + HW, end, cp_next, lane, nxt);
+        cp_next = cp_after;
+        T e3[3], da[3];
+        face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, dudv, reg_alpha, (T *)sj.partial, e3,
+                                  da);
+        acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+        cur = nxt;
+        __syncwarp(hmask);
+      }
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) sm.red[hw][q] = acc.get(q);
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double s = 0;
+#pragma unroll
+      for (int h = 0; h < HW; ++h) s += sm.red[h][threadIdx.x];
+      tile_sums[3 * (size_t)(tile_base + t) + threadIdx.x] = s;
+    }
+  }
+}
+
+// Per job (one warp each): sum its tiles in listed order, record the step's
+// energy in the job's run, flag non-finite or diverging energies (src/hd.C:
+// 1280-1305) for that job only, advance its run index. live[j] tells the
+// update whether job j took this step; prog[j] = {steps done, status}.
+__global__ void batch_reduce_kernel(const BatchJob *__restrict__ jobs, const int *__restrict__ counts,
+                                    const int *__restrict__ tile_off, const int *__restrict__ tile_idx,
+                                    const double *__restrict__ tile_sums, int *__restrict__ live,
+                                    unsigned long long *__restrict__ prog) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= counts[6]) return;
+  const BatchJob &J = jobs[j];
+  const bool active = job_active(J.f);  // uniform over the warp: nothing below changes it before the sync
+  __syncwarp();
+  double a[3] = {0, 0, 0};
+  if (active)
+    for (int k = tile_off[j] + lane; k < tile_off[j + 1]; k += 32)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) a[q] += tile_sums[3 * (size_t)tile_idx[k] + q];
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) a[q] += __shfl_xor_sync(0xffffffffu, a[q], off);
+  if (lane != 0) return;
+  int st = *J.f.status;
+  uint64_t done = J.f.cnt[1];
+  if (active) {
+    const double e = a[0] + a[1] + a[2];
+    J.E[0] = e;
+    J.parts[0] = a[0]; J.parts[1] = a[1]; J.parts[2] = a[2];
+    if (!isfinite(e)) st |= kStatusNonFinite;
+    if (J.energies) {
+      J.energies[done] = e;
+      if (J.threshold > 0 && done > 0 && e - J.energies[done - 1] > J.threshold) st |= kStatusDiverged;
+    }
+    *J.f.status = st;
+    // As in a single-mesh run, the step whose energy is flagged does not move.
+    J.f.cnt[1] = ++done;
+  }
+  live[j] = active && !st;
+  prog[2 * j] = done;
+  prog[2 * j + 1] = (unsigned long long)st;
+}
+
+// Gather fused with each live job's vertex-local update (overdamped BD, or the
+// leapfrog kinds with identity mass), with the job's own integrator settings.
+template <typename T>
+__global__ void batch_gather_step_kernel(const BatchJob *__restrict__ jobs, const BatchTile *__restrict__ vtiles,
+                                         const int *__restrict__ counts, const int *__restrict__ live) {
+  const int nvtiles = counts[7];
+  for (int t = blockIdx.x; t < nvtiles; t += gridDim.x) {
+    const BatchTile tile = vtiles[t];
+    if (!live[tile.job] || (int)threadIdx.x >= tile.count) continue;
+    const BatchJob &J = jobs[tile.job];
+    const StepArgs &a = J.a;
+    const int v = tile.first + threadIdx.x;
+    const uint64_t st = J.f.cnt[0] + J.f.cnt[1] - 1;
+    double gg[3], n[3];
+    vertex_gradient((const T *)J.f.partial, J.off, v, gg);
+    if constexpr (sizeof(T) == 8) normals3(a.seed, a.stream, st, v, n);
+    else normals3_f32(a.seed, a.stream, st, v, n);
+    double *r = J.r, *p = J.p;
+    double rn[3] = {r[3 * (size_t)v], r[3 * (size_t)v + 1], r[3 * (size_t)v + 2]};
+    double pp[3] = {0, 0, 0};
+    if (a.kind != 0)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pp[c] = p[3 * (size_t)v + c];
+    vertex_update(a, gg, n, rn, pp);
+    if (a.kind != 0)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) p[3 * (size_t)v + c] = (a.kind == 1) ? 0.0 : pp[c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      r[3 * (size_t)v + c] = rn[c];
+      if (J.rhi) {
+        const float h = (float)rn[c];
+        J.rhi[3 * (size_t)v + c] = h;
+        J.rlo[3 * (size_t)v + c] = (float)(rn[c] - (double)h);
+      }
+    }
+  }
+}
+
+// Start of the runs of the jobs flagged in start[]: counters {step0, 0},
+// status cleared, FP32 hi/lo pairs of the positions (precision form).
+__global__ void batch_start_kernel(const BatchJob *__restrict__ jobs, const BatchTile *__restrict__ vtiles,
+                                   const int *__restrict__ counts, const int *__restrict__ start,
+                                   const unsigned long long *__restrict__ step0) {
+  const int nvtiles = counts[7];
+  for (int t = blockIdx.x; t < nvtiles; t += gridDim.x) {
+    const BatchTile tile = vtiles[t];
+    if (!start[tile.job]) continue;
+    const BatchJob &J = jobs[tile.job];
+    if (tile.first == 0 && threadIdx.x == 0) {
+      J.f.cnt[0] = step0[tile.job];
+      J.f.cnt[1] = 0;
+      *J.f.status = 0;
+    }
+    if (J.rhi && (int)threadIdx.x < tile.count) {
+      const int v = tile.first + threadIdx.x;
+      for (int c = 0; c < 3; ++c) {
+        const double x = J.r[3 * (size_t)v + c];
+        const float h = (float)x;
+        J.rhi[3 * (size_t)v + c] = h;
+        J.rlo[3 * (size_t)v + c] = (float)(x - (double)h);
+      }
     }
   }
 }
@@ -664,6 +888,66 @@ cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const doub
   if (grid > 152 * 16) grid = 152 * 16;
   dev::spmv_kernel<<<grid, 32 * warps_per_block, 0, s>>>(nrow, row_ptr, col, val, scalev, scale, alphas, in, out,
                                                         accumulate);
+  return cudaGetLastError();
+}
+
+}  // namespace umcp
+
+namespace umcp {
+
+template <typename T>
+int batch_face_blocks(int ncp, int npt) {
+  return face_blocks<T>(1 << 30, ncp, npt);  // device-filling persistent grid
+}
+template int batch_face_blocks<double>(int, int);
+template int batch_face_blocks<float>(int, int);
+
+template <typename T>
+cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile *tiles, const int *counts,
+                               const double *basis, const double *weight, int ncp, int npt, double dudv,
+                               int irregular, double *tile_sums, int grid, cudaStream_t s) {
+  constexpr int NT = dev::FaceCfg<T>::threads;
+  if (ncp == 12 && npt == 15)
+    dev::batch_face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv, irregular,
+                                                          tile_sums);
+  else if (ncp == 11 && npt == 16)
+    dev::batch_face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv, irregular,
+                                                          tile_sums);
+  else if (ncp == 13 && npt == 16)
+    dev::batch_face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv, irregular,
+                                                          tile_sums);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+template cudaError_t launch_batch_faces<double>(const BatchJob *, int, const BatchTile *, const int *,
+                                                const double *, const double *, int, int, double, int, double *, int,
+                                                cudaStream_t);
+template cudaError_t launch_batch_faces<float>(const BatchJob *, int, const BatchTile *, const int *, const double *,
+                                               const double *, int, int, double, int, double *, int, cudaStream_t);
+
+cudaError_t launch_batch_reduce(const BatchJob *jobs, const int *counts, int max_jobs, const int *tile_off,
+                                const int *tile_idx, const double *tile_sums, int *live, unsigned long long *prog,
+                                cudaStream_t s) {
+  dev::batch_reduce_kernel<<<grid_for(max_jobs * 32, 256), 256, 0, s>>>(jobs, counts, tile_off, tile_idx, tile_sums,
+                                                                        live, prog);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_batch_gather_step(const BatchJob *jobs, const BatchTile *vtiles, const int *counts,
+                                     const int *live, int grid, cudaStream_t s) {
+  dev::batch_gather_step_kernel<T><<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, live);
+  return cudaGetLastError();
+}
+template cudaError_t launch_batch_gather_step<double>(const BatchJob *, const BatchTile *, const int *, const int *,
+                                                      int, cudaStream_t);
+template cudaError_t launch_batch_gather_step<float>(const BatchJob *, const BatchTile *, const int *, const int *,
+                                                     int, cudaStream_t);
+
+cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const int *start,
+                               const unsigned long long *step0, int grid, cudaStream_t s) {
+  dev::batch_start_kernel<<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, start, step0);
   return cudaGetLastError();
 }
 
