@@ -114,6 +114,8 @@ umcp_status umcp_ctx_synchronize(umcp_ctx *ctx);
 /* The cudaStream_t (as void*) every call on this ctx is queued on, so a
  * caller can order its own work (timing events, copies) with the engine's. */
 umcp_status umcp_ctx_stream(umcp_ctx *ctx, void **stream);
+/* Free and total device memory of the context's device (cudaMemGetInfo). */
+umcp_status umcp_ctx_mem_info(umcp_ctx *ctx, size_t *free_bytes, size_t *total_bytes);
 
 /* Upload a plan; the mesh keeps its own state buffers on the device. */
 umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, const umcp_params *p, umcp_mesh **out);
@@ -156,8 +158,14 @@ typedef struct {
   int nv, n_faces, n_points, n_slots;
   int kernels_per_step, kernels_per_step_mass;
   int precision;
+  long long device_bytes;  /* device memory held by the mesh's buffers */
 } umcp_mesh_info;
 umcp_status umcp_mesh_info_get(const umcp_mesh *mesh, umcp_mesh_info *info);
+/* Device bytes umcp_mesh_create would allocate for this plan at this
+ * precision, plus the energy record of an n_energies-step run: the
+ * footprint a server admits jobs by. */
+umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *ctx, int precision, int64_t n_energies,
+                                   size_t *bytes);
 
 /* ---- effective mass ---------------------------------------------------- */
 /* Install M^-1 as a CSR matrix over vertices (SparseMatrix nzl/nzv rows,
@@ -252,6 +260,72 @@ umcp_status umcp_batch_run(umcp_batch *batch, int n_steps);
 umcp_status umcp_batch_poll(umcp_batch *batch, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_job(umcp_batch *batch, const umcp_mesh *mesh, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_info_get(const umcp_batch *batch, umcp_batch_info *info);
+
+/* ---- Serving: a request loop over one batch.
+ * No counterpart in the reference. Jobs (a .mesh file, parameters, an
+ * integrator, a step count) are submitted from any host thread. Host worker
+ * threads build their plans; the server thread admits ready jobs in arrival
+ * order while their device footprint (umcp_plan_device_bytes) fits the HBM
+ * budget, adds them to its batch (their state stays resident until they
+ * finish), runs the batch in chunks of steps, and at each chunk boundary
+ * copies out the results of finished jobs and frees their memory. Jobs
+ * admitted while a chunk runs are built and uploaded during it and join at
+ * the next chunk. Each job's trajectory is the one umcp_run gives its mesh
+ * alone. Times are seconds on the server's steady clock. */
+typedef struct umcp_server umcp_server;
+typedef struct {
+  int precision;               /* of every job (a job's params.precision is overridden) */
+  double hbm_budget_bytes;     /* footprint limit of resident jobs; 0: 80% of the free memory at creation */
+  int max_jobs;                /* resident job cap; 0: none */
+  double chunk_ms;             /* target wall time of one chunk; 0: 25 ms */
+  int builder_threads;         /* plan-building threads; 0: hardware threads, at most 16 */
+  int tile_faces;              /* as umcp_batch_opts.tile_faces */
+} umcp_server_opts;
+typedef struct {
+  const char *mesh_path;       /* read by a worker thread; must exist until the job is built */
+  umcp_params params;          /* lipid_directives text is copied at submit */
+  umcp_integrator it;          /* use_mass must be 0 */
+  uint64_t step0;
+  int64_t n_steps;
+  int keep_energies;           /* keep the per-step energies for umcp_server_fetch */
+} umcp_job_desc;
+typedef enum { UMCP_JOB_QUEUED = 0, UMCP_JOB_BUILDING = 1, UMCP_JOB_READY = 2, UMCP_JOB_RUNNING = 3,
+               UMCP_JOB_DONE = 4 } umcp_job_state;
+typedef struct {
+  int state;                   /* umcp_job_state */
+  int status;                  /* umcp_status of a done job */
+  int nv;
+  int64_t steps_done;
+  double t_submit, t_admit, t_done;  /* -1 until reached */
+  double device_bytes;
+  char message[160];           /* error text of a failed job */
+} umcp_job_info;
+typedef struct {
+  long long submitted, completed, failed, queued, running, chunks;
+  double p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;  /* submit to done, completed jobs */
+  double vertex_steps;         /* performed by all jobs so far */
+  double busy_s;               /* wall time spent in chunks (launch to results) */
+  double vertex_steps_per_s;   /* vertex_steps / busy_s */
+  double hbm_budget_bytes, hbm_in_use_bytes, hbm_peak_bytes;
+  int chunk_steps;             /* size of the latest chunk */
+} umcp_server_stats;
+umcp_status umcp_server_create(umcp_ctx *ctx, const umcp_server_opts *opts, umcp_server **out);
+/* Stops the loop after the chunk in flight; unfinished jobs are dropped. */
+void umcp_server_destroy(umcp_server *server);
+umcp_status umcp_server_submit(umcp_server *server, const umcp_job_desc *job, uint64_t *job_id);
+/* Waits until the job is done (UMCP_OK) or timeout_s passes (UMCP_ERR_TIMEOUT);
+ * timeout_s < 0 waits without limit. The job's own status is in its info. */
+umcp_status umcp_server_wait(umcp_server *server, uint64_t job_id, double timeout_s);
+umcp_status umcp_server_wait_all(umcp_server *server, double timeout_s);
+umcp_status umcp_server_job(umcp_server *server, uint64_t job_id, umcp_job_info *info);
+/* Copies a done job's final state r (3*nv+3) and, if kept, its energies
+ * (steps_done of them); either may be NULL. */
+umcp_status umcp_server_fetch(umcp_server *server, uint64_t job_id, double *r, double *energies);
+/* Forgets a done job and its results. */
+umcp_status umcp_server_release(umcp_server *server, uint64_t job_id);
+umcp_status umcp_server_stats_get(umcp_server *server, umcp_server_stats *stats);
+/* Seconds on the server's clock (the clock of the job times). */
+double umcp_server_now(const umcp_server *server);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,7 @@ OVERDAMPED_BD = 0
 BD_MEMBRANE = 1
 LANGEVIN = 2
 
+ERR_NOMEM = 6
 ERR_NONFINITE = 4
 ERR_DIVERGED = 8
 
@@ -62,6 +63,7 @@ class MeshInfo(C.Structure):
     _fields_ = [
         ("nv", C.c_int), ("n_faces", C.c_int), ("n_points", C.c_int), ("n_slots", C.c_int),
         ("kernels_per_step", C.c_int), ("kernels_per_step_mass", C.c_int), ("precision", C.c_int),
+        ("device_bytes", C.c_longlong),
     ]
 
 
@@ -84,6 +86,41 @@ class BatchInfo(C.Structure):
         ("tile_faces", C.c_int), ("kernels_per_step", C.c_int), ("tuned_face_ms", C.c_double),
     ]
 
+
+class ServerOpts(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int), ("hbm_budget_bytes", C.c_double), ("max_jobs", C.c_int), ("chunk_ms", C.c_double),
+        ("builder_threads", C.c_int), ("tile_faces", C.c_int),
+    ]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [
+        ("mesh_path", C.c_char_p), ("params", Params), ("it", Integrator), ("step0", C.c_uint64),
+        ("n_steps", C.c_int64), ("keep_energies", C.c_int),
+    ]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [
+        ("state", C.c_int), ("status", C.c_int), ("nv", C.c_int), ("steps_done", C.c_int64),
+        ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("device_bytes", C.c_double),
+        ("message", C.c_char * 160),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+        ("queued", C.c_longlong), ("running", C.c_longlong), ("chunks", C.c_longlong),
+        ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double),
+        ("max_latency_s", C.c_double), ("vertex_steps", C.c_double), ("busy_s", C.c_double),
+        ("vertex_steps_per_s", C.c_double), ("hbm_budget_bytes", C.c_double), ("hbm_in_use_bytes", C.c_double),
+        ("hbm_peak_bytes", C.c_double), ("chunk_steps", C.c_int),
+    ]
+
+
+JOB_DONE = 4
 
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -137,10 +174,23 @@ _SIGNATURES = {
     "umcp_batch_poll": [_VP, _I64, _I],
     "umcp_batch_job": [_VP, _VP, _I64, _I],
     "umcp_batch_info_get": [_VP, C.POINTER(BatchInfo)],
+    "umcp_ctx_mem_info": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
+    "umcp_plan_device_bytes": [_VP, _VP, C.c_int, C.c_int64, C.POINTER(C.c_size_t)],
+    "umcp_server_create": [_VP, C.POINTER(ServerOpts), C.POINTER(_VP)],
+    "umcp_server_destroy": [_VP],
+    "umcp_server_submit": [_VP, C.POINTER(JobDesc), C.POINTER(C.c_uint64)],
+    "umcp_server_wait": [_VP, C.c_uint64, C.c_double],
+    "umcp_server_wait_all": [_VP, C.c_double],
+    "umcp_server_job": [_VP, C.c_uint64, C.POINTER(JobInfo)],
+    "umcp_server_fetch": [_VP, C.c_uint64, _D, _D],
+    "umcp_server_release": [_VP, C.c_uint64],
+    "umcp_server_stats_get": [_VP, C.POINTER(ServerStats)],
+    "umcp_server_now": [_VP],
     "umcp_last_error": [],
     "umcp_status_string": [C.c_int],
 }
-_VOID = {"umcp_plan_destroy", "umcp_ctx_destroy", "umcp_mesh_destroy", "umcp_batch_destroy"}
+_VOID = {"umcp_plan_destroy", "umcp_ctx_destroy", "umcp_mesh_destroy", "umcp_batch_destroy", "umcp_server_destroy"}
+_DOUBLE = {"umcp_server_now"}
 _STR = {"umcp_last_error", "umcp_status_string"}
 
 _lib = None
@@ -156,7 +206,8 @@ def library() -> C.CDLL:
         for name, args in _SIGNATURES.items():
             fn = getattr(lib, name)
             fn.argtypes = args
-            fn.restype = None if name in _VOID else (C.c_char_p if name in _STR else C.c_int)
+            fn.restype = (None if name in _VOID else C.c_char_p if name in _STR else C.c_double if name in _DOUBLE
+                          else C.c_int)
         _lib = lib
     return _lib
 
@@ -230,6 +281,12 @@ class Plan:
     def handle(self):
         return self._h
 
+    def device_bytes(self, ctx: "Context", precision: int, n_energies: int = 0) -> int:
+        """Device bytes a Mesh of this plan holds (plus an n_energies-step energy record)."""
+        b = C.c_size_t()
+        _check(library().umcp_plan_device_bytes(self._h, ctx.handle, precision, n_energies, C.byref(b)))
+        return b.value
+
     def positions(self) -> np.ndarray:
         r = np.zeros(3 * self.nv + 3)
         _check(library().umcp_plan_positions(self._h, _dp(r)))
@@ -290,6 +347,11 @@ class Context:
 
     def synchronize(self) -> None:
         _check(library().umcp_ctx_synchronize(self._h))
+
+    def mem_info(self) -> tuple[int, int]:
+        f, t = C.c_size_t(), C.c_size_t()
+        _check(library().umcp_ctx_mem_info(self._h, C.byref(f), C.byref(t)))
+        return f.value, t.value
 
     def stream(self) -> int:
         """The cudaStream_t every engine call on this context is queued on."""
@@ -451,3 +513,70 @@ class Batch:
 def integrator(kind=OVERDAMPED_BD, time_step=1.0, gamma=0.0, D=0.0, seed=1, stream=0, divergence_threshold=0.0,
                use_mass=0) -> Integrator:
     return Integrator(kind, time_step, gamma, D, seed, stream, divergence_threshold, use_mass)
+
+
+class Server:
+    """Request loop over one batch (umcp_server_*): submit jobs from any thread,
+    wait for them, fetch their final state and energies."""
+
+    def __init__(self, ctx: Context, precision: int = FP32_CENTRED, hbm_budget_bytes: float = 0.0, max_jobs: int = 0,
+                 chunk_ms: float = 0.0, builder_threads: int = 0, tile_faces: int = 0):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        self._keep = {}  # id -> (path bytes, lipid bytes, nv) kept alive until the job is built
+        opts = ServerOpts(precision, hbm_budget_bytes, max_jobs, chunk_ms, builder_threads, tile_faces)
+        _check(library().umcp_server_create(ctx.handle, C.byref(opts), C.byref(self._h)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.umcp_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, mesh_path, prm: Params, it: Integrator, step0: int, n_steps: int,
+               keep_energies: bool = False) -> int:
+        path = str(mesh_path).encode()
+        d = JobDesc(path, prm, it, step0, n_steps, int(keep_energies))
+        jid = C.c_uint64()
+        _check(library().umcp_server_submit(self._h, C.byref(d), C.byref(jid)))
+        self._keep[jid.value] = path
+        return jid.value
+
+    def wait(self, jid: int, timeout_s: float = -1.0) -> bool:
+        st = library().umcp_server_wait(self._h, jid, timeout_s)
+        if st not in (0, 5):
+            _check(st)
+        return st == 0
+
+    def wait_all(self, timeout_s: float = -1.0) -> bool:
+        st = library().umcp_server_wait_all(self._h, timeout_s)
+        if st not in (0, 5):
+            _check(st)
+        return st == 0
+
+    def job(self, jid: int) -> JobInfo:
+        i = JobInfo()
+        _check(library().umcp_server_job(self._h, jid, C.byref(i)))
+        return i
+
+    def fetch(self, jid: int) -> tuple[np.ndarray, np.ndarray]:
+        """(final r, kept energies) of a done job."""
+        i = self.job(jid)
+        r = np.zeros(3 * i.nv + 3)
+        e = np.zeros(max(i.steps_done, 1))
+        _check(library().umcp_server_fetch(self._h, jid, _dp(r), _dp(e)))
+        return r, e[:i.steps_done]
+
+    def release(self, jid: int) -> None:
+        _check(library().umcp_server_release(self._h, jid))
+        self._keep.pop(jid, None)
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(library().umcp_server_stats_get(self._h, C.byref(s)))
+        return s
+
+    def now(self) -> float:
+        return library().umcp_server_now(self._h)

@@ -249,6 +249,16 @@ extern "C" umcp_status umcp_ctx_stream(umcp_ctx *ctx, void **stream) {
   return UMCP_OK;
 }
 
+extern "C" umcp_status umcp_ctx_mem_info(umcp_ctx *ctx, size_t *free_bytes, size_t *total_bytes) {
+  if (!ctx) return fail(UMCP_ERR_INVALID, "null ctx");
+  UMCP_CUDA(cudaSetDevice(ctx->device));
+  size_t f = 0, t = 0;
+  UMCP_CUDA(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return UMCP_OK;
+}
+
 extern "C" umcp_status umcp_ctx_synchronize(umcp_ctx *ctx) {
   if (!ctx) return fail(UMCP_ERR_INVALID, "null ctx");
   UMCP_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -401,8 +411,10 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   if (m->precision == UMCP_FP32_CENTRED) {
     UMCP_CUDA(m->rhi.alloc(3 * (size_t)ME.nv * sizeof(float)));
     UMCP_CUDA(m->rlo.alloc(3 * (size_t)ME.nv * sizeof(float)));
+    // On the legacy stream, which does not wait for (or stall) work queued on
+    // the context's non-blocking stream, e.g. a batch a server is running.
     UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), 0));
-    UMCP_CUDA(cudaDeviceSynchronize());
+    UMCP_CUDA(cudaStreamSynchronize(0));
     m->split_valid = true;
   }
   *out = m.release();
@@ -555,6 +567,44 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
   info->kernels_per_step = groups + 1;
   info->kernels_per_step_mass = groups + 5;
   info->precision = m->precision;
+  info->device_bytes = (long long)m->device_bytes();
+  return UMCP_OK;
+}
+
+// Device bytes umcp_mesh_create allocates for a plan, plus the energy record
+// of a run of n_energies steps: the same sizes, buffer by buffer.
+extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *ctx, int precision,
+                                              int64_t n_energies, size_t *bytes) {
+  if (!plan || !ctx || !bytes || n_energies < 0) return fail(UMCP_ERR_INVALID, "bad argument");
+  if (precision != UMCP_FP64 && precision != UMCP_FP32_CENTRED) return fail(UMCP_ERR_INVALID, "unknown precision");
+  UMCP_CUDA(cudaSetDevice(ctx->device));
+  const Plan &PL = plan->plan;
+  const size_t nv = (size_t)plan->mesh.nv, nst = 3 * nv + 3;
+  const bool f32 = precision == UMCP_FP32_CENTRED;
+  size_t b = 0, slots = 0;
+  int nblocks = 0;
+  auto group = [&](const PatchBasis &B, size_t nf) {
+    const size_t ncpp = (size_t)(B.ncp + 3) / 4 * 4;
+    b += nf * B.ncp * 4 + 2 * nf * B.npt * 8 + nf * 3 * 8 + (size_t)B.npt * 5 * ncpp * 8 + B.weight.size() * 8 +
+         nf * B.ncp * 4;
+    if (f32) b += 2 * nf * B.npt * 4 + nf * 3 * 4;
+    slots += nf * B.ncp;
+    nblocks += f32 ? face_blocks<float>((int)nf, B.ncp, B.npt) : face_blocks<double>((int)nf, B.ncp, B.npt);
+  };
+  group(PL.regular, PL.reg_faces.size());
+  for (int val : {5, 7}) {
+    size_t nf = 0;
+    for (const Face &F : PL.irr_faces) nf += F.valence == val;
+    if (nf) group(PL.irregular[val], nf);
+  }
+  b += (nv + 1) * 4;                                  // off
+  b += (size_t)std::max(nblocks, 1) * 6 * 8;          // blockpart
+  b += slots * 3 * (f32 ? 4 : 8);                     // partial
+  b += 3 * nst * 8 + 2 * 3 * nv * 8;                  // r, g, r_eval; p, qdot
+  b += 8 + 3 * 8 + 4 + 2 * 8 + 4 + 3 * 8;             // E, parts, status, cnt, done, alphas
+  if (f32) b += 2 * 3 * nv * 4;                       // rhi, rlo
+  b += (size_t)n_energies * 8;                        // energy record
+  *bytes = b;
   return UMCP_OK;
 }
 

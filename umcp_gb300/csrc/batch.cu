@@ -43,6 +43,7 @@ struct umcp_batch {
   int opt_tile_faces = 0, opt_blocks_per_sm = 0;
   int tile_faces = 0;  // chosen at the first run when opt_tile_faces is 0
   double tuned_ms = 0;
+  long long tuned_faces = 0;  // faces in the batch when the tile size was last timed
   std::vector<Job> jobs;
   bool dirty = true;
   // Each patch type's basis (the same for every mesh: it depends on the
@@ -386,7 +387,8 @@ extern "C" umcp_status umcp_batch_add(umcp_batch *b, umcp_mesh *m, const umcp_in
   J.n_steps = n_steps;
   UMCP_CUDA(cudaSetDevice(b->ctx->device));
   if ((size_t)n_steps > m->energies_cap) {
-    UMCP_CUDA(cudaStreamSynchronize(b->ctx->stream));  // the buffer may be in use by queued steps
+    // A buffer that exists may be in use by queued steps; a new mesh has none.
+    if (m->energies.p) UMCP_CUDA(cudaStreamSynchronize(b->ctx->stream));
     m->drop_graphs();  // the mesh's own graphs hold the energies pointer
     UMCP_CUDA(m->energies.alloc((size_t)n_steps * sizeof(double)));
     m->energies_cap = (size_t)n_steps;
@@ -428,7 +430,14 @@ extern "C" umcp_status umcp_batch_run(umcp_batch *b, int n_steps) {
   if ((st = harvest(b)) != UMCP_OK) return st;
   if (b->dirty && (st = rebuild(b)) != UMCP_OK) return st;
   if ((st = start_jobs(b)) != UMCP_OK) return st;
-  if (b->tile_faces == 0 && (st = autotune(b)) != UMCP_OK) return st;
+  // Tile size by timing, at the first run and again whenever the batch has
+  // grown fourfold in faces since (a few times at most over a batch's life).
+  long long faces = 0;
+  for (const Job &J : b->jobs) faces += J.m->nfaces;
+  if (b->opt_tile_faces == 0 && (b->tile_faces == 0 || faces >= 4 * b->tuned_faces)) {
+    if ((st = autotune(b)) != UMCP_OK) return st;
+    b->tuned_faces = faces;
+  }
   const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
   if (full > 0) {
     if (!b->g_chunk && (st = capture(b, kGraphChunk, &b->g_chunk)) != UMCP_OK) return st;

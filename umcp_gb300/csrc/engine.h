@@ -100,6 +100,19 @@ struct umcp_mesh {
     graphs.clear();
   }
 
+  // Device bytes held by the mesh's buffers.
+  size_t device_bytes() const {
+    size_t b = 0;
+    for (auto &G : groups)
+      for (const umcp::DevBuf *x : {&G->cp, &G->g0, &G->rr0, &G->comp, &G->basis, &G->weight, &G->dest, &G->g0f,
+                                    &G->rr0f, &G->compf})
+        b += x->bytes;
+    for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
+                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas})
+      b += x->bytes;
+    return b;
+  }
+
   ~umcp_mesh() {
     drop_graphs();
     if (h_stage) cudaFreeHost(h_stage);
