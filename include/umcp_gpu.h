@@ -159,6 +159,7 @@ typedef struct {
   int kernels_per_step, kernels_per_step_mass;
   int precision;
   long long device_bytes;  /* device memory held by the mesh's buffers */
+  long long h2d_bytes;     /* host-to-device bytes umcp_mesh_create copied (tables, bases, positions) */
 } umcp_mesh_info;
 umcp_status umcp_mesh_info_get(const umcp_mesh *mesh, umcp_mesh_info *info);
 /* Device bytes umcp_mesh_create would allocate for this plan at this
@@ -260,6 +261,11 @@ umcp_status umcp_batch_run(umcp_batch *batch, int n_steps);
 umcp_status umcp_batch_poll(umcp_batch *batch, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_job(umcp_batch *batch, const umcp_mesh *mesh, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_info_get(const umcp_batch *batch, umcp_batch_info *info);
+/* Queues only the face launches of one step over the batch's current jobs
+ * (tables as of the latest run): the unit a roofline measurement times. The
+ * jobs' states and counters do not change; jobs that have done their step
+ * count or stopped are skipped, as in a step. */
+umcp_status umcp_batch_face_pass(umcp_batch *batch);
 
 /* ---- Serving: a request loop over one batch.
  * No counterpart in the reference. Jobs (a .mesh file, parameters, an
@@ -298,6 +304,7 @@ typedef struct {
   int64_t steps_done;
   double t_submit, t_admit, t_done;  /* -1 until reached */
   double device_bytes;
+  double h2d_bytes, d2h_bytes; /* copied in at admission; copied out at the end */
   char message[160];           /* error text of a failed job */
 } umcp_job_info;
 typedef struct {

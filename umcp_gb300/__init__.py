@@ -63,7 +63,7 @@ class MeshInfo(C.Structure):
     _fields_ = [
         ("nv", C.c_int), ("n_faces", C.c_int), ("n_points", C.c_int), ("n_slots", C.c_int),
         ("kernels_per_step", C.c_int), ("kernels_per_step_mass", C.c_int), ("precision", C.c_int),
-        ("device_bytes", C.c_longlong),
+        ("device_bytes", C.c_longlong), ("h2d_bytes", C.c_longlong),
     ]
 
 
@@ -105,6 +105,7 @@ class JobInfo(C.Structure):
     _fields_ = [
         ("state", C.c_int), ("status", C.c_int), ("nv", C.c_int), ("steps_done", C.c_int64),
         ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("device_bytes", C.c_double),
+        ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
         ("message", C.c_char * 160),
     ]
 
@@ -174,6 +175,7 @@ _SIGNATURES = {
     "umcp_batch_poll": [_VP, _I64, _I],
     "umcp_batch_job": [_VP, _VP, _I64, _I],
     "umcp_batch_info_get": [_VP, C.POINTER(BatchInfo)],
+    "umcp_batch_face_pass": [_VP],
     "umcp_ctx_mem_info": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
     "umcp_plan_device_bytes": [_VP, _VP, C.c_int, C.c_int64, C.POINTER(C.c_size_t)],
     "umcp_server_create": [_VP, C.POINTER(ServerOpts), C.POINTER(_VP)],
@@ -508,6 +510,10 @@ class Batch:
         i = BatchInfo()
         _check(library().umcp_batch_info_get(self._h, C.byref(i)))
         return i
+
+    def face_pass(self) -> None:
+        """Queues the face launches of one step only (for timing)."""
+        _check(library().umcp_batch_face_pass(self._h))
 
 
 def integrator(kind=OVERDAMPED_BD, time_step=1.0, gamma=0.0, D=0.0, seed=1, stream=0, divergence_threshold=0.0,

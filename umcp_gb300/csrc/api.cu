@@ -568,6 +568,13 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
   info->kernels_per_step_mass = groups + 5;
   info->precision = m->precision;
   info->device_bytes = (long long)m->device_bytes();
+  // bytes umcp_mesh_create copied in: face tables, bases, slot offsets, positions
+  long long h2d = (long long)(m->off.bytes + (3 * (size_t)m->nv + 3) * sizeof(double));
+  for (auto &G : m->groups)
+    for (const DevBuf *x : {&G->cp, &G->g0, &G->rr0, &G->comp, &G->basis, &G->weight, &G->dest, &G->g0f, &G->rr0f,
+                            &G->compf})
+      h2d += (long long)x->bytes;
+  info->h2d_bytes = h2d;
   return UMCP_OK;
 }
 

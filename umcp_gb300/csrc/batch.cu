@@ -504,3 +504,11 @@ extern "C" umcp_status umcp_batch_info_get(const umcp_batch *b, umcp_batch_info 
   info->tuned_face_ms = b->tuned_ms;
   return UMCP_OK;
 }
+
+extern "C" umcp_status umcp_batch_face_pass(umcp_batch *b) {
+  if (!b) return fail(UMCP_ERR_INVALID, "null batch");
+  if (b->dirty || b->jobs.empty()) return fail(UMCP_ERR_INVALID, "the batch has not run with its current jobs");
+  UMCP_CUDA(cudaSetDevice(b->ctx->device));
+  UMCP_CUDA(queue_faces(b));
+  return UMCP_OK;
+}

@@ -48,6 +48,7 @@ struct SJob {
   umcp_mesh *mesh = nullptr;
   int64_t steps_done = 0;
   double t_submit = -1, t_admit = -1, t_done = -1;
+  double h2d = 0, d2h = 0;
   std::vector<double> r, energies;
 };
 
@@ -155,7 +156,10 @@ void umcp_server::admit_pass() {
     }
     umcp_mesh *m = nullptr;
     umcp_status st = umcp_mesh_create(ctx, j->plan, &j->prm, &m);
+    umcp_mesh_info mi{};
+    if (st == UMCP_OK) st = umcp_mesh_info_get(m, &mi);
     if (st == UMCP_OK) st = umcp_batch_add(batch, m, &j->it, j->step0, j->n_steps);
+    j->h2d = (double)mi.h2d_bytes;
     const std::string err = st == UMCP_OK ? std::string() : std::string(umcp_last_error());
     umcp_plan_destroy(j->plan);
     j->plan = nullptr;
@@ -199,6 +203,7 @@ void umcp_server::harvest(const std::vector<int64_t> &done, const std::vector<in
       errs[i] = umcp_last_error();
       fin[i].second = s;
     }
+    j->d2h = (double)((j->r.size() + j->energies.size()) * sizeof(double));
     umcp_mesh_destroy(j->mesh);  // leaves the batch
     j->mesh = nullptr;
   }
@@ -375,6 +380,8 @@ extern "C" umcp_status umcp_server_job(umcp_server *s, uint64_t id, umcp_job_inf
   info->t_admit = j->t_admit;
   info->t_done = j->t_done;
   info->device_bytes = (double)j->bytes;
+  info->h2d_bytes = j->h2d;
+  info->d2h_bytes = j->d2h;
   snprintf(info->message, sizeof(info->message), "%s", j->msg.c_str());
   return UMCP_OK;
 }

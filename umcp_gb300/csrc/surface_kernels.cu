@@ -97,6 +97,15 @@ __device__ __forceinline__ T point_data(const double *d64, const float *d32, siz
   else return d32[i];
 }
 
+// The moduli in the arithmetic type, converted once per launch (or per
+// tile) rather than per face: conversions from FP64 run on the narrow FP64 pipe.
+template <typename T>
+struct Moduli {
+  T kc, KA, kg, k_reg;
+  __device__ __forceinline__ explicit Moduli(const SurfaceParams &P)
+      : kc((T)P.kc), KA((T)P.KA), kg((T)P.kg), k_reg((T)P.k_reg) {}
+};
+
 // Global data of one face, loaded one face ahead (control-point indices two
 // ahead) so the loads are in flight while the previous face computes.
 template <typename T>
@@ -166,10 +175,10 @@ __device__ __forceinline__ void stage_basis(FaceSmem<T, NCP, NPT> &sm, const dou
 template <typename T, int NCP, int NPT>
 __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, int lane, unsigned hmask,
                                              const FaceAhead<T> &cur, const SurfaceParams &P, const T alpha[3],
-                                             const T ialpha[3], T dudv, bool reg_alpha, T *__restrict__ partial,
+                                             const T ialpha[3], const Moduli<T> &mod, T dudv, bool reg_alpha, T *__restrict__ partial,
                                              T e3[3], T da[3]) {
   constexpr int NC4 = FaceSmem<T, NCP, NPT>::NC4;
-  const T kc = (T)P.kc, KA = (T)P.KA, kg = (T)P.kg, k_reg = (T)P.k_reg;
+  const T kc = mod.kc, KA = mod.KA, kg = mod.kg, k_reg = mod.k_reg;
   // ---- 1. control points, relative to the patch corner
   T xl[3] = {0, 0, 0};
   if constexpr (sizeof(T) == 8) {
@@ -305,6 +314,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
   const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
   const T dudv = (T)L.dudv;
   const bool reg_alpha = L.irregular && P.k_reg != 0.0;
+  const Moduli<T> mod(P);
   const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
   HalfWarpSums<T> acc;
 
@@ -320,7 +330,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     load_ahead<T, NCP, NPT>(src, P, f + stride, end, cp_next, lane, nxt);
     cp_next = cp_after;
     T e3[3], da[3];
-    face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, dudv, reg_alpha, partial, e3, da);
+    face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, mod, dudv, reg_alpha, partial, e3, da);
     acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
     acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
     if (lane == 0 && !isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
@@ -596,6 +606,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
       const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
       const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
       const bool reg_alpha = irregular && P.k_reg != 0.0;
+      const Moduli<T> mod(P);
       const int end = tile.first + tile.count;
       int f = tile.first + hw;
       FaceAhead<T> cur, nxt;
@@ -606,8 +617,8 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
         load_ahead<T, NCP, NPT>(src, P, f + HW, end, cp_next, lane, nxt);
         cp_next = cp_after;
         T e3[3], da[3];
-        face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, dudv, reg_alpha, (T *)sj.partial, e3,
-                                  da);
+        face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, mod, dudv, reg_alpha, (T *)sj.partial,
+                                  e3, da);
         acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
         cur = nxt;
         __syncwarp(hmask);
