@@ -103,6 +103,11 @@ umcp_status umcp_plan_faces(const umcp_plan *plan, int kind, int *cp, int8_t *im
 umcp_status umcp_plan_basis(const umcp_plan *plan, int valence, double *rows, double *weight, double *u, double *v);
 /* Lipid types of the plan: c0[ntypes], apl[ntypes]. */
 umcp_status umcp_plan_lipids(const umcp_plan *plan, double *c0, double *apl);
+/* Limit-surface point at (u,v) of face `face` (regular faces first, then
+ * irregular, the reference's face numbering) as weights coef[n] of vertices
+ * ids[n] (surface::get_pt_coeffs, src/uv_map.C:14-195); n <= 13. */
+umcp_status umcp_plan_point_coeffs(const umcp_plan *plan, int face, double u, double v, int *ids, double *coef,
+                                   int *n);
 void umcp_plan_destroy(umcp_plan *plan);
 
 /* ---- device context and meshes --------------------------------------- */
@@ -172,6 +177,30 @@ umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *ctx, int pre
 /* Install M^-1 as a CSR matrix over vertices (SparseMatrix nzl/nzv rows,
  * src/sparse.h:4-53). */
 umcp_status umcp_mass_set(umcp_mesh *mesh, int nrow, const int *row_ptr, const int *col, const double *val);
+/* Build and install M^-1 from the limit surface (getSparseEffectiveMass,
+ * src/modes.C:1719-1990, with the mass points of src/hd.C:417-481): per face
+ * the (p+1)(p+2)/2 points (u,v) = (i/p, j/p), each carrying the mass per
+ * point of src/hd.C:442-452 (mass_scale x 760.09 g/mol per 65.35 A^2 of
+ * lipid, two leaflets, over surface::area's area0); M = sum_k m_k c_k c_k^T
+ * with c_k the limit-point weights of the control points (umcp_plan_point_coeffs);
+ * then the Cholesky inverse on the device (dense FP64, cuSOLVER potrf/potri
+ * as the reference's LAPACK dpotrf/dpotri), symmetrised, and entries with
+ * |M^-1_ij| <= rel_tol sqrt(|M^-1_ii M^-1_jj|) dropped (src/modes.C:1893).
+ * The plan must be the one the mesh was created from. */
+typedef struct {
+  double mass_scale;    /* MSCALE of src/hd.C:445 (5) */
+  int points_per_edge;  /* plim of src/hd.C:418 (10: 66 points per face) */
+  double rel_tol;       /* truncation tolerance (1e-20, src/modes.C:16) */
+} umcp_mass_opts;
+typedef struct {
+  double area0;         /* surface::area's area0 (src/interpLib.C:4413-4601) */
+  double mass_per_point;
+  long long points, nnz_mass, nnz_inverse;
+  int dense;            /* 1: M^-1 kept dense (fill >= 30%), 0: CSR */
+} umcp_mass_info;
+umcp_status umcp_mass_build(umcp_mesh *mesh, const umcp_plan *plan, const umcp_mass_opts *opts, umcp_mass_info *info);
+/* The installed M^-1 as a dense nv x nv row-major array. */
+umcp_status umcp_mass_get(umcp_mesh *mesh, double *dense);
 /* AltSparseCartMatVecIncrScale (src/parallel.C:1028-1075):
  * out[3i+c] += scale/alpha_c^2 * (scalev ? scalev[c*nrow+i] : 1) * sum_k val[k] in[3 col[k]+c]. */
 umcp_status umcp_mass_apply(umcp_mesh *mesh, const double *in, double *out, const double *scalev, double scale,

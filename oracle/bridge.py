@@ -187,6 +187,26 @@ def reference_dump(mesh: Path, params_txt: Path, positions: Path | None, prefix:
     return out
 
 
+MASS_POINT = np.dtype([("face", "i4"), ("n", "i4"), ("u", "f8"), ("v", "f8"), ("ids", "i4", 13), ("coef", "f8", 13)])
+
+
+def reference_mass(mesh: Path, params_txt: Path, prefix: Path, timeout: float = 600) -> dict:
+    """Runs the reference's own mass-point setup and effective-mass inverse
+    (ref_driver mass) and returns M^-1 (dense), the mass per point, area0 and
+    every mass point's limit-surface weights."""
+    cmd = [str(REF_DRIVER), "mass", str(mesh), str(params_txt), "-", str(prefix)]
+    subprocess.run(cmd, check=True, capture_output=True, timeout=timeout)
+    out = {}
+    for line in Path(f"{prefix}.mass.txt").read_text().splitlines():
+        k, v = line.split()
+        out[k] = float(v) if k in ("area0", "mass_per_pt") else int(v)
+    minv = np.fromfile(f"{prefix}.minv.bin", dtype=np.float64)
+    n = int(round(np.sqrt(minv.size)))
+    out["minv"] = minv.reshape(n, n)
+    out["points"] = np.fromfile(f"{prefix}.coef.bin", dtype=MASS_POINT)
+    return out
+
+
 def reference_time(mesh: Path, params_txt: Path, n_calls: int, timeout: float = 600) -> dict:
     import json
     res = subprocess.run([str(REF_DRIVER), "time", str(mesh), str(params_txt), "-", str(n_calls)], check=True,

@@ -14,6 +14,13 @@
  * Usage:
  *   ref_driver dump <mesh> <params> <positions.bin|-> <out_prefix>
  *   ref_driver time <mesh> <params> <positions.bin|-> <n_calls>
+ *   ref_driver mass <mesh> <params> - <out_prefix>
+ *
+ * "mass" sets up the mass points as hd.C does before a dynamics run
+ * (src/hd.C:417-481: a 66-point grid per triangle, mass per point from
+ * surface::area's area0), calls load_least_squares_fitting and
+ * getSparseEffectiveMass (src/hd.C:740-751), and dumps the inverse effective
+ * mass densely, the mass per point and the coefficients of every point.
  *
  * <params> holds "kc X", "KA X", "kg X", "k_reg X" lines and any
  * "lipid ..." lines (read by the reference's readLipidComposition).
@@ -28,6 +35,9 @@
 #include <sys/time.h>
 #include "interp.h"
 #include "parallel.h"
+#include "lagrange.h"
+#include "sparse.h"
+#include "units.h"
 
 extern double kc, KA, kg, k_reg;
 extern double VA, VC, VR, AVC;
@@ -135,6 +145,67 @@ int main(int argc, char **argv)
 	int nv = s->nv;
 	load_positions(argv[4], r, nv);
 	double *g = (double *)calloc(3 * nv + 3, sizeof(double));
+
+	if (!strcmp(argv[1], "mass")) {
+		const int plim = 10, ppf = (plim + 1) * (plim + 2) / 2;
+		force_set fs;
+		memset(&fs, 0, sizeof fs);
+		fs.npts = ppf * s->nt;
+		fs.face_set = (int *)malloc(sizeof(int) * fs.npts);
+		fs.uv_set = (double *)malloc(sizeof(double) * 2 * fs.npts);
+		fs.mass = (double *)malloc(sizeof(double) * fs.npts);
+		double cur_area = 0, area0 = 0;
+		s->area(r, -1, &cur_area, &area0);
+		const double mass_per_lipid = 5 * 1000 * 760.09 / 6.022e23 / 1000;
+		const double mass_per_pt = AMU_PER_KG * 2 * area0 / (s->nf_faces + s->nf_irr_faces) / ppf * mass_per_lipid / 65.35;
+		int p = 0;
+		for (int t = 0; t < s->nt; t++)
+			for (int fi = 0; fi <= plim; fi++)
+				for (int fj = 0; fj <= plim - fi; fj++, p++) {
+					fs.face_set[p] = s->theTriangles[t].f;
+					fs.uv_set[2 * p] = fi / (double)plim;
+					fs.uv_set[2 * p + 1] = fj / (double)plim;
+					fs.mass[p] = mass_per_pt;
+				}
+		s->load_least_squares_fitting(&fs);
+		/* serial vertex partition (what setupParallel gives one process) */
+		par_info.nv = (int *)malloc(sizeof(int));
+		par_info.verts = (int **)malloc(sizeof(int *));
+		par_info.nv[0] = nv;
+		par_info.verts[0] = (int *)malloc(sizeof(int) * nv);
+		for (int v = 0; v < nv; v++) par_info.verts[0][v] = v;
+		int *use = (int *)malloc(sizeof(int) * nv), nuse = 0;
+		SparseMatrix *M = NULL;
+		s->getSparseEffectiveMass(&fs, use, &nuse, &M, NULL, nv, NULL);
+		double *dense = (double *)calloc((size_t)nv * nv, sizeof(double));
+		for (int a = 0; a < M->nneed; a++)
+			for (int x = 0; x < M->nnz[a]; x++)
+				dense[(size_t)M->need_list[a] * nv + M->source_list[M->nzl[a][x]]] = M->nzv[a][x];
+		FILE *f = open_out(argv[5], "mass.txt", "w");
+		fprintf(f, "area0 %.17e\nmass_per_pt %.17e\nnpts %d\nnuse %d\nnt %d\n", area0, mass_per_pt, fs.npts, nuse, s->nt);
+		fclose(f);
+		f = open_out(argv[5], "minv.bin", "wb");
+		fwrite(dense, sizeof(double), (size_t)nv * nv, f);
+		fclose(f);
+		/* per point: face, u, v, ncoef, then 13 vertex ids and 13 coefficients (zero padded) */
+		f = open_out(argv[5], "coef.bin", "wb");
+		for (int q = 0; q < fs.npts; q++) {
+			int hdr[2] = {fs.face_set[q], fs.frc_ncoef[q]};
+			fwrite(hdr, sizeof(int), 2, f);
+			fwrite(&fs.uv_set[2 * q], sizeof(double), 2, f);
+			int ids[13] = {0};
+			double cf[13] = {0};
+			for (int c = 0; c < fs.frc_ncoef[q]; c++) {
+				ids[c] = fs.frc_coef_list[q * 13 + c];
+				cf[c] = fs.frc_coef[q * 13 + c];
+			}
+			fwrite(ids, sizeof(int), 13, f);
+			fwrite(cf, sizeof(double), 13, f);
+		}
+		fclose(f);
+		printf("mass_per_pt %.17e nuse %d\n", mass_per_pt, nuse);
+		return 0;
+	}
 
 	if (!strcmp(argv[1], "time")) {
 		int ncalls = atoi(argv[5]);

@@ -42,3 +42,15 @@ void dsytrf(char *u, int *n, double *a, int *lda, int *ipiv, double *w, int *lw,
 { scipy_dsytrf_(u, n, a, lda, ipiv, w, lw, info); }
 void dsytri(char *u, int *n, double *a, int *lda, int *ipiv, double *w, int *info)
 { scipy_dsytri_(u, n, a, lda, ipiv, w, info); }
+
+/* The underscored names, for reference units compiled with LAPACK_UNDERSCORE. */
+void dgemm_(char *ta, char *tb, int *m, int *n, int *k, double *al, double *a, int *lda, double *b, int *ldb,
+            double *be, double *c, int *ldc)
+{ scipy_dgemm_(ta, tb, m, n, k, al, a, lda, b, ldb, be, c, ldc); }
+void dsyev_(char *jobz, char *uplo, int *n, double *a, int *lda, double *w, double *work, int *lwork, int *info)
+{ scipy_dsyev_(jobz, uplo, n, a, lda, w, work, lwork, info); }
+void dgetrf_(int *m, int *n, double *a, int *lda, int *ipiv, int *info) { scipy_dgetrf_(m, n, a, lda, ipiv, info); }
+void dgetri_(int *n, double *a, int *lda, int *ipiv, double *work, int *lwork, int *info)
+{ scipy_dgetri_(n, a, lda, ipiv, work, lwork, info); }
+void dposv_(char *uplo, int *n, int *nrhs, double *a, int *lda, double *b, int *ldb, int *info)
+{ scipy_dposv_(uplo, n, nrhs, a, lda, b, ldb, info); }

@@ -27,7 +27,7 @@ def built_libraries():
 
 
 def golden_cases() -> list[str]:
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.endswith(".mass"))  # <case>.mass.npz: mass dumps
 
 
 def params_from_file(name: str, precision: int = 0):

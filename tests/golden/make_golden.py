@@ -8,6 +8,11 @@ Each case writes <name>.mesh (the input mesh, full-precision positions),
 <name>.params (the reference's input keywords) and <name>.npz with the
 reference's energy terms, gradient, evaluation positions, per-face energies
 and, for small meshes, its plan tables (control points, basis rows, g0).
+
+`--mass` writes <name>.mass.npz for the MASS_CASES instead, from the existing
+mesh and params files: the reference's inverse effective mass (dense), its
+mass per point and area0, and the limit-surface weights of the 66 mass
+points of four faces (two regular, two irregular where there are any).
 """
 from __future__ import annotations
 
@@ -105,10 +110,29 @@ def make_case(name, gen, params_txt, deform, keep_plan, work: Path) -> None:
     print(f"{name}: nv={plan.nv} E={ref['E']:.12g}")
 
 
+MASS_CASES = ["ico2_plain", "planar12_deformed"]
+
+
+def make_mass_case(name: str, work: Path) -> None:
+    ref = B.reference_mass(HERE / f"{name}.mesh", HERE / f"{name}.params", work / name)
+    pts = ref["points"]
+    nreg = int(np.load(HERE / f"{name}.npz")["nf_faces"])
+    faces = [0, 1] + ([nreg, nreg + 1] if pts["face"].max() >= nreg else [])
+    keep = pts[np.isin(pts["face"], faces)]
+    np.savez_compressed(HERE / f"{name}.mass.npz", minv=ref["minv"], mass_per_pt=ref["mass_per_pt"],
+                        area0=ref["area0"], npts=ref["npts"], pt_face=keep["face"], pt_n=keep["n"], pt_u=keep["u"],
+                        pt_v=keep["v"], pt_ids=keep["ids"], pt_coef=keep["coef"])
+    print(f"{name}: mass per point {ref['mass_per_pt']:.12g}, {len(keep)} points kept")
+
+
 def main() -> None:
     if not B.reference_available():
         raise SystemExit("reference-built oracle missing; build it with __graft_entry__.build() where the reference exists")
     with tempfile.TemporaryDirectory() as td:
+        if "--mass" in sys.argv:
+            for name in MASS_CASES:
+                make_mass_case(name, Path(td))
+            return
         for case in CASES:
             make_case(*case, Path(td))
 

@@ -87,6 +87,17 @@ class BatchInfo(C.Structure):
     ]
 
 
+class MassOpts(C.Structure):
+    _fields_ = [("mass_scale", C.c_double), ("points_per_edge", C.c_int), ("rel_tol", C.c_double)]
+
+
+class MassInfo(C.Structure):
+    _fields_ = [
+        ("area0", C.c_double), ("mass_per_point", C.c_double), ("points", C.c_longlong),
+        ("nnz_mass", C.c_longlong), ("nnz_inverse", C.c_longlong), ("dense", C.c_int),
+    ]
+
+
 class ServerOpts(C.Structure):
     _fields_ = [
         ("precision", C.c_int), ("hbm_budget_bytes", C.c_double), ("max_jobs", C.c_int), ("chunk_ms", C.c_double),
@@ -167,6 +178,9 @@ _SIGNATURES = {
     "umcp_run_async": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int],
     "umcp_step_host": [_VP, C.POINTER(Integrator), C.c_uint64, _D, _D, _D],
     "umcp_mesh_energies": [_VP, _D, C.c_int64],
+    "umcp_mass_build": [_VP, _VP, C.POINTER(MassOpts), C.POINTER(MassInfo)],
+    "umcp_mass_get": [_VP, _D],
+    "umcp_plan_point_coeffs": [_VP, C.c_int, C.c_double, C.c_double, _I, _D, _I],
     "umcp_batch_create": [_VP, C.c_int, C.POINTER(BatchOpts), C.POINTER(_VP)],
     "umcp_batch_destroy": [_VP],
     "umcp_batch_add": [_VP, _VP, C.POINTER(Integrator), C.c_uint64, C.c_int64],
@@ -288,6 +302,14 @@ class Plan:
         b = C.c_size_t()
         _check(library().umcp_plan_device_bytes(self._h, ctx.handle, precision, n_energies, C.byref(b)))
         return b.value
+
+    def point_coeffs(self, face: int, u: float, v: float) -> tuple[np.ndarray, np.ndarray]:
+        """Limit-surface point (u,v) of a face as (vertex ids, weights)."""
+        ids = np.zeros(13, dtype=np.int32)
+        coef = np.zeros(13)
+        n = C.c_int()
+        _check(library().umcp_plan_point_coeffs(self._h, face, u, v, _ip(ids), _dp(coef), C.byref(n)))
+        return ids[:n.value], coef[:n.value]
 
     def positions(self) -> np.ndarray:
         r = np.zeros(3 * self.nv + 3)
@@ -457,6 +479,19 @@ class Mesh:
         E = C.c_double()
         _check(library().umcp_step_host(self._h, C.byref(it), step, _dp(r), _dp(p), C.byref(E)))
         return E.value
+
+    def mass_build(self, plan: "Plan", mass_scale: float = 5.0, points_per_edge: int = 10,
+                   rel_tol: float = 1e-20) -> MassInfo:
+        """Builds and installs M^-1 from the limit surface (umcp_mass_build)."""
+        info = MassInfo()
+        opts = MassOpts(mass_scale, points_per_edge, rel_tol)
+        _check(library().umcp_mass_build(self._h, plan.handle, C.byref(opts), C.byref(info)))
+        return info
+
+    def mass_get(self) -> np.ndarray:
+        out = np.zeros((self.nv, self.nv))
+        _check(library().umcp_mass_get(self._h, _dp(out)))
+        return out
 
     def energies(self, n: int) -> np.ndarray:
         """The first n energies recorded by the latest run or batch job."""

@@ -76,7 +76,7 @@ def build_engine(verbose: bool = False) -> Path:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
     if jobs or _stale(ENGINE_LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(ENGINE_LIB)] + [str(o) for o in objs])
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(ENGINE_LIB)] + [str(o) for o in objs] + ["-ldl"])
     if verbose:
         print(f"built {ENGINE_LIB}")
     return ENGINE_LIB

@@ -134,6 +134,23 @@ extern "C" umcp_status umcp_plan_from_file(const char *mesh_path, const umcp_par
   return UMCP_OK;
 }
 
+const Plan &umcp::plan_of(const umcp_plan *p) { return p->plan; }
+
+extern "C" umcp_status umcp_plan_point_coeffs(const umcp_plan *plan, int face, double u, double v, int *ids,
+                                              double *coef, int *n) {
+  if (!plan || !ids || !coef || !n) return fail(UMCP_ERR_INVALID, "null argument");
+  const Plan &P = plan->plan;
+  const int nreg = (int)P.reg_faces.size(), nirr = (int)P.irr_faces.size();
+  if (face < 0 || face >= nreg + nirr) return fail(UMCP_ERR_INVALID, "face index out of range");
+  if (!(u >= -1e-4 && v >= -1e-4 && u + v <= 1.0 + 1e-4)) return fail(UMCP_ERR_INVALID, "(u,v) outside the face");
+  const Face &F = face < nreg ? P.reg_faces[face] : P.irr_faces[face - nreg];
+  IrregularMap m5(5), m7(7);
+  IrregularMap *maps[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, &m5, nullptr, &m7};
+  *n = limit_point_coeffs(F, u, v, maps, coef);
+  for (int x = 0; x < *n; ++x) ids[x] = F.cp[x];
+  return UMCP_OK;
+}
+
 extern "C" umcp_status umcp_plan_set_reference(umcp_plan *plan, const double *r) {
   if (!plan || !r) return fail(UMCP_ERR_INVALID, "null argument");
   set_reference_state(plan->mesh, r, &plan->plan);
@@ -635,6 +652,8 @@ extern "C" umcp_status umcp_mass_set(umcp_mesh *m, int nrow, const int *row_ptr,
   UMCP_CUDA(upload(m->mrow, std::vector<int>(row_ptr, row_ptr + nrow + 1)));
   UMCP_CUDA(upload(m->mcol, std::vector<int>(col, col + nnz)));
   UMCP_CUDA(upload(m->mval, std::vector<double>(val, val + nnz)));
+  UMCP_CUDA(m->mdense.alloc(0));
+  m->mass_dense = false;
   m->mrows = nrow;
   m->drop_graphs();
   return UMCP_OK;
@@ -648,8 +667,7 @@ extern "C" umcp_status umcp_mass_apply_device(umcp_mesh *m, const double *d_in, 
   double a[3] = {1, 1, 1};
   if (alphas) { a[0] = alphas[0]; a[1] = alphas[1]; a[2] = alphas[2]; }
   UMCP_CUDA(cudaMemcpyAsync(m->alphas.p, a, sizeof a, cudaMemcpyHostToDevice, m->ctx->stream));
-  UMCP_CUDA(launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), d_scalev, scale,
-                        m->alphas.as<double>(), d_in, d_out, 1, m->ctx->stream));
+  UMCP_CUDA(queue_mass_apply(m, d_scalev, scale, m->alphas.as<double>(), d_in, d_out, 1, m->ctx->stream));
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
   return UMCP_OK;
 }
@@ -673,9 +691,8 @@ extern "C" umcp_status umcp_mass_apply(umcp_mesh *m, const double *in, double *o
   double a[3] = {1, 1, 1};
   if (alphas) { a[0] = alphas[0]; a[1] = alphas[1]; a[2] = alphas[2]; }
   UMCP_CUDA(cudaMemcpyAsync(m->alphas.p, a, sizeof a, cudaMemcpyHostToDevice, s));
-  UMCP_CUDA(launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(),
-                        scalev ? dsc.as<double>() : nullptr, scale, m->alphas.as<double>(), din.as<double>(),
-                        dout.as<double>(), 1, s));
+  UMCP_CUDA(queue_mass_apply(m, scalev ? dsc.as<double>() : nullptr, scale, m->alphas.as<double>(),
+                             din.as<double>(), dout.as<double>(), 1, s));
   UMCP_CUDA(cudaMemcpyAsync(out, dout.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   UMCP_CUDA(cudaStreamSynchronize(s));
   return UMCP_OK;
@@ -759,8 +776,7 @@ static cudaError_t queue_step_t(umcp_mesh *m, const StepArgs &a, int use_mass, d
   if (e == cudaSuccess)
     e = launch_kick(m->nv, a, m->cnt.as<uint64_t>(), m->p.as<double>(), m->g.as<double>(), m->status.as<int>(), s);
   if (e == cudaSuccess)
-    e = launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), nullptr, 1.0, nullptr,
-                    m->p.as<double>(), m->qdot.as<double>(), 0, s);
+    e = queue_mass_apply(m, nullptr, 1.0, nullptr, m->p.as<double>(), m->qdot.as<double>(), 0, s);
   if (e == cudaSuccess)
     e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->rhi.as<float>(),
                      m->rlo.as<float>(), m->status.as<int>(), s);

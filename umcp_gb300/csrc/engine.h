@@ -82,9 +82,10 @@ struct umcp_mesh {
   double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
   double *h_stage2 = nullptr; // pinned, 3*nv doubles
   uint64_t *h_cnt = nullptr;  // pinned, 2 counters
-  // effective inverse mass
+  // effective inverse mass: CSR (mrow, mcol, mval) or dense row-major (mdense)
   int mrows = 0;
-  umcp::DevBuf mrow, mcol, mval, alphas;
+  umcp::DevBuf mrow, mcol, mval, alphas, mdense;
+  bool mass_dense = false;
   // captured step sequences, by length (1 and kGraphChunk steps)
   struct CachedGraph {
     cudaGraphExec_t exec = nullptr;
@@ -108,7 +109,7 @@ struct umcp_mesh {
                                     &G->rr0f, &G->compf})
         b += x->bytes;
     for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
-                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas})
+                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense})
       b += x->bytes;
     return b;
   }
@@ -122,6 +123,15 @@ struct umcp_mesh {
 };
 
 namespace umcp {
+
+struct Plan;
+// Host-side plan of a umcp_plan.
+const Plan &plan_of(const umcp_plan *p);
+
+// out (+)= M^-1 in with the installed inverse mass, dense or CSR (see launch_spmv
+// for the scaling arguments).
+cudaError_t queue_mass_apply(umcp_mesh *m, const double *scalev, double scale, const double *alphas,
+                             const double *in, double *out, int accumulate, cudaStream_t s);
 
 // Integrator settings of a run on mesh m (validates it).
 umcp_status make_step_args(const umcp_mesh *m, const umcp_integrator *it, StepArgs *a);

@@ -1,0 +1,285 @@
+// The limit-surface effective mass and its inverse on the device
+// (getSparseEffectiveMass, src/modes.C:1719-1990), and the M^-1 apply.
+//
+// M is assembled on the host from the mass points (plan.cpp
+// build_effective_mass), expanded to a dense FP64 matrix on the device,
+// factorised and inverted there (Cholesky: potrf + potri, as the reference
+// does with LAPACK), symmetrised and truncated at the reference's relative
+// tolerance (|M^-1_ij| / sqrt(|M^-1_ii M^-1_jj|) > rel_tol, src/modes.C:1893).
+// The reference's tolerance of 1e-20 keeps every entry, so M^-1 stays dense
+// and the apply is a dense FP64 matrix times the three Cartesian components;
+// a looser tolerance that leaves it sparse (under 30% fill) stores CSR.
+//
+// The factorisation uses cuSOLVER's dense Cholesky routines, loaded at run
+// time so the engine does not depend on the library where no mass matrix is
+// built.
+#include <dlfcn.h>
+#include <string.h>
+
+#include <cmath>
+#include <vector>
+
+#include "engine.h"
+#include "plan.h"
+
+using namespace umcp;
+
+namespace {
+
+// The dense Cholesky entry points of cuSOLVER, by their C ABI: the handle is
+// an opaque pointer, status and fill-mode enums are ints (0 = success,
+// 0 = lower triangle).
+constexpr int kFillLower = 0;
+struct Solver {
+  using create_t = int (*)(void **);
+  using destroy_t = int (*)(void *);
+  using stream_t = int (*)(void *, cudaStream_t);
+  using size_t_ = int (*)(void *, int, int, double *, int, int *);
+  using run_t = int (*)(void *, int, int, double *, int, double *, int, int *);
+  void *lib = nullptr;
+  create_t create = nullptr;
+  destroy_t destroy = nullptr;
+  stream_t set_stream = nullptr;
+  size_t_ potrf_size = nullptr, potri_size = nullptr;
+  run_t potrf = nullptr, potri = nullptr;
+  bool ok() const { return potri != nullptr; }
+};
+
+const Solver &solver() {
+  static Solver s = [] {
+    Solver x;
+    for (const char *name : {"libcusolver.so.12", "libcusolver.so.13", "libcusolver.so.11", "libcusolver.so"}) {
+      x.lib = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+      if (x.lib) break;
+    }
+    if (!x.lib) return x;
+    x.create = (Solver::create_t)dlsym(x.lib, "cusolverDnCreate");
+    x.destroy = (Solver::destroy_t)dlsym(x.lib, "cusolverDnDestroy");
+    x.set_stream = (Solver::stream_t)dlsym(x.lib, "cusolverDnSetStream");
+    x.potrf_size = (Solver::size_t_)dlsym(x.lib, "cusolverDnDpotrf_bufferSize");
+    x.potrf = (Solver::run_t)dlsym(x.lib, "cusolverDnDpotrf");
+    x.potri_size = (Solver::size_t_)dlsym(x.lib, "cusolverDnDpotri_bufferSize");
+    x.potri = (Solver::run_t)dlsym(x.lib, "cusolverDnDpotri");
+    if (!x.create || !x.destroy || !x.set_stream || !x.potrf_size || !x.potrf || !x.potri_size) x.potri = nullptr;
+    return x;
+  }();
+  return s;
+}
+
+__global__ void csr_to_dense_kernel(int n, const int *__restrict__ row_ptr, const int *__restrict__ col,
+                                    const double *__restrict__ val, double *__restrict__ A) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) A[(size_t)i * n + col[k]] = val[k];
+}
+
+// potri with the lower triangle (column-major) leaves the inverse in the
+// row-major upper triangle; mirror it below the diagonal.
+__global__ void symmetrize_kernel(int n, double *__restrict__ A) {
+  const size_t total = (size_t)n * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (i > j) A[e] = A[(size_t)j * n + i];
+  }
+}
+
+// Drops entries at or below rel_tol of the geometric mean of their diagonal
+// entries; counts those kept (integer atomics: the count is exact).
+__global__ void truncate_kernel(int n, double rel_tol, double *__restrict__ A, unsigned long long *__restrict__ kept) {
+  const size_t total = (size_t)n * n;
+  unsigned long long k = 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    const double a = A[e];
+    const double d = sqrt(fabs(A[(size_t)i * n + i] * A[(size_t)j * n + j]));
+    if (fabs(a) / d > rel_tol) ++k;
+    else A[e] = 0.0;
+  }
+  for (int off = 16; off >= 1; off >>= 1) k += __shfl_xor_sync(0xffffffffu, k, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(kept, k);
+}
+
+// out[3i+c] (+)= scale/alpha_c^2 * (scalev ? scalev[c*n+i] : 1) * sum_j A[i][j] in[3j+c].
+// One block per row (grid-stride), fixed-order block reduction.
+__global__ void dense_apply_kernel(int n, const double *__restrict__ A, const double *__restrict__ scalev, double scale,
+                                   const double *__restrict__ alphas, const double *__restrict__ in,
+                                   double *__restrict__ out, int accumulate) {
+  __shared__ double red[3][8];
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const double *row = A + (size_t)i * n;
+    double a0 = 0, a1 = 0, a2 = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const double m = row[j];
+      a0 += m * in[3 * (size_t)j];
+      a1 += m * in[3 * (size_t)j + 1];
+      a2 += m * in[3 * (size_t)j + 2];
+    }
+    for (int off = 16; off >= 1; off >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red[0][w] = a0; red[1][w] = a1; red[2][w] = a2; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      const int c = threadIdx.x;
+      double s = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[c][k];
+      const double al = alphas ? alphas[c] : 1.0;
+      double f = scale / (al * al);
+      if (scalev) f *= scalev[(size_t)c * n + i];
+      const double v = f * s;
+      out[3 * (size_t)i + c] = accumulate ? out[3 * (size_t)i + c] + v : v;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double scale, const double *alphas,
+                                   const double *in, double *out, int accumulate, cudaStream_t s) {
+  if (m->mass_dense) {
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
+    const int grid = m->mrows < sms * 8 ? m->mrows : sms * 8;
+    dense_apply_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<double>(), scalev, scale, alphas, in, out,
+                                            accumulate);
+    return cudaGetLastError();
+  }
+  return launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), scalev, scale, alphas, in,
+                     out, accumulate, s);
+}
+
+static umcp_status fail(umcp_status s, const std::string &msg) { return umcp::set_error(s, msg); }
+
+extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, const umcp_mass_opts *opts,
+                                       umcp_mass_info *info) {
+  if (!m || !plan) return fail(UMCP_ERR_INVALID, "null argument");
+  umcp_mass_opts o{5.0, 10, 1e-20};
+  if (opts) o = *opts;
+  if (!(o.mass_scale > 0) || o.points_per_edge < 1 || !(o.rel_tol >= 0))
+    return fail(UMCP_ERR_INVALID, "mass options: mass_scale > 0, points_per_edge >= 1, rel_tol >= 0");
+  const Plan &P = plan_of(plan);
+  const int n = m->nv;
+  if ((int)(P.reg_faces.size() + P.irr_faces.size()) != m->nfaces) return fail(UMCP_ERR_INVALID, "plan does not match the mesh");
+  const Solver &S = solver();
+  if (!S.ok()) return fail(UMCP_ERR_UNSUPPORTED, "cuSOLVER (dense Cholesky) is not available on this host");
+
+  EffectiveMass EM;
+  build_effective_mass(P, n, o.mass_scale, o.points_per_edge, &EM);
+
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t s = m->ctx->stream;
+  UMCP_CUDA(cudaStreamSynchronize(s));  // queued steps may still read the previous M^-1
+  m->drop_graphs();
+  DevBuf A, drow, dcol, dval, work, dinfo, dkept;
+  UMCP_CUDA(A.alloc((size_t)n * n * sizeof(double)));
+  UMCP_CUDA(cudaMemsetAsync(A.p, 0, A.bytes, s));
+  UMCP_CUDA(upload(drow, EM.row_ptr));
+  UMCP_CUDA(upload(dcol, EM.col));
+  UMCP_CUDA(upload(dval, EM.val));
+  csr_to_dense_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, drow.as<int>(), dcol.as<int>(), dval.as<double>(),
+                                                      A.as<double>());
+  UMCP_CUDA(cudaGetLastError());
+
+  void *h = nullptr;
+  if (S.create(&h) != 0) return fail(UMCP_ERR_CUDA, "cusolverDnCreate failed");
+  struct Guard { const Solver &S; void *h; ~Guard() { S.destroy(h); } } guard{S, h};
+  S.set_stream(h, s);
+  int lw1 = 0, lw2 = 0;
+  if (S.potrf_size(h, kFillLower, n, A.as<double>(), n, &lw1) != 0 ||
+      S.potri_size(h, kFillLower, n, A.as<double>(), n, &lw2) != 0)
+    return fail(UMCP_ERR_CUDA, "cuSOLVER workspace query failed");
+  UMCP_CUDA(work.alloc((size_t)std::max(std::max(lw1, lw2), 1) * sizeof(double)));
+  UMCP_CUDA(dinfo.alloc(sizeof(int)));
+  int hinfo = 0;
+  if (S.potrf(h, kFillLower, n, A.as<double>(), n, work.as<double>(), lw1, dinfo.as<int>()) !=
+      0)
+    return fail(UMCP_ERR_CUDA, "cusolverDnDpotrf failed");
+  UMCP_CUDA(cudaMemcpyAsync(&hinfo, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaStreamSynchronize(s));
+  if (hinfo != 0)
+    return fail(UMCP_ERR_INVALID, "effective mass matrix is not positive definite (the reference stops here, "
+                                  "src/modes.C:1833-1837)");
+  if (S.potri(h, kFillLower, n, A.as<double>(), n, work.as<double>(), lw2, dinfo.as<int>()) !=
+      0)
+    return fail(UMCP_ERR_CUDA, "cusolverDnDpotri failed");
+  UMCP_CUDA(cudaMemcpyAsync(&hinfo, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaStreamSynchronize(s));
+  if (hinfo != 0) return fail(UMCP_ERR_INVALID, "effective mass matrix could not be inverted");
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
+  symmetrize_kernel<<<sms * 8, 256, 0, s>>>(n, A.as<double>());
+  UMCP_CUDA(cudaGetLastError());
+  UMCP_CUDA(dkept.alloc(sizeof(unsigned long long)));
+  UMCP_CUDA(cudaMemsetAsync(dkept.p, 0, sizeof(unsigned long long), s));
+  truncate_kernel<<<sms * 8, 256, 0, s>>>(n, o.rel_tol, A.as<double>(), dkept.as<unsigned long long>());
+  UMCP_CUDA(cudaGetLastError());
+  unsigned long long kept = 0;
+  UMCP_CUDA(cudaMemcpyAsync(&kept, dkept.p, sizeof kept, cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaStreamSynchronize(s));
+
+  const double fill = (double)kept / ((double)n * n);
+  if (fill >= 0.3) {
+    std::swap(m->mdense.p, A.p);
+    std::swap(m->mdense.bytes, A.bytes);
+    m->mass_dense = true;
+    UMCP_CUDA(m->mrow.alloc(0));
+    UMCP_CUDA(m->mcol.alloc(0));
+    UMCP_CUDA(m->mval.alloc(0));
+  } else {
+    std::vector<double> h_a((size_t)n * n);
+    UMCP_CUDA(cudaMemcpy(h_a.data(), A.p, A.bytes, cudaMemcpyDeviceToHost));
+    std::vector<int> rp((size_t)n + 1, 0), cl;
+    std::vector<double> vl;
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j)
+        if (h_a[(size_t)i * n + j] != 0.0) {
+          cl.push_back(j);
+          vl.push_back(h_a[(size_t)i * n + j]);
+        }
+      rp[(size_t)i + 1] = (int)cl.size();
+    }
+    UMCP_CUDA(upload(m->mrow, rp));
+    UMCP_CUDA(upload(m->mcol, cl));
+    UMCP_CUDA(upload(m->mval, vl));
+    UMCP_CUDA(m->mdense.alloc(0));
+    m->mass_dense = false;
+  }
+  m->mrows = n;
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->area0 = EM.area0;
+    info->mass_per_point = EM.mass_per_point;
+    info->points = EM.points;
+    info->nnz_mass = (long long)EM.val.size();
+    info->nnz_inverse = (long long)kept;
+    info->dense = m->mass_dense ? 1 : 0;
+  }
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_mass_get(umcp_mesh *m, double *dense) {
+  if (!m || !dense) return fail(UMCP_ERR_INVALID, "null argument");
+  if (!m->mrows) return fail(UMCP_ERR_INVALID, "no mass matrix installed");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  const int n = m->mrows;
+  if (m->mass_dense) {
+    UMCP_CUDA(cudaMemcpy(dense, m->mdense.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost));
+    return UMCP_OK;
+  }
+  std::vector<int> rp((size_t)n + 1);
+  UMCP_CUDA(cudaMemcpy(rp.data(), m->mrow.p, rp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> cl((size_t)rp[n]);
+  std::vector<double> vl((size_t)rp[n]);
+  if (rp[n] > 0) {
+    UMCP_CUDA(cudaMemcpy(cl.data(), m->mcol.p, cl.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    UMCP_CUDA(cudaMemcpy(vl.data(), m->mval.p, vl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  memset(dense, 0, (size_t)n * n * sizeof(double));
+  for (int i = 0; i < n; ++i)
+    for (int k = rp[i]; k < rp[(size_t)i + 1]; ++k) dense[(size_t)i * n + cl[k]] += vl[k];
+  return UMCP_OK;
+}

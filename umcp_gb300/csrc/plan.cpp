@@ -283,10 +283,70 @@ static std::vector<double> subdivision_matrix(int val) {
   return A;
 }
 
+IrregularMap::IrregularMap(int val) : val_(val), n_(val + 6), atot_(subdivision_matrix(val)) {
+  powers_.assign(1, std::vector<double>((size_t)n_ * n_, 0.0));
+  for (int i = 0; i < n_; ++i) powers_[0][(size_t)i * n_ + i] = 1.0;
+}
+
+// Powers of the square block A (the first val+6 rows of Atot), A^0 = I.
+const std::vector<double> &IrregularMap::power(int e) {
+  const int N = n_;
+  while ((int)powers_.size() <= e) {
+    const std::vector<double> &P = powers_.back();
+    std::vector<double> Q((size_t)N * N, 0.0);
+    for (int i = 0; i < N; ++i)
+      for (int l = 0; l < N; ++l) {
+        double a = atot_[(size_t)i * N + l];
+        if (a == 0.0) continue;
+        for (int j = 0; j < N; ++j) Q[(size_t)i * N + j] += a * P[(size_t)l * N + j];
+      }
+    powers_.push_back(Q);
+  }
+  return powers_[e];
+}
+
+void IrregularMap::at(double *u, double *v, double *scale_out, double cmap[12][kMaxCp]) {
+  const int val = val_, N = n_;
+  double fu = *u, fv = *v;
+  // Sub-triangle selection in the domain ring containing (fu,fv)
+  // (src/interpLib.C:5648-5730, src/irr_kernel.C:474-541).
+  double f_domain = -std::log10(fu + fv) / std::log10(2.0);
+  if (fu + fv >= 1.0 - 1e-9) f_domain = 1;
+  const int domain = (int)std::lround(std::ceil(f_domain));
+  const double pow2 = std::pow(2.0, domain - 1.0);
+  double scale = pow2;
+  fu *= pow2;
+  fv *= pow2;
+  int pc[12];
+  if (fu > 0.5) {
+    fv = 2 * fv; fu = 2.0 * fu - 1.0; scale *= 2;
+    int c[12] = {2, val + 3, val + 4, val + 5, 3, 0, 1, val + 2, val + 8, val + 9, val + 10, val + 11};
+    std::memcpy(pc, c, sizeof pc);
+  } else if (fv > 0.5) {
+    fu = 2 * fu; fv = 2.0 * fv - 1.0; scale *= 2;
+    int c[12] = {1, val + 2, val + 3, 2, 0, val, val + 1, val + 6, val + 7, val + 8, val + 9, val + 4};
+    std::memcpy(pc, c, sizeof pc);
+  } else {
+    fv = 1 - 2 * fv; fu = 1 - 2 * fu; scale *= -2;
+    int c[12] = {val + 3, 2, 1, val + 2, val + 8, val + 9, val + 4, val + 5, 3, 0, val, val + 1};
+    std::memcpy(pc, c, sizeof pc);
+  }
+  const std::vector<double> &Ap = power(domain - 1);
+  // cmap[y][x] = (Atot * A^(domain-1))[pc[y]][x]
+  for (int y = 0; y < 12; ++y)
+    for (int x = 0; x < N; ++x) {
+      double s = 0.0;
+      for (int l = 0; l < N; ++l) s += atot_[(size_t)pc[y] * N + l] * Ap[(size_t)l * N + x];
+      cmap[y][x] = s;
+    }
+  *u = fu;
+  *v = fv;
+  *scale_out = scale;
+}
+
 std::string build_irregular_basis(int val, PatchBasis *b) {
   if (val != 5 && val != 7) return "irregular valence must be 5 or 7";
-  const int N = val + 6, R = val + 12;
-  const std::vector<double> Atot = subdivision_matrix(val);
+  const int N = val + 6;
   const double k = irregular_k(val);
   b->valence = val;
   b->ncp = N;
@@ -295,24 +355,7 @@ std::string build_irregular_basis(int val, PatchBasis *b) {
   b->weight.assign(kIrrPts, 0.0);
   b->u.assign(kIrrPts, 0.0);
   b->v.assign(kIrrPts, 0.0);
-
-  // Powers of the square block A (first N rows of Atot), A^0 = I.
-  std::vector<std::vector<double>> powers(1, std::vector<double>((size_t)N * N, 0.0));
-  for (int i = 0; i < N; ++i) powers[0][(size_t)i * N + i] = 1.0;
-  auto power = [&](int e) -> const std::vector<double> & {
-    while ((int)powers.size() <= e) {
-      const std::vector<double> &P = powers.back();
-      std::vector<double> Q((size_t)N * N, 0.0);
-      for (int i = 0; i < N; ++i)
-        for (int l = 0; l < N; ++l) {
-          double a = Atot[(size_t)i * N + l];
-          if (a == 0.0) continue;
-          for (int j = 0; j < N; ++j) Q[(size_t)i * N + j] += a * P[(size_t)l * N + j];
-        }
-      powers.push_back(Q);
-    }
-    return powers[e];
-  };
+  IrregularMap map(val);
 
   const int n = 4;
   double vx[n], vw[n];
@@ -331,39 +374,8 @@ std::string build_irregular_basis(int val, PatchBasis *b) {
       b->weight[pt] = v_weight * u_weight;
       b->u[pt] = fu;
       b->v[pt] = fv;
-      // Sub-triangle selection in the domain ring containing (fu,fv)
-      // (src/interpLib.C:5648-5730).
-      double f_domain = -std::log10(fu + fv) / std::log10(2.0);
-      if (fu + fv >= 1.0 - 1e-9) f_domain = 1;
-      const int domain = (int)std::lround(std::ceil(f_domain));
-      const double pow2 = std::pow(2.0, domain - 1.0);
-      double scale = pow2;
-      fu *= pow2;
-      fv *= pow2;
-      int pc[12];
-      if (fu > 0.5) {
-        fv = 2 * fv; fu = 2.0 * fu - 1.0; scale *= 2;
-        int c[12] = {2, val + 3, val + 4, val + 5, 3, 0, 1, val + 2, val + 8, val + 9, val + 10, val + 11};
-        std::memcpy(pc, c, sizeof pc);
-      } else if (fv > 0.5) {
-        fu = 2 * fu; fv = 2.0 * fv - 1.0; scale *= 2;
-        int c[12] = {1, val + 2, val + 3, 2, 0, val, val + 1, val + 6, val + 7, val + 8, val + 9, val + 4};
-        std::memcpy(pc, c, sizeof pc);
-      } else {
-        fv = 1 - 2 * fv; fu = 1 - 2 * fu; scale *= -2;
-        int c[12] = {val + 3, 2, 1, val + 2, val + 8, val + 9, val + 4, val + 5, 3, 0, val, val + 1};
-        std::memcpy(pc, c, sizeof pc);
-      }
-      const std::vector<double> &Ap = power(domain - 1);
-      // coord_map[y][x] = (Atot * A^(domain-1))[pc[y]][x]
-      double cmap[12][kMaxCp];
-      for (int y = 0; y < 12; ++y)
-        for (int x = 0; x < N; ++x) {
-          double s = 0.0;
-          for (int l = 0; l < N; ++l) s += Atot[(size_t)pc[y] * N + l] * Ap[(size_t)l * N + x];
-          cmap[y][x] = s;
-        }
-      (void)R;
+      double scale, cmap[12][kMaxCp];
+      map.at(&fu, &fv, &scale, cmap);
       double sp[kKinds][12];
       box_spline_rows(fu, fv, sp);
       const double ks[kKinds] = {1.0, scale, scale, scale * scale, scale * scale, scale * scale};
@@ -376,6 +388,94 @@ std::string build_irregular_basis(int val, PatchBasis *b) {
     }
   }
   return "";
+}
+
+// ------------------------------------------------------------ limit points
+
+int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8], double *coef) {
+  const int N = f.ncp;
+  for (int x = 0; x < N; ++x) coef[x] = 0.0;
+  if (f.valence == 6) {
+    double sp[kKinds][12];
+    box_spline_rows(u, v, sp);
+    for (int x = 0; x < 12; ++x) coef[x] = sp[0][x];
+    return N;
+  }
+  if (!(std::isfinite(-std::log10(u + v))) && u < 1e-10 && v < 1e-10) {
+    // The extraordinary vertex itself: half the vertex plus half the mean of
+    // its ring (src/uv_map.C:32-61); the ring is control points 1..val.
+    coef[0] = 0.5;
+    for (int e = 1; e <= f.valence; ++e) coef[e] = 1.0 / (2.0 * f.valence);
+    return N;
+  }
+  double fu = u, fv = v, scale, cmap[12][kMaxCp];
+  maps[f.valence]->at(&fu, &fv, &scale, cmap);
+  double sp[kKinds][12];
+  box_spline_rows(fu, fv, sp);
+  for (int x = 0; x < N; ++x) {
+    double s = 0.0;
+    for (int y = 0; y < 12; ++y) s += cmap[y][x] * sp[0][y];
+    coef[x] = s;
+  }
+  return N;
+}
+
+void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, EffectiveMass *out) {
+  // Mass per point (src/hd.C:442-452): a lipid mass of 760.09 g/mol (POPC)
+  // times mass_scale, spread over area0 at 65.35 A^2 per lipid and two
+  // leaflets. area0 is surface::area's: 0.5 g0 w over the regular faces'
+  // points plus g0 w over the irregular ones' (src/interpLib.C:4413-4601).
+  double area0 = 0.0;
+  for (size_t f = 0; f < p.reg_faces.size(); ++f)
+    for (int q = 0; q < kRegPts; ++q) area0 += 0.5 * p.reg_g0[f * kRegPts + q] * p.regular.weight[q];
+  for (size_t f = 0; f < p.irr_faces.size(); ++f)
+    for (int q = 0; q < kIrrPts; ++q)
+      area0 += p.irr_g0[f * kIrrPts + q] * p.irregular[p.irr_faces[f].valence].weight[q];
+  const int ppf = (plim + 1) * (plim + 2) / 2;
+  const double amu_per_kg = 1.0 / 1.661e-27;
+  const double mass_per_lipid = mass_scale * 1000 * 760.09 / 6.022e23 / 1000;
+  const size_t nfaces = p.reg_faces.size() + p.irr_faces.size();
+  const double m = amu_per_kg * 2 * area0 / (double)nfaces / ppf * mass_per_lipid / 65.35;
+  out->area0 = area0;
+  out->mass_per_point = m;
+  out->points = (long long)ppf * (long long)nfaces;
+
+  IrregularMap map5(5), map7(7);
+  IrregularMap *maps[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, &map5, nullptr, &map7};
+  // Per face: B = m sum_points c c^T over its control points (every point of
+  // a face is a combination of the face's own control points), then scattered.
+  struct Entry { int r, c; double v; };
+  std::vector<Entry> ent;
+  ent.reserve(nfaces * 144);
+  auto face_block = [&](const Face &f) {
+    const int N = f.ncp;
+    double B[kMaxCp][kMaxCp] = {};
+    double c[kMaxCp];
+    for (int fi = 0; fi <= plim; ++fi)
+      for (int fj = 0; fj <= plim - fi; ++fj) {
+        limit_point_coeffs(f, fi / (double)plim, fj / (double)plim, maps, c);
+        for (int a = 0; a < N; ++a)
+          for (int b = 0; b < N; ++b) B[a][b] += c[a] * c[b] * m;
+      }
+    for (int a = 0; a < N; ++a)
+      for (int b = 0; b < N; ++b) ent.push_back({f.cp[a], f.cp[b], B[a][b]});
+  };
+  for (const Face &f : p.reg_faces) face_block(f);
+  for (const Face &f : p.irr_faces) face_block(f);
+  std::sort(ent.begin(), ent.end(), [](const Entry &x, const Entry &y) { return x.r != y.r ? x.r < y.r : x.c < y.c; });
+  out->row_ptr.assign((size_t)nv + 1, 0);
+  out->col.clear();
+  out->val.clear();
+  for (size_t i = 0; i < ent.size();) {
+    size_t j = i;
+    double s = 0.0;
+    while (j < ent.size() && ent[j].r == ent[i].r && ent[j].c == ent[i].c) s += ent[j++].v;
+    out->col.push_back(ent[i].c);
+    out->val.push_back(s);
+    out->row_ptr[(size_t)ent[i].r + 1]++;
+    i = j;
+  }
+  for (int r = 0; r < nv; ++r) out->row_ptr[(size_t)r + 1] += out->row_ptr[r];
 }
 
 // ------------------------------------------------------------ lipids

@@ -55,6 +55,39 @@ double irregular_k(int valence);
 void build_regular_basis(PatchBasis *b);
 std::string build_irregular_basis(int valence, PatchBasis *b);
 
+// The irregular patch's map at (u,v) (irr_kernel::get_map,
+// src/irr_kernel.C:474-541): moves (u,v) into the coordinates of the
+// sub-triangle of its domain ring, returns the derivative scale of that move,
+// and cmap[y][x] = (Atot A^(domain-1))[pcycle[y]][x], the weights of control
+// point x in box spline y of the sub-triangle. Powers of A are cached.
+class IrregularMap {
+ public:
+  explicit IrregularMap(int valence);
+  void at(double *u, double *v, double *scale, double cmap[12][kMaxCp]);
+
+ private:
+  const std::vector<double> &power(int e);
+  int val_, n_;
+  std::vector<double> atot_;
+  std::vector<std::vector<double>> powers_;
+};
+
+// Limit-surface point at (u,v) of a face as weights of the face's control
+// points (surface::get_pt_coeffs, src/uv_map.C:14-195): coef[x] for cp[x].
+// maps[valence] serves irregular faces. Returns the number of weights.
+int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8], double *coef);
+
+// Effective mass of the limit surface (getSparseEffectiveMass,
+// src/modes.C:1735-1740): M = sum over mass points k of m c_k c_k^T, with the
+// (plim+1)(plim+2)/2 points per face and the mass per point of src/hd.C:417-452.
+struct EffectiveMass {
+  double area0 = 0, mass_per_point = 0;
+  long long points = 0;
+  std::vector<int> row_ptr, col;  // CSR of M over vertices, columns ascending
+  std::vector<double> val;
+};
+void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, EffectiveMass *out);
+
 // Parses the lipid directives of an input file ("lipid library NAME APL c0",
 // "lipid outer NAME parts", "lipid inner NAME parts"; src/lipid_composition.C:47-300).
 std::string parse_lipids(const std::string &text, std::vector<Lipid> *lipids);
