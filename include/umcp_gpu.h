@@ -173,6 +173,24 @@ umcp_status umcp_mesh_info_get(const umcp_mesh *mesh, umcp_mesh_info *info);
 umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *ctx, int precision, int64_t n_energies,
                                    size_t *bytes);
 
+/* ---- global area and volume restraints ----------------------------------
+ * New global terms (the reference has no restraint energy on the total area
+ * or enclosed volume; its surface::area and volume.C only measure them):
+ *   A = sum over points of dudv w |Ru x Rv|   (the limit surface's area)
+ *   V = 1/3 sum of dudv w R.(Ru x Rv)         (its enclosed volume, signed by orientation)
+ *   E_r = 1/2 K_area (A - area0)^2 / area0 + 1/2 K_volume (V - volume0)^2
+ * added to every energy, gradient and step of the mesh (kcal/mol; K_area in
+ * kcal/mol/A^2, K_volume in kcal/mol/A^6). area0 or volume0 < 0 takes the
+ * resident state's value at the call. A volume restraint needs a closed
+ * surface. NULL or both constants 0 turns them off. Not available in batches
+ * or through umcp_energy_grad_static. */
+typedef struct {
+  double K_area, area0, K_volume, volume0;
+} umcp_restraints;
+umcp_status umcp_restraints_set(umcp_mesh *mesh, const umcp_restraints *rs);
+/* A, V and E_r of the latest evaluation (energy, gradient or step). */
+umcp_status umcp_restraints_get(umcp_mesh *mesh, double *area, double *volume, double *energy);
+
 /* ---- effective mass ---------------------------------------------------- */
 /* Install M^-1 as a CSR matrix over vertices (SparseMatrix nzl/nzv rows,
  * src/sparse.h:4-53). */

@@ -87,6 +87,10 @@ class BatchInfo(C.Structure):
     ]
 
 
+class Restraints(C.Structure):
+    _fields_ = [("K_area", C.c_double), ("area0", C.c_double), ("K_volume", C.c_double), ("volume0", C.c_double)]
+
+
 class MassOpts(C.Structure):
     _fields_ = [("mass_scale", C.c_double), ("points_per_edge", C.c_int), ("rel_tol", C.c_double)]
 
@@ -180,6 +184,8 @@ _SIGNATURES = {
     "umcp_mesh_energies": [_VP, _D, C.c_int64],
     "umcp_mass_build": [_VP, _VP, C.POINTER(MassOpts), C.POINTER(MassInfo)],
     "umcp_mass_get": [_VP, _D],
+    "umcp_restraints_set": [_VP, C.POINTER(Restraints)],
+    "umcp_restraints_get": [_VP, _D, _D, _D],
     "umcp_plan_point_coeffs": [_VP, C.c_int, C.c_double, C.c_double, _I, _D, _I],
     "umcp_batch_create": [_VP, C.c_int, C.POINTER(BatchOpts), C.POINTER(_VP)],
     "umcp_batch_destroy": [_VP],
@@ -487,6 +493,21 @@ class Mesh:
         opts = MassOpts(mass_scale, points_per_edge, rel_tol)
         _check(library().umcp_mass_build(self._h, plan.handle, C.byref(opts), C.byref(info)))
         return info
+
+    def restraints_set(self, K_area: float = 0.0, area0: float = -1.0, K_volume: float = 0.0,
+                       volume0: float = -1.0) -> None:
+        """Global area/volume restraints (umcp_restraints_set); area0/volume0 < 0: the resident state's."""
+        rs = Restraints(K_area, area0, K_volume, volume0)
+        _check(library().umcp_restraints_set(self._h, C.byref(rs)))
+
+    def restraints_clear(self) -> None:
+        _check(library().umcp_restraints_set(self._h, None))
+
+    def restraints_get(self) -> tuple[float, float, float]:
+        """(A, V, E_r) of the latest evaluation."""
+        a, v, e = C.c_double(), C.c_double(), C.c_double()
+        _check(library().umcp_restraints_get(self._h, C.byref(a), C.byref(v), C.byref(e)))
+        return a.value, v.value, e.value
 
     def mass_get(self) -> np.ndarray:
         out = np.zeros((self.nv, self.nv))

@@ -381,6 +381,12 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
       UMCP_CUDA(upload(G->compf, std::vector<float>(comp.begin(), comp.end())));
     }
     UMCP_CUDA(upload(G->weight, B.weight));
+    {
+      std::vector<double> bw((size_t)G->npt * G->ncp);
+      for (int p = 0; p < G->npt; ++p)
+        for (int x = 0; x < G->ncp; ++x) bw[(size_t)p * G->ncp + x] = B.at(0, p, x);
+      UMCP_CUDA(upload(G->basis_w, bw));
+    }
     face_base += G->nfaces;
     slot_base += G->nfaces * G->ncp;
     m->groups.push_back(std::move(G));
@@ -457,12 +463,59 @@ extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *
   return UMCP_OK;
 }
 
-// Queue energy+gradient of state d_r: E -> d_E (and parts), gradient ADDED
-// into d_g (3*nv+3). d_g may be null to skip the gather.
+// Arguments of the area/volume kernels for state d_r.
+static GeoArgs geo_args(umcp_mesh *m, const double *d_r) {
+  GeoArgs G{};
+  int base = 0;
+  for (auto &Gp : m->groups) {
+    GeoGroup &g = G.g[G.ngroups++];
+    g.cp = Gp->cp.as<uint32_t>();
+    g.dest = Gp->dest.as<int>();
+    g.basis = Gp->basis.as<double>();
+    g.basis_w = Gp->basis_w.as<double>();
+    g.weight = Gp->weight.as<double>();
+    g.ncp = Gp->ncp;
+    g.npt = Gp->npt;
+    g.ncpp = (Gp->ncp + 3) / 4 * 4;
+    g.nfaces = Gp->nfaces;
+    g.face_base = base;
+    g.dudv = Gp->dudv;
+    base += Gp->nfaces;
+  }
+  G.nfaces = base;
+  G.nv = m->nv;
+  G.r = d_r;
+  for (int d = 0; d < 3; ++d)
+    for (int c = 0; c < 3; ++c) G.box[d][c] = m->P.box[d][c];
+  G.KA = m->rs.KA;
+  G.A0 = m->rs.A0;
+  G.KV = m->rs.KV;
+  G.V0 = m->rs.V0;
+  G.block = m->geo_block.as<double>();
+  G.gterm = m->gterm.as<double>();
+  G.done = m->geo_done.as<unsigned>();
+  return G;
+}
+
+// Face launches of an evaluation at d_r. With restraints on, the area and
+// volume sums run first (the face pass's finish adds their energy) and their
+// gradient is added into the partial slots after it.
 template <typename T>
-static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs *fin) {
+static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs *fin_in) {
   cudaStream_t s = m->ctx->stream;
   FinishArgs none{};
+  FinishArgs fin_geo{};
+  const FinishArgs *fin = fin_in;
+  const bool geo = m->rs.on && fin_in;
+  GeoArgs GA{};
+  if (geo) {
+    GA = geo_args(m, d_r);
+    cudaError_t e = launch_geo_sums(GA, s);
+    if (e != cudaSuccess) return e;
+    fin_geo = *fin_in;
+    fin_geo.gterm = m->gterm.as<double>();
+    fin = &fin_geo;
+  }
   for (size_t gi = 0; gi < m->groups.size(); ++gi) {
     auto &G = m->groups[gi];
     const bool last = (gi + 1 == m->groups.size());
@@ -485,6 +538,7 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
                                     m->status.as<int>(), G->nblocks, (last && fin) ? *fin : none, s);
     if (e != cudaSuccess) return e;
   }
+  if (geo) return launch_geo_grad<T>(GA, m->partial.as<T>(), s);
   return cudaSuccess;
 }
 
@@ -589,7 +643,7 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
   long long h2d = (long long)(m->off.bytes + (3 * (size_t)m->nv + 3) * sizeof(double));
   for (auto &G : m->groups)
     for (const DevBuf *x : {&G->cp, &G->g0, &G->rr0, &G->comp, &G->basis, &G->weight, &G->dest, &G->g0f, &G->rr0f,
-                            &G->compf})
+                            &G->compf, &G->basis_w})
       h2d += (long long)x->bytes;
   info->h2d_bytes = h2d;
   return UMCP_OK;
@@ -610,7 +664,7 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
   auto group = [&](const PatchBasis &B, size_t nf) {
     const size_t ncpp = (size_t)(B.ncp + 3) / 4 * 4;
     b += nf * B.ncp * 4 + 2 * nf * B.npt * 8 + nf * 3 * 8 + (size_t)B.npt * 5 * ncpp * 8 + B.weight.size() * 8 +
-         nf * B.ncp * 4;
+         nf * B.ncp * 4 + (size_t)B.npt * B.ncp * 8;
     if (f32) b += 2 * nf * B.npt * 4 + nf * 3 * 4;
     slots += nf * B.ncp;
     nblocks += f32 ? face_blocks<float>((int)nf, B.ncp, B.npt) : face_blocks<double>((int)nf, B.ncp, B.npt);
@@ -724,6 +778,69 @@ extern "C" umcp_status umcp_state_get(umcp_mesh *m, double *r, double *p) {
   if (r) UMCP_CUDA(cudaMemcpyAsync(r, m->r.p, nst * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
   if (p) UMCP_CUDA(cudaMemcpyAsync(p, m->p.p, (nst - 3) * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_restraints_set(umcp_mesh *m, const umcp_restraints *rs) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  if (m->batch) return fail(UMCP_ERR_INVALID, "remove the mesh from its batch first");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  cudaStream_t s = m->ctx->stream;
+  UMCP_CUDA(cudaStreamSynchronize(s));  // captured steps hold the previous setting
+  m->drop_graphs();
+  if (!rs || (rs->K_area == 0.0 && rs->K_volume == 0.0)) {
+    m->rs = umcp_mesh::Restraints{};
+    return UMCP_OK;
+  }
+  if (rs->K_area < 0 || rs->K_volume < 0) return fail(UMCP_ERR_INVALID, "restraint constants must be >= 0");
+  if (rs->K_volume != 0.0)
+    for (auto &G : m->groups) {
+      std::vector<uint32_t> cp((size_t)G->nfaces * G->ncp);
+      if (!cp.empty())
+        UMCP_CUDA(cudaMemcpy(cp.data(), G->cp.p, cp.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      const uint32_t home = (uint32_t)13 << dev::kVertexBits;  // image code of (0,0,0)
+      for (uint32_t c : cp)
+        if ((c & ~dev::kVertexMask) != home)
+          return fail(UMCP_ERR_INVALID, "a volume restraint needs a closed surface (this mesh is periodic)");
+    }
+  if (!m->gterm.p) {
+    int nblk = geo_blocks(m->nfaces);
+    UMCP_CUDA(m->geo_block.alloc((size_t)nblk * kGeoWords * sizeof(double)));
+    UMCP_CUDA(m->gterm.alloc(kGeoWords * sizeof(double)));
+    UMCP_CUDA(m->geo_done.alloc(sizeof(unsigned)));
+    UMCP_CUDA(cudaMemset(m->geo_done.p, 0, sizeof(unsigned)));
+  }
+  umcp_mesh::Restraints R;
+  R.on = true;
+  R.KA = rs->K_area;
+  R.KV = rs->K_volume;
+  R.A0 = rs->area0;
+  R.V0 = rs->volume0;
+  if (R.A0 < 0 || R.V0 < 0) {
+    // targets from the resident state: one sums pass with the constants off
+    m->rs = umcp_mesh::Restraints{true, 0, 1, 0, 0};
+    UMCP_CUDA(launch_geo_sums(geo_args(m, m->r.as<double>()), s));
+    double gt[kGeoWords];
+    UMCP_CUDA(cudaMemcpyAsync(gt, m->gterm.p, sizeof gt, cudaMemcpyDeviceToHost, s));
+    UMCP_CUDA(cudaStreamSynchronize(s));
+    if (R.A0 < 0) R.A0 = gt[kGeoA];
+    if (R.V0 < 0) R.V0 = gt[kGeoV];
+  }
+  if (!(R.A0 > 0) && R.KA != 0) return fail(UMCP_ERR_INVALID, "area restraint needs area0 > 0");
+  m->rs = R;
+  return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_restraints_get(umcp_mesh *m, double *area, double *volume, double *energy) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  if (!m->rs.on) return fail(UMCP_ERR_INVALID, "no restraints set");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  double gt[kGeoWords];
+  UMCP_CUDA(cudaMemcpyAsync(gt, m->gterm.p, sizeof gt, cudaMemcpyDeviceToHost, m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  if (area) *area = gt[kGeoA];
+  if (volume) *volume = gt[kGeoV];
+  if (energy) *energy = gt[kGeoE];
   return UMCP_OK;
 }
 
@@ -916,6 +1033,7 @@ static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, double *d_E, double *d_g) {
   if (!m || !d_r || !d_E) return fail(UMCP_ERR_INVALID, "null argument");
+  if (m->rs.on) return fail(UMCP_ERR_UNSUPPORTED, "the static entry point has no area/volume restraint terms");
   const int dev = m->ctx->device;
   if (dev < 0 || dev >= 128) return fail(UMCP_ERR_INVALID, "device index out of range for the static scratch table");
   UMCP_CUDA(cudaSetDevice(dev));

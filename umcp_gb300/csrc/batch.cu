@@ -376,6 +376,7 @@ extern "C" umcp_status umcp_batch_add(umcp_batch *b, umcp_mesh *m, const umcp_in
   if (m->batch) return fail(UMCP_ERR_INVALID, "mesh is already in a batch");
   if (n_steps < 0) return fail(UMCP_ERR_INVALID, "negative step count");
   if (it->use_mass) return fail(UMCP_ERR_INVALID, "batched jobs use the identity mass (use_mass must be 0)");
+  if (m->rs.on) return fail(UMCP_ERR_UNSUPPORTED, "batched jobs have no area/volume restraints");
   for (auto &Gp : m->groups)
     if (type_of(*Gp) < 0) return fail(UMCP_ERR_INVALID, "patch type not supported in a batch");
   Job J;

@@ -35,6 +35,7 @@ struct Group {
   int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
   double dudv = 0.5;
   DevBuf cp, g0, rr0, comp, basis, weight, dest;
+  DevBuf basis_w;           // value rows [npt][ncp] (area and volume terms)
   DevBuf g0f, rr0f, compf;  // FP32 copies for the precision form
 };
 }  // namespace umcp
@@ -79,6 +80,12 @@ struct umcp_mesh {
   umcp::DevBuf energies;
   size_t energies_cap = 0;
   umcp_batch *batch = nullptr;  // the batch this mesh is a job of, if any
+  // global area/volume restraints (umcp_restraints_set)
+  struct Restraints {
+    bool on = false;
+    double KA = 0, A0 = 0, KV = 0, V0 = 0;
+  } rs;
+  umcp::DevBuf geo_block, gterm, geo_done;
   double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
   double *h_stage2 = nullptr; // pinned, 3*nv doubles
   uint64_t *h_cnt = nullptr;  // pinned, 2 counters
@@ -106,10 +113,11 @@ struct umcp_mesh {
     size_t b = 0;
     for (auto &G : groups)
       for (const umcp::DevBuf *x : {&G->cp, &G->g0, &G->rr0, &G->comp, &G->basis, &G->weight, &G->dest, &G->g0f,
-                                    &G->rr0f, &G->compf})
+                                    &G->rr0f, &G->compf, &G->basis_w})
         b += x->bytes;
     for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
-                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense})
+                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &geo_block, &gterm,
+                                  &geo_done})
       b += x->bytes;
     return b;
   }

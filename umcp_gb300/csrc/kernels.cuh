@@ -25,6 +25,7 @@
 namespace umcp {
 namespace dev {
 
+constexpr int kMaxCpDev = 13;   // control points of the largest patch (valence 7 + 6)
 constexpr int kVertexBits = 27;  // packed control point: vertex | image_code << 27
 constexpr uint32_t kVertexMask = (1u << kVertexBits) - 1u;
 constexpr double kSafety = 1e-12;  // SAFETY, src/interp.h:14

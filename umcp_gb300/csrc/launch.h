@@ -22,7 +22,41 @@ struct FinishArgs {
   double threshold;    // energy rise that flags divergence (<= 0: off)
   int *status;
   unsigned *done;
+  const double *gterm; // global restraint terms to add (NULL: none), see GeoArgs
 };
+
+// Global area and volume of the limit surface and their restraint (one FP64
+// thread per face over every patch type):
+//   A = sum dudv w |Ru x Rv|,  V = 1/3 sum dudv w R.(Ru x Rv)
+//   E_r = 1/2 K_A (A-A0)^2/A0 + 1/2 K_V (V-V0)^2
+// gterm receives {A, V, E_r, dE_r/dA, dE_r/dV, dE_r/dalpha_xyz}.
+struct GeoGroup {
+  const uint32_t *cp;      // [nfaces][ncp] packed control points
+  const int *dest;         // [nfaces][ncp] gradient-partial slots
+  const double *basis;     // [npt][5][ncpp] rows u,v,uu,uv,vv
+  const double *basis_w;   // [npt][ncp] value rows
+  const double *weight;    // [npt]
+  int ncp, npt, ncpp, nfaces, face_base;
+  double dudv;
+};
+enum : int { kGeoA = 0, kGeoV, kGeoE, kGeoCA, kGeoCV, kGeoDAlpha, kGeoWords = 8 };
+struct GeoArgs {
+  GeoGroup g[3];
+  int ngroups, nfaces, nv;
+  const double *r;
+  double box[3][3];
+  double KA, A0, KV, V0;
+  double *block;           // [blocks][8] partial sums
+  double *gterm;           // kGeoWords
+  unsigned *done;          // finished-block counter (zero between launches)
+};
+constexpr int kGeoThreads = 128;
+inline int geo_blocks(int nfaces) { return nfaces > 0 ? (nfaces + kGeoThreads - 1) / kGeoThreads : 1; }
+// Sums A, V and their alpha derivatives; the last block writes gterm.
+cudaError_t launch_geo_sums(const GeoArgs &G, cudaStream_t s);
+// partial[slot] += alpha * (dE_r/dA dA/dX + dE_r/dV dV/dX) for every (face, control point).
+template <typename T>
+cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s);
 
 // Persistent grid of the face pass for one patch type (fixed per device and
 // face count, so the order of every sum is fixed).

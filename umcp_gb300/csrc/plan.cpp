@@ -78,6 +78,21 @@ void box_spline_rows(double u, double v, double out[kKinds][12]) {
     }
 }
 
+void box_spline_values(double u, double v, double out[12]) {
+  const double w = 1.0 - u - v;
+  double pu[5] = {1, 0, 0, 0, 0}, pv[5] = {1, 0, 0, 0, 0}, pw[5] = {1, 0, 0, 0, 0};
+  for (int k = 1; k < 5; ++k) {
+    pu[k] = pu[k - 1] * u;
+    pv[k] = pv[k - 1] * v;
+    pw[k] = pw[k - 1] * w;
+  }
+  for (int x = 0; x < 12; ++x) {
+    double s = 0.0;
+    for (const Term &t : kSpline[kPerm[x]]) s += t.coef * (pu[t.a] * pv[t.b] * pw[t.c]);
+    out[x] = s / 12.0;
+  }
+}
+
 // ------------------------------------------------------------ quadrature
 
 double irregular_k(int valence) {
@@ -396,9 +411,7 @@ int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8],
   const int N = f.ncp;
   for (int x = 0; x < N; ++x) coef[x] = 0.0;
   if (f.valence == 6) {
-    double sp[kKinds][12];
-    box_spline_rows(u, v, sp);
-    for (int x = 0; x < 12; ++x) coef[x] = sp[0][x];
+    box_spline_values(u, v, coef);
     return N;
   }
   if (!(std::isfinite(-std::log10(u + v))) && u < 1e-10 && v < 1e-10) {
@@ -410,11 +423,11 @@ int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8],
   }
   double fu = u, fv = v, scale, cmap[12][kMaxCp];
   maps[f.valence]->at(&fu, &fv, &scale, cmap);
-  double sp[kKinds][12];
-  box_spline_rows(fu, fv, sp);
+  double sp[12];
+  box_spline_values(fu, fv, sp);
   for (int x = 0; x < N; ++x) {
     double s = 0.0;
-    for (int y = 0; y < 12; ++y) s += cmap[y][x] * sp[0][y];
+    for (int y = 0; y < 12; ++y) s += cmap[y][x] * sp[y];
     coef[x] = s;
   }
   return N;

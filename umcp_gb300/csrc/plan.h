@@ -43,6 +43,8 @@ struct Plan {
 // first and second derivatives at (u,v), in the reference's control-point
 // order (ceff_map, src/interpLib.C:6012): out[kind][cp].
 void box_spline_rows(double u, double v, double out[kKinds][12]);
+// The values alone (the w row of box_spline_rows), out[cp].
+void box_spline_values(double u, double v, double out[12]);
 
 // Gauss nodes/weights for the singular weights of an irregular patch
 // (src/gauss.C get_v_pts / get_u_pts): n points, eigenvalue parameter k.

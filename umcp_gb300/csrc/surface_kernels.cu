@@ -77,10 +77,15 @@ __device__ void finish_sums(const FinishArgs &F, const double *__restrict__ bloc
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double e = red[0][0] + red[1][0] + red[2][0];
+    double e = red[0][0] + red[1][0] + red[2][0];
+    double ga[3] = {red[3][0], red[4][0], red[5][0]};
+    if (F.gterm) {  // the global restraints, summed before the face pass
+      e += F.gterm[kGeoE];
+      for (int c = 0; c < 3; ++c) ga[c] += F.gterm[kGeoDAlpha + c];
+    }
     if (F.E) F.E[0] = e;
     if (F.parts) { F.parts[0] = red[0][0]; F.parts[1] = red[1][0]; F.parts[2] = red[2][0]; }
-    if (F.galpha) { F.galpha[0] += red[3][0]; F.galpha[1] += red[4][0]; F.galpha[2] += red[5][0]; }
+    if (F.galpha) { F.galpha[0] += ga[0]; F.galpha[1] += ga[1]; F.galpha[2] += ga[2]; }
     if (!isfinite(e)) atomicOr(F.status, kStatusNonFinite);
     if (F.energies) {
       const uint64_t idx = F.cnt[1];
@@ -747,6 +752,159 @@ __global__ void batch_start_kernel(const BatchJob *__restrict__ jobs, const Batc
   }
 }
 
+// ---------------------------------------------------------------- area, volume
+
+// One face's limit-surface positions and tangents at its points, FP64, in
+// absolute coordinates (alpha-scaled, lattice images applied).
+struct GeoFace {
+  double X[kMaxCpDev][3];
+  int ncp;
+};
+
+__device__ __forceinline__ const GeoGroup &geo_group(const GeoArgs &G, int f, int *local) {
+  int k = 0;
+  while (k + 1 < G.ngroups && f >= G.g[k + 1].face_base) ++k;
+  *local = f - G.g[k].face_base;
+  return G.g[k];
+}
+
+__device__ __forceinline__ void geo_load(const GeoArgs &G, const GeoGroup &g, int lf, const double alpha[3],
+                                         GeoFace &F) {
+  F.ncp = g.ncp;
+  for (int x = 0; x < g.ncp; ++x) {
+    const uint32_t packed = g.cp[(size_t)lf * g.ncp + x];
+    const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+    const int im[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+    for (int c = 0; c < 3; ++c)
+      F.X[x][c] = alpha[c] * (G.r[3 * (size_t)v + c] + im[0] * G.box[0][c] + im[1] * G.box[1][c] + im[2] * G.box[2][c]);
+  }
+}
+
+__device__ __forceinline__ void cross3(const double a[3], const double b[3], double o[3]) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Point p of face F: R, Ru, Rv and the weight dudv w.
+__device__ __forceinline__ void geo_point(const GeoGroup &g, const GeoFace &F, int p, double R[3], double Ru[3],
+                                          double Rv[3]) {
+  for (int c = 0; c < 3; ++c) R[c] = Ru[c] = Rv[c] = 0.0;
+  const double *bu = g.basis + (size_t)p * 5 * g.ncpp, *bv = bu + g.ncpp, *bw = g.basis_w + (size_t)p * g.ncp;
+  for (int x = 0; x < F.ncp; ++x)
+    for (int c = 0; c < 3; ++c) {
+      R[c] += bw[x] * F.X[x][c];
+      Ru[c] += bu[x] * F.X[x][c];
+      Rv[c] += bv[x] * F.X[x][c];
+    }
+}
+
+__global__ void __launch_bounds__(kGeoThreads) geo_sums_kernel(GeoArgs G) {
+  __shared__ double red[kGeoWords][kGeoThreads];
+  __shared__ bool last;
+  const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
+  double acc[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0};  // A, V, dA/dalpha (3), dV/dalpha (3)
+  const int f = blockIdx.x * kGeoThreads + threadIdx.x;
+  if (f < G.nfaces) {
+    int lf;
+    const GeoGroup &g = geo_group(G, f, &lf);
+    GeoFace F;
+    geo_load(G, g, lf, alpha, F);
+    for (int p = 0; p < g.npt; ++p) {
+      double R[3], Ru[3], Rv[3], m[3];
+      geo_point(g, F, p, R, Ru, Rv);
+      cross3(Ru, Rv, m);
+      const double gg = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+      const double c = g.dudv * g.weight[p];
+      acc[0] += c * gg;
+      acc[1] += c / 3.0 * (R[0] * m[0] + R[1] * m[1] + R[2] * m[2]);
+      // d/dalpha_c through X = alpha Y: the tangents scale with alpha_c
+      double n[3] = {m[0] / gg, m[1] / gg, m[2] / gg}, a1[3], a2[3], v1[3], v2[3];
+      cross3(Rv, n, a1);  // dg/dRu
+      cross3(n, Ru, a2);  // dg/dRv
+      cross3(Rv, R, v1);  // d(R.m)/dRu
+      cross3(R, Ru, v2);  // d(R.m)/dRv
+      for (int k = 0; k < 3; ++k) {
+        acc[2 + k] += c * (a1[k] * Ru[k] + a2[k] * Rv[k]) / alpha[k];
+        acc[5 + k] += c / 3.0 * (m[k] * R[k] + v1[k] * Ru[k] + v2[k] * Rv[k]) / alpha[k];
+      }
+    }
+  }
+  for (int q = 0; q < kGeoWords; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = kGeoThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < kGeoWords; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < kGeoWords) G.block[(size_t)blockIdx.x * kGeoWords + threadIdx.x] = red[threadIdx.x][0];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(G.done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // Fixed-order sum of the block rows (thread q sums word q).
+  if (threadIdx.x < kGeoWords) {
+    double t = 0;
+    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(&G.block[(size_t)b * kGeoWords + threadIdx.x]);
+    red[threadIdx.x][0] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double A = red[0][0], V = red[1][0];
+    const double cA = G.A0 > 0 ? G.KA * (A - G.A0) / G.A0 : 0.0, cV = G.KV * (V - G.V0);
+    G.gterm[kGeoA] = A;
+    G.gterm[kGeoV] = V;
+    G.gterm[kGeoE] = (G.A0 > 0 ? 0.5 * G.KA * (A - G.A0) * (A - G.A0) / G.A0 : 0.0) + 0.5 * G.KV * (V - G.V0) * (V - G.V0);
+    G.gterm[kGeoCA] = cA;
+    G.gterm[kGeoCV] = cV;
+    for (int k = 0; k < 3; ++k) G.gterm[kGeoDAlpha + k] = cA * red[2 + k][0] + cV * red[5 + k][0];
+    *G.done = 0u;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__restrict__ partial) {
+  const int f = blockIdx.x * kGeoThreads + threadIdx.x;
+  if (f >= G.nfaces) return;
+  const double cA = G.gterm[kGeoCA], cV = G.gterm[kGeoCV];
+  if (cA == 0.0 && cV == 0.0) return;
+  const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
+  int lf;
+  const GeoGroup &g = geo_group(G, f, &lf);
+  GeoFace F;
+  geo_load(G, g, lf, alpha, F);
+  double Gx[kMaxCpDev][3];
+  for (int x = 0; x < F.ncp; ++x) Gx[x][0] = Gx[x][1] = Gx[x][2] = 0.0;
+  for (int p = 0; p < g.npt; ++p) {
+    double R[3], Ru[3], Rv[3], m[3];
+    geo_point(g, F, p, R, Ru, Rv);
+    cross3(Ru, Rv, m);
+    const double gg = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    const double c = g.dudv * g.weight[p];
+    double n[3] = {m[0] / gg, m[1] / gg, m[2] / gg}, a1[3], a2[3], v1[3], v2[3];
+    cross3(Rv, n, a1);
+    cross3(n, Ru, a2);
+    cross3(Rv, R, v1);
+    cross3(R, Ru, v2);
+    // dE_r/dR, dE_r/dRu, dE_r/dRv at this point
+    double eR[3], eU[3], eV[3];
+    for (int k = 0; k < 3; ++k) {
+      eR[k] = cV * c / 3.0 * m[k];
+      eU[k] = cA * c * a1[k] + cV * c / 3.0 * v1[k];
+      eV[k] = cA * c * a2[k] + cV * c / 3.0 * v2[k];
+    }
+    const double *bu = g.basis + (size_t)p * 5 * g.ncpp, *bv = bu + g.ncpp, *bw = g.basis_w + (size_t)p * g.ncp;
+    for (int x = 0; x < F.ncp; ++x)
+      for (int k = 0; k < 3; ++k) Gx[x][k] += bw[x] * eR[k] + bu[x] * eU[k] + bv[x] * eV[k];
+  }
+  for (int x = 0; x < F.ncp; ++x) {
+    const int d = g.dest[(size_t)lf * g.ncp + x];
+    for (int k = 0; k < 3; ++k) partial[3 * (size_t)d + k] = (T)((double)partial[3 * (size_t)d + k] + alpha[k] * Gx[x][k]);
+  }
+}
+
 // One warp per row; lanes stride the row's nonzeros (coalesced reads of the
 // value/column streams), warp-shuffle sum in fixed order.
 __global__ void spmv_kernel(int nrow, const int *__restrict__ row_ptr, const int *__restrict__ col,
@@ -961,5 +1119,23 @@ cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, co
   dev::batch_start_kernel<<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, start, step0);
   return cudaGetLastError();
 }
+
+}  // namespace umcp
+
+namespace umcp {
+
+cudaError_t launch_geo_sums(const GeoArgs &G, cudaStream_t s) {
+  dev::geo_sums_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s) {
+  if (G.nfaces <= 0) return cudaSuccess;
+  dev::geo_grad_kernel<T><<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G, partial);
+  return cudaGetLastError();
+}
+template cudaError_t launch_geo_grad<double>(const GeoArgs &, double *, cudaStream_t);
+template cudaError_t launch_geo_grad<float>(const GeoArgs &, float *, cudaStream_t);
 
 }  // namespace umcp
