@@ -260,6 +260,21 @@ umcp_status umcp_run_async(umcp_mesh *mesh, const umcp_integrator *it, uint64_t 
  * This is the drop-in for one pass of the reference's dynamics loop body
  * (src/hd.C:1102-1720): energy, gradient, update. */
 umcp_status umcp_step_host(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step, double *r, double *p, double *E);
+/* ---- Loop subdivision of regular patches (fast_sub6_0..3, src/fast_mm.C) --
+ * d_in: n patches of 12 control points (xyz each, 36 doubles, the regular
+ * patch's point order); d_out: n x 4 child patches of 36 doubles, children in
+ * the reference's order. Device pointers, queued on the context's stream. */
+umcp_status umcp_subdivide_patches(umcp_ctx *ctx, const double *d_in, double *d_out, long long n);
+/* The stencils themselves: S[child][out point][in point], 4 x 12 x 12 (host). */
+umcp_status umcp_subdivision_stencils(double *S);
+
+/* Restart files in the reference's save format (src/restart.C:7-168): the
+ * box scales, one "x y z px py pz" line per vertex and one for the box
+ * scales, "seed N". Reading accepts lines without momenta and ignores the
+ * particle records a reference save may hold after the surface. */
+umcp_status umcp_restart_write(umcp_mesh *mesh, const char *path, int seed);
+/* Sets the resident state (r and p) from the file; *seed gets its seed (-1 if none). */
+umcp_status umcp_restart_read(umcp_mesh *mesh, const char *path, int *seed);
 /* Energies recorded by the mesh's latest run (umcp_run, umcp_run_async or a
  * batch job): the first n of them. Synchronizes the context stream. */
 umcp_status umcp_mesh_energies(umcp_mesh *mesh, double *energies, int64_t n);

@@ -207,6 +207,19 @@ def reference_mass(mesh: Path, params_txt: Path, prefix: Path, timeout: float = 
     return out
 
 
+def reference_sub6(prefix: Path, timeout: float = 60) -> np.ndarray:
+    """The reference's fast_sub6_0..3 (ref_driver sub6) as S[child][out point][in point]."""
+    subprocess.run([str(REF_DRIVER), "sub6", "-", "-", "-", str(prefix)], check=True, capture_output=True,
+                   timeout=timeout)
+    M = np.fromfile(f"{prefix}.sub6.bin", dtype=np.float64).reshape(4, 36, 36).transpose(0, 2, 1)
+    for k in range(4):  # the same 12 x 12 stencil acts on x, y and z
+        for c in range(3):
+            for d in range(3):
+                blk = M[k][c::3, d::3]
+                assert np.array_equal(blk, M[k][0::3, 0::3] if c == d else np.zeros_like(blk))
+    return M[:, 0::3, 0::3].copy()
+
+
 def reference_time(mesh: Path, params_txt: Path, n_calls: int, timeout: float = 600) -> dict:
     import json
     res = subprocess.run([str(REF_DRIVER), "time", str(mesh), str(params_txt), "-", str(n_calls)], check=True,

@@ -15,6 +15,7 @@
  *   ref_driver dump <mesh> <params> <positions.bin|-> <out_prefix>
  *   ref_driver time <mesh> <params> <positions.bin|-> <n_calls>
  *   ref_driver mass <mesh> <params> - <out_prefix>
+ *   ref_driver sub6 - - - <out_prefix>
  *
  * "mass" sets up the mass points as hd.C does before a dynamics run
  * (src/hd.C:417-481: a 66-point grid per triangle, mass per point from
@@ -134,8 +135,28 @@ static void dump_formulas(FILE *f, formula *frm, int n)
 	}
 }
 
+void fast_sub6_0(double *r_in, double *r_out);
+void fast_sub6_1(double *r_in, double *r_out);
+void fast_sub6_2(double *r_in, double *r_out);
+void fast_sub6_3(double *r_in, double *r_out);
+
 int main(int argc, char **argv)
 {
+	if (argc >= 6 && !strcmp(argv[1], "sub6")) {
+		/* The reference's four child stencils (src/fast_mm.C) as 36 x 36
+		 * matrices: column j is the image of unit vector j. */
+		void (*fn[4])(double *, double *) = {fast_sub6_0, fast_sub6_1, fast_sub6_2, fast_sub6_3};
+		FILE *f = open_out(argv[5], "sub6.bin", "wb");
+		for (int k = 0; k < 4; k++)
+			for (int j = 0; j < 36; j++) {
+				double in[36] = {0}, out[36] = {0};
+				in[j] = 1.0;
+				fn[k](in, out);
+				fwrite(out, sizeof(double), 36, f);
+			}
+		fclose(f);
+		return 0;
+	}
 	if (argc < 6) {
 		fprintf(stderr, "usage: %s dump|time <mesh> <params> <positions|-> <out_prefix|n_calls>\n", argv[0]);
 		return 2;

@@ -9,7 +9,8 @@ Each case writes <name>.mesh (the input mesh, full-precision positions),
 reference's energy terms, gradient, evaluation positions, per-face energies
 and, for small meshes, its plan tables (control points, basis rows, g0).
 
-`--mass` writes <name>.mass.npz for the MASS_CASES instead, from the existing
+`--sub6` writes sub6.npz: the reference's regular-patch subdivision
+stencils. `--mass` writes <name>.mass.npz for the MASS_CASES instead, from the existing
 mesh and params files: the reference's inverse effective mass (dense), its
 mass per point and area0, and the limit-surface weights of the 66 mass
 points of four faces (two regular, two irregular where there are any).
@@ -113,6 +114,14 @@ def make_case(name, gen, params_txt, deform, keep_plan, work: Path) -> None:
 MASS_CASES = ["ico2_plain", "planar12_deformed"]
 
 
+def make_sub6(work: Path) -> None:
+    """The reference's four regular-patch subdivision stencils (fast_sub6_k),
+    as 12 x 12 matrices per child (the same for x, y and z)."""
+    S = B.reference_sub6(work / "s")
+    np.savez_compressed(HERE / "sub6.npz", stencils=S)
+    print("sub6: 4 stencils")
+
+
 def make_mass_case(name: str, work: Path) -> None:
     ref = B.reference_mass(HERE / f"{name}.mesh", HERE / f"{name}.params", work / name)
     pts = ref["points"]
@@ -129,6 +138,9 @@ def main() -> None:
     if not B.reference_available():
         raise SystemExit("reference-built oracle missing; build it with __graft_entry__.build() where the reference exists")
     with tempfile.TemporaryDirectory() as td:
+        if "--sub6" in sys.argv:
+            make_sub6(Path(td))
+            return
         if "--mass" in sys.argv:
             for name in MASS_CASES:
                 make_mass_case(name, Path(td))

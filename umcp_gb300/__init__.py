@@ -182,6 +182,10 @@ _SIGNATURES = {
     "umcp_run_async": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int],
     "umcp_step_host": [_VP, C.POINTER(Integrator), C.c_uint64, _D, _D, _D],
     "umcp_mesh_energies": [_VP, _D, C.c_int64],
+    "umcp_subdivide_patches": [_VP, _VP, _VP, C.c_longlong],
+    "umcp_subdivision_stencils": [_D],
+    "umcp_restart_write": [_VP, C.c_char_p, C.c_int],
+    "umcp_restart_read": [_VP, C.c_char_p, _I],
     "umcp_mass_build": [_VP, _VP, C.POINTER(MassOpts), C.POINTER(MassInfo)],
     "umcp_mass_get": [_VP, _D],
     "umcp_restraints_set": [_VP, C.POINTER(Restraints)],
@@ -514,6 +518,15 @@ class Mesh:
         _check(library().umcp_mass_get(self._h, _dp(out)))
         return out
 
+    def restart_write(self, path, seed: int = -1) -> None:
+        _check(library().umcp_restart_write(self._h, str(path).encode(), seed))
+
+    def restart_read(self, path) -> int:
+        """Loads a restart file into the resident state; returns its seed (-1 if none)."""
+        seed = C.c_int()
+        _check(library().umcp_restart_read(self._h, str(path).encode(), C.byref(seed)))
+        return seed.value
+
     def energies(self, n: int) -> np.ndarray:
         """The first n energies recorded by the latest run or batch job."""
         e = np.zeros(max(n, 1))
@@ -570,6 +583,18 @@ class Batch:
     def face_pass(self) -> None:
         """Queues the face launches of one step only (for timing)."""
         _check(library().umcp_batch_face_pass(self._h))
+
+
+def subdivision_stencils() -> np.ndarray:
+    """S[child][out point][in point] of regular-patch Loop subdivision (4 x 12 x 12)."""
+    S = np.zeros((4, 12, 12))
+    _check(library().umcp_subdivision_stencils(_dp(S)))
+    return S
+
+
+def subdivide_patches(ctx: "Context", d_in: int, d_out: int, n: int) -> None:
+    """Device-pointer batched subdivision: n x 36 doubles in, n x 4 x 36 out."""
+    _check(library().umcp_subdivide_patches(ctx.handle, C.c_void_p(d_in), C.c_void_p(d_out), n))
 
 
 def integrator(kind=OVERDAMPED_BD, time_step=1.0, gamma=0.0, D=0.0, seed=1, stream=0, divergence_threshold=0.0,

@@ -4,6 +4,7 @@ reference-built oracle binary. Objects are rebuilt only when a source is newer.
 
 Outputs (all git-ignored):
   umcp_gb300/lib/libumcp_gb300.so   engine: kernels + C ABI (include/umcp_gpu.h)
+  umcp_gb300/lib/hd_gb300           the hd-style dynamics driver on the engine
   oracle/lib/libumcp_oracle.so      CPU restatement used by tests as the checker
   oracle/_ref/ref_driver            reference sources + shims (only where they exist)
 """
@@ -21,6 +22,7 @@ CSRC = ROOT / "umcp_gb300" / "csrc"
 BUILD = ROOT / "umcp_gb300" / "_build"
 LIB_DIR = ROOT / "umcp_gb300" / "lib"
 ENGINE_LIB = LIB_DIR / "libumcp_gb300.so"
+HD_EXE = LIB_DIR / "hd_gb300"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "lib" / "libumcp_oracle.so"
 REF_TREE = Path(os.environ.get("UMCP_REFERENCE_SRC", "/root/reference/src"))
@@ -77,6 +79,10 @@ def build_engine(verbose: bool = False) -> Path:
             fut.result()
     if jobs or _stale(ENGINE_LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(ENGINE_LIB)] + [str(o) for o in objs] + ["-ldl"])
+    hd_src = ROOT / "umcp_gb300" / "hd" / "hd_main.cpp"
+    if _stale(HD_EXE, [hd_src, ENGINE_LIB, ROOT / "include" / "umcp_gpu.h"]):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-o", str(HD_EXE), str(hd_src), "-L", str(LIB_DIR), "-lumcp_gb300",
+              "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print(f"built {ENGINE_LIB}")
     return ENGINE_LIB

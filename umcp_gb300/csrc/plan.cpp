@@ -405,6 +405,64 @@ std::string build_irregular_basis(int val, PatchBasis *b) {
   return "";
 }
 
+// ------------------------------------------------------------ subdivision
+
+void subdivision_stencils(double S[4][12][12]) {
+  // Refinability of the box splines: the patch over a child triangle is
+  // itself a box-spline patch, so its control points C_k = S_k P are the
+  // exact least-squares fit of the parent patch on the child. Child frames
+  // (origin, u' corner, v' corner) in parent coordinates, in the order the
+  // reference numbers its children (src/fast_mm.C fast_sub6_0..3): the corner
+  // children share the parent's orientation, the centre one is turned 180
+  // degrees.
+  static const double frame[4][3][2] = {{{0, 0}, {0.5, 0}, {0, 0.5}},
+                                        {{0.5, 0}, {1, 0}, {0.5, 0.5}},
+                                        {{0, 0.5}, {0.5, 0.5}, {0, 1}},
+                                        {{0.5, 0.5}, {0, 0.5}, {0.5, 0}}};
+  const int ns = 28;  // sample points: a triangular grid strictly inside the child
+  double sp[ns][2];
+  int q = 0;
+  for (int i = 1; i <= 7 && q < ns; ++i)
+    for (int j = 1; i + j <= 8 && q < ns; ++j) sp[q][0] = i / 9.0, sp[q][1] = j / 9.0, ++q;
+  for (int k = 0; k < 4; ++k) {
+    const double *P0 = frame[k][0], *P1 = frame[k][1], *P2 = frame[k][2];
+    // normal equations (Bc^T Bc) S = Bc^T Bp
+    double A[12][12] = {}, R[12][12] = {};
+    for (int t = 0; t < q; ++t) {
+      double bc[12], bp[12];
+      const double a = sp[t][0], b = sp[t][1];
+      box_spline_values(a, b, bc);
+      box_spline_values(P0[0] + a * (P1[0] - P0[0]) + b * (P2[0] - P0[0]),
+                        P0[1] + a * (P1[1] - P0[1]) + b * (P2[1] - P0[1]), bp);
+      for (int x = 0; x < 12; ++x)
+        for (int y = 0; y < 12; ++y) {
+          A[x][y] += bc[x] * bc[y];
+          R[x][y] += bc[x] * bp[y];
+        }
+    }
+    // Gauss-Jordan with partial pivoting on [A | R]
+    for (int c = 0; c < 12; ++c) {
+      int piv = c;
+      for (int r = c + 1; r < 12; ++r)
+        if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+      for (int y = 0; y < 12; ++y) {
+        std::swap(A[c][y], A[piv][y]);
+        std::swap(R[c][y], R[piv][y]);
+      }
+      const double d = A[c][c];
+      for (int y = 0; y < 12; ++y) { A[c][y] /= d; R[c][y] /= d; }
+      for (int r = 0; r < 12; ++r) {
+        if (r == c || A[r][c] == 0.0) continue;
+        const double f = A[r][c];
+        for (int y = 0; y < 12; ++y) { A[r][y] -= f * A[c][y]; R[r][y] -= f * R[c][y]; }
+      }
+    }
+    // Loop subdivision weights are multiples of 1/16: round the fit to them.
+    for (int x = 0; x < 12; ++x)
+      for (int y = 0; y < 12; ++y) S[k][x][y] = std::nearbyint(R[x][y] * 16.0) / 16.0;
+  }
+}
+
 // ------------------------------------------------------------ limit points
 
 int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8], double *coef) {

@@ -74,6 +74,11 @@ class IrregularMap {
   std::vector<std::vector<double>> powers_;
 };
 
+// Loop subdivision of a regular 12-point patch into its four children
+// (fast_sub6_0..3, src/fast_mm.C): child k's control point x is
+// sum_y S[k][x][y] P[y], in the reference's child numbering and point order.
+void subdivision_stencils(double S[4][12][12]);
+
 // Limit-surface point at (u,v) of a face as weights of the face's control
 // points (surface::get_pt_coeffs, src/uv_map.C:14-195): coef[x] for cp[x].
 // maps[valence] serves irregular faces. Returns the number of weights.
