@@ -108,6 +108,15 @@ umcp_status umcp_plan_lipids(const umcp_plan *plan, double *c0, double *apl);
  * ids[n] (surface::get_pt_coeffs, src/uv_map.C:14-195); n <= 13. */
 umcp_status umcp_plan_point_coeffs(const umcp_plan *plan, int face, double u, double v, int *ids, double *coef,
                                    int *n);
+/* Limit-surface points and unit normals (surface::evaluateRNRM,
+ * src/interpLib.C:7936-8100) of state r (3*nv+3, box scales applied) at n
+ * queries (faces[q], uv[2q], uv[2q+1]): R[3n], N[3n] (N may be NULL; the
+ * normal of the surface before the box scaling, as the reference forms it). At an
+ * extraordinary vertex itself the normal is NaN, as the reference leaves it;
+ * the position there follows r, where the reference reads its stored vertex
+ * positions. Host only. */
+umcp_status umcp_plan_evaluate(const umcp_plan *plan, const double *r, int n, const int *faces, const double *uv,
+                               double *R, double *N);
 void umcp_plan_destroy(umcp_plan *plan);
 
 /* ---- device context and meshes --------------------------------------- */

@@ -220,6 +220,14 @@ def reference_sub6(prefix: Path, timeout: float = 60) -> np.ndarray:
     return M[:, 0::3, 0::3].copy()
 
 
+def reference_rnrm(mesh: Path, params_txt: Path, positions: Path | None, prefix: Path, timeout: float = 600):
+    """surface::evaluateRNRM of the reference at 7 fixed (u,v) on every face:
+    rows of (face, u, v, R[3], N[3])."""
+    cmd = [str(REF_DRIVER), "rnrm", str(mesh), str(params_txt), str(positions) if positions else "-", str(prefix)]
+    subprocess.run(cmd, check=True, capture_output=True, timeout=timeout)
+    return np.fromfile(f"{prefix}.rnrm.bin", dtype=np.float64).reshape(-1, 9)
+
+
 def reference_time(mesh: Path, params_txt: Path, n_calls: int, timeout: float = 600) -> dict:
     import json
     res = subprocess.run([str(REF_DRIVER), "time", str(mesh), str(params_txt), "-", str(n_calls)], check=True,

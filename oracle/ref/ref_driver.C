@@ -16,6 +16,8 @@
  *   ref_driver time <mesh> <params> <positions.bin|-> <n_calls>
  *   ref_driver mass <mesh> <params> - <out_prefix>
  *   ref_driver sub6 - - - <out_prefix>
+ *   ref_driver rnrm <mesh> <params> <positions.bin|-> <out_prefix>
+ *     surface::evaluateRNRM at 7 fixed (u,v) on every face: face, u, v, R, N
  *
  * "mass" sets up the mass points as hd.C does before a dynamics run
  * (src/hd.C:417-481: a 66-point grid per triangle, mass per point from
@@ -166,6 +168,21 @@ int main(int argc, char **argv)
 	int nv = s->nv;
 	load_positions(argv[4], r, nv);
 	double *g = (double *)calloc(3 * nv + 3, sizeof(double));
+
+	if (!strcmp(argv[1], "rnrm")) {
+		const double uvs[7][2] = {{1.0 / 3, 1.0 / 3}, {0.1, 0.2}, {0.7, 0.1}, {0.05, 0.05}, {0.0, 0.5}, {0.25, 0.0}, {0.45, 0.45}};
+		FILE *f = open_out(argv[5], "rnrm.bin", "wb");
+		for (int fc = 0; fc < s->nf_faces + s->nf_irr_faces; fc++)
+			for (int q = 0; q < 7; q++) {
+				double rp[3], nrm[3], rec[9];
+				s->evaluateRNRM(fc, uvs[q][0], uvs[q][1], rp, nrm, r);
+				rec[0] = fc; rec[1] = uvs[q][0]; rec[2] = uvs[q][1];
+				for (int c = 0; c < 3; c++) { rec[3 + c] = rp[c]; rec[6 + c] = nrm[c]; }
+				fwrite(rec, sizeof(double), 9, f);
+			}
+		fclose(f);
+		return 0;
+	}
 
 	if (!strcmp(argv[1], "mass")) {
 		const int plim = 10, ppf = (plim + 1) * (plim + 2) / 2;

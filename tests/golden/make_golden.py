@@ -9,7 +9,8 @@ Each case writes <name>.mesh (the input mesh, full-precision positions),
 reference's energy terms, gradient, evaluation positions, per-face energies
 and, for small meshes, its plan tables (control points, basis rows, g0).
 
-`--sub6` writes sub6.npz: the reference's regular-patch subdivision
+`--rnrm` writes <name>.rnrm.npz for RNRM_CASES: the reference's limit
+points and normals on every face. `--sub6` writes sub6.npz: the reference's regular-patch subdivision
 stencils. `--mass` writes <name>.mass.npz for the MASS_CASES instead, from the existing
 mesh and params files: the reference's inverse effective mass (dense), its
 mass per point and area0, and the limit-surface weights of the 66 mass
@@ -114,6 +115,20 @@ def make_case(name, gen, params_txt, deform, keep_plan, work: Path) -> None:
 MASS_CASES = ["ico2_plain", "planar12_deformed"]
 
 
+RNRM_CASES = ["ico2_lipids", "planar12_deformed"]
+
+
+def make_rnrm(name: str, work: Path) -> None:
+    """The reference's limit points and normals (evaluateRNRM) on every face of
+    the case's evaluation state."""
+    r = np.load(HERE / f"{name}.npz")["r"]
+    pos = work / f"{name}.r.bin"
+    r.tofile(pos)
+    rows = B.reference_rnrm(HERE / f"{name}.mesh", HERE / f"{name}.params", pos, work / name)
+    np.savez_compressed(HERE / f"{name}.rnrm.npz", rows=rows)
+    print(f"{name}: {len(rows)} limit points")
+
+
 def make_sub6(work: Path) -> None:
     """The reference's four regular-patch subdivision stencils (fast_sub6_k),
     as 12 x 12 matrices per child (the same for x, y and z)."""
@@ -138,6 +153,10 @@ def main() -> None:
     if not B.reference_available():
         raise SystemExit("reference-built oracle missing; build it with __graft_entry__.build() where the reference exists")
     with tempfile.TemporaryDirectory() as td:
+        if "--rnrm" in sys.argv:
+            for name in RNRM_CASES:
+                make_rnrm(name, Path(td))
+            return
         if "--sub6" in sys.argv:
             make_sub6(Path(td))
             return

@@ -191,6 +191,7 @@ _SIGNATURES = {
     "umcp_restraints_set": [_VP, C.POINTER(Restraints)],
     "umcp_restraints_get": [_VP, _D, _D, _D],
     "umcp_plan_point_coeffs": [_VP, C.c_int, C.c_double, C.c_double, _I, _D, _I],
+    "umcp_plan_evaluate": [_VP, _D, C.c_int, _I, _D, _D, _D],
     "umcp_batch_create": [_VP, C.c_int, C.POINTER(BatchOpts), C.POINTER(_VP)],
     "umcp_batch_destroy": [_VP],
     "umcp_batch_add": [_VP, _VP, C.POINTER(Integrator), C.c_uint64, C.c_int64],
@@ -320,6 +321,16 @@ class Plan:
         n = C.c_int()
         _check(library().umcp_plan_point_coeffs(self._h, face, u, v, _ip(ids), _dp(coef), C.byref(n)))
         return ids[:n.value], coef[:n.value]
+
+    def evaluate(self, r: np.ndarray, faces, uv) -> tuple[np.ndarray, np.ndarray]:
+        """Limit-surface points and unit normals of state r at (face, u, v) queries."""
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        uv = np.ascontiguousarray(uv, dtype=np.float64).reshape(-1, 2)
+        n = len(faces)
+        R, N = np.zeros((n, 3)), np.zeros((n, 3))
+        _check(library().umcp_plan_evaluate(self._h, _dp(np.ascontiguousarray(r, dtype=np.float64)), n, _ip(faces),
+                                            _dp(uv), _dp(R), _dp(N)))
+        return R, N
 
     def positions(self) -> np.ndarray:
         r = np.zeros(3 * self.nv + 3)

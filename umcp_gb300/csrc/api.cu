@@ -151,6 +151,43 @@ extern "C" umcp_status umcp_plan_point_coeffs(const umcp_plan *plan, int face, d
   return UMCP_OK;
 }
 
+extern "C" umcp_status umcp_plan_evaluate(const umcp_plan *plan, const double *r, int n, const int *faces,
+                                          const double *uv, double *R, double *N) {
+  if (!plan || !r || n < 0 || (n > 0 && (!faces || !uv || !R))) return fail(UMCP_ERR_INVALID, "bad argument");
+  const Plan &P = plan->plan;
+  const Mesh &ME = plan->mesh;
+  const int nreg = (int)P.reg_faces.size(), nirr = (int)P.irr_faces.size(), nv = ME.nv;
+  IrregularMap m5(5), m7(7);
+  IrregularMap *maps[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, &m5, nullptr, &m7};
+  for (int q = 0; q < n; ++q) {
+    const int face = faces[q];
+    const double u = uv[2 * q], v = uv[2 * q + 1];
+    if (face < 0 || face >= nreg + nirr) return fail(UMCP_ERR_INVALID, "face index out of range");
+    if (!(u >= -1e-4 && v >= -1e-4 && u + v <= 1.0 + 1e-4)) return fail(UMCP_ERR_INVALID, "(u,v) outside the face");
+    const Face &F = face < nreg ? P.reg_faces[face] : P.irr_faces[face - nreg];
+    double w[kMaxCp], du[kMaxCp], dv[kMaxCp];
+    limit_point_rows(F, u, v, maps, w, du, dv);
+    double X[3] = {0, 0, 0}, Xu[3] = {0, 0, 0}, Xv[3] = {0, 0, 0};
+    for (int x = 0; x < F.ncp; ++x)
+      for (int c = 0; c < 3; ++c) {
+        const double pos = r[3 * (size_t)F.cp[x] + c] + F.img[x][0] * ME.box[0][c] + F.img[x][1] * ME.box[1][c] +
+                           F.img[x][2] * ME.box[2][c];
+        X[c] += w[x] * pos;
+        Xu[c] += du[x] * pos;
+        Xv[c] += dv[x] * pos;
+      }
+    for (int c = 0; c < 3; ++c) R[3 * (size_t)q + c] = r[3 * (size_t)nv + c] * X[c];
+    if (N) {
+      // from the tangents before the box scaling, as the reference forms it
+      const double *a = Xu, *b = Xv;
+      double m[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+      const double l = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+      for (int c = 0; c < 3; ++c) N[3 * (size_t)q + c] = m[c] / l;
+    }
+  }
+  return UMCP_OK;
+}
+
 extern "C" umcp_status umcp_plan_set_reference(umcp_plan *plan, const double *r) {
   if (!plan || !r) return fail(UMCP_ERR_INVALID, "null argument");
   set_reference_state(plan->mesh, r, &plan->plan);

@@ -491,6 +491,37 @@ int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8],
   return N;
 }
 
+int limit_point_rows(const Face &f, double u, double v, IrregularMap *maps[8], double *w, double *du, double *dv) {
+  const int N = f.ncp;
+  for (int x = 0; x < N; ++x) w[x] = du[x] = dv[x] = 0.0;
+  double sp[kKinds][12];
+  if (f.valence == 6) {
+    box_spline_rows(u, v, sp);
+    for (int x = 0; x < 12; ++x) { w[x] = sp[0][x]; du[x] = sp[1][x]; dv[x] = sp[2][x]; }
+    return N;
+  }
+  if (!(std::isfinite(-std::log10(u + v))) && u < 1e-10 && v < 1e-10) {
+    limit_point_coeffs(f, u, v, maps, w);
+    for (int x = 0; x < N; ++x) du[x] = dv[x] = std::nan("");  // no tangent frame at the vertex itself
+    return N;
+  }
+  double fu = u, fv = v, scale, cmap[12][kMaxCp];
+  maps[f.valence]->at(&fu, &fv, &scale, cmap);
+  box_spline_rows(fu, fv, sp);
+  for (int x = 0; x < N; ++x) {
+    double a = 0, b = 0, c = 0;
+    for (int y = 0; y < 12; ++y) {
+      a += cmap[y][x] * sp[0][y];
+      b += cmap[y][x] * sp[1][y];
+      c += cmap[y][x] * sp[2][y];
+    }
+    w[x] = a;
+    du[x] = scale * b;
+    dv[x] = scale * c;
+  }
+  return N;
+}
+
 void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, EffectiveMass *out) {
   // Mass per point (src/hd.C:442-452): a lipid mass of 760.09 g/mol (POPC)
   // times mass_scale, spread over area0 at 65.35 A^2 per lipid and two

@@ -84,6 +84,11 @@ void subdivision_stencils(double S[4][12][12]);
 // maps[valence] serves irregular faces. Returns the number of weights.
 int limit_point_coeffs(const Face &f, double u, double v, IrregularMap *maps[8], double *coef);
 
+// The value rows with the u and v derivative rows (surface::evaluateRNRM,
+// src/interpLib.C:7936); at an extraordinary vertex itself the derivatives
+// are NaN, as the reference leaves the normal there.
+int limit_point_rows(const Face &f, double u, double v, IrregularMap *maps[8], double *w, double *du, double *dv);
+
 // Effective mass of the limit surface (getSparseEffectiveMass,
 // src/modes.C:1735-1740): M = sum over mass points k of m c_k c_k^T, with the
 // (plim+1)(plim+2)/2 points per face and the mass per point of src/hd.C:417-452.
