@@ -49,6 +49,8 @@ typedef struct {
   double temperature; /* K ("T", default 298) */
   int precision;      /* umcp_precision */
   const char *lipid_directives; /* text holding "lipid library|inner|outer ..." lines, or NULL */
+  int face_kernel;    /* precision form, regular faces: 0 FP32 SIMT kernel (default, faster here),
+                         1 tcgen05 tensor-core kernel (3xTF32 contractions) */
 } umcp_params;
 
 /* Sizes of a plan. */

@@ -215,3 +215,24 @@ def test_divergence_stops_the_run(ctx):
     it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=5.0, seed=2, divergence_threshold=10.0)
     with pytest.raises(U.UmcpError, match="diverged"):
         mesh.run(it, 0, 40)
+
+
+@pytest.mark.parametrize("name", ["ico3_deformed", "planar12_deformed", "ico4_plain", "ico2_lipids"])
+def test_tensor_core_face_kernel_matches_reference(ctx, name):
+    """The tcgen05 form of the regular-face pass (3xTF32 contractions on
+    affine-centred control points) meets the precision form's bounds against
+    the reference and is deterministic; its meshes run the same integrators."""
+    plan, prm, gold = load_case(name, U.FP32_CENTRED)
+    prm.face_kernel = U.TENSOR_CORES
+    mesh = U.Mesh(ctx, plan, prm)
+    r = gold["r"]
+    E, g = mesh.energy_grad(r)
+    assert abs(E - gold["E"]) <= E32 * abs(gold["E"])
+    assert rel_inf(g[:-3], gold["grad"][:-3]) <= G32 * 1.5
+    E2, g2 = mesh.energy_grad(r)
+    assert E2 == E and np.array_equal(g2, g)
+    it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.00125, seed=3)
+    e = mesh.run(it, 0, 40)
+    prm.face_kernel = U.SIMT
+    e_simt = U.Mesh(ctx, plan, prm).run(it, 0, 40)
+    assert np.all(np.isfinite(e)) and np.max(np.abs(e - e_simt)) <= 1e-5 * np.max(np.abs(e_simt))

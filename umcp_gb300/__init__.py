@@ -49,6 +49,7 @@ class Params(C.Structure):
     _fields_ = [
         ("kc", C.c_double), ("KA", C.c_double), ("kg", C.c_double), ("k_reg", C.c_double),
         ("temperature", C.c_double), ("precision", C.c_int), ("lipid_directives", C.c_char_p),
+        ("face_kernel", C.c_int),
     ]
 
 
@@ -262,10 +263,16 @@ def _ip(a: np.ndarray | None):
     return a.ctypes.data_as(_I)
 
 
-def params(kc=14.0, KA=0.215, kg=0.0, k_reg=0.0, temperature=298.0, precision=FP64, lipids: str | None = None) -> Params:
+SIMT = 0          # Params.face_kernel: the FP32 SIMT face kernel (default)
+TENSOR_CORES = 1  # regular faces of the precision form through tcgen05 (3xTF32 contractions)
+
+
+def params(kc=14.0, KA=0.215, kg=0.0, k_reg=0.0, temperature=298.0, precision=FP64, lipids: str | None = None,
+           face_kernel: int = SIMT) -> Params:
     p = Params()
     _check(library().umcp_params_default(C.byref(p)))
     p.kc, p.KA, p.kg, p.k_reg, p.temperature, p.precision = kc, KA, kg, k_reg, temperature, precision
+    p.face_kernel = face_kernel
     p._lipid_bytes = lipids.encode() if lipids else None  # keep alive
     p.lipid_directives = p._lipid_bytes
     return p

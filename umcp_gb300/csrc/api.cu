@@ -61,6 +61,7 @@ extern "C" umcp_status umcp_params_default(umcp_params *p) {
   p->temperature = 298.0;  // src/input.C:71
   p->precision = UMCP_FP64;
   p->lipid_directives = nullptr;
+  p->face_kernel = 0;
   return UMCP_OK;
 }
 
@@ -369,7 +370,7 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   }
   const int nt = PL.ntypes;
   std::vector<std::vector<int>> vslots(ME.nv);  // slots touching each vertex, ascending
-  int face_base = 0, slot_base = 0, block_base = 0;
+  int face_base = 0, slot_base = 0, block_base = 0, block_rows = 0;
   for (const Src &s : srcs) {
     auto G = std::make_unique<Group>();
     const PatchBasis &B = *s.B;
@@ -403,10 +404,11 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     for (int p = 0; p < G->npt; ++p)
       for (int k = 0; k < 5; ++k)
         for (int x = 0; x < G->ncp; ++x) basis[((size_t)p * 5 + k) * ncpp + x] = B.at(k + 1, p, x);
-    G->nblocks = (prm->precision == UMCP_FP64) ? face_blocks<double>(G->nfaces, G->ncp, G->npt)
-                                               : face_blocks<float>(G->nfaces, G->ncp, G->npt);
+    G->tc = prm->precision == UMCP_FP32_CENTRED && prm->face_kernel == 1 && G->ncp == 12 && G->npt == 15;
+    G->nblocks = group_blocks(prm->precision, G->tc, G->ncp, G->npt, G->nfaces);
     G->block_base = block_base;
     block_base += G->nblocks;
+    block_rows += group_block_rows(prm->precision, G->ncp, G->npt, G->nfaces);
     UMCP_CUDA(upload(G->cp, cp));
     UMCP_CUDA(upload(G->g0, g0));
     UMCP_CUDA(upload(G->rr0, rr0));
@@ -441,7 +443,7 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   }
   UMCP_CUDA(upload(m->off, off));
   m->nblocks = block_base;
-  UMCP_CUDA(m->blockpart.alloc((size_t)(block_base > 0 ? block_base : 1) * 6 * sizeof(double)));
+  UMCP_CUDA(m->blockpart.alloc((size_t)(block_rows > 0 ? block_rows : 1) * 6 * sizeof(double)));
   UMCP_CUDA(cudaMemset(m->blockpart.p, 0, m->blockpart.bytes));
   const size_t elem = (m->precision == UMCP_FP64) ? sizeof(double) : sizeof(float);
   UMCP_CUDA(m->partial.alloc((size_t)slot_base * 3 * elem));
@@ -498,6 +500,17 @@ extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *
   mesh->drop_graphs();
   if (mesh->batch) batch_mesh_changed(mesh->batch);  // its job entry holds the parameters
   return UMCP_OK;
+}
+
+int umcp::group_blocks(int precision, bool tc, int ncp, int npt, int nfaces) {
+  if (tc) return face_blocks_tc(nfaces);
+  return precision == UMCP_FP64 ? face_blocks<double>(nfaces, ncp, npt) : face_blocks<float>(nfaces, ncp, npt);
+}
+
+int umcp::group_block_rows(int precision, int ncp, int npt, int nfaces) {
+  int b = group_blocks(precision, false, ncp, npt, nfaces);
+  if (precision == UMCP_FP32_CENTRED && ncp == 12 && npt == 15) b = std::max(b, face_blocks_tc(nfaces));
+  return b;
 }
 
 // Arguments of the area/volume kernels for state d_r.
@@ -570,9 +583,21 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
     L.weight = G->weight.as<double>();
     L.dudv = G->dudv;
     L.irregular = G->irregular;
-    cudaError_t e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(),
-                                    m->rlo.as<float>(), m->partial.as<T>(), m->blockpart.as<double>(),
-                                    m->status.as<int>(), G->nblocks, (last && fin) ? *fin : none, s);
+    cudaError_t e;
+    if constexpr (sizeof(T) == 4) {
+      if (G->tc)
+        e = launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
+                            m->partial.as<float>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+                            (last && fin) ? *fin : none, s);
+      else
+        e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
+                            m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+                            (last && fin) ? *fin : none, s);
+    } else {
+      e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
+                          m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+                          (last && fin) ? *fin : none, s);
+    }
     if (e != cudaSuccess) return e;
   }
   if (geo) return launch_geo_grad<T>(GA, m->partial.as<T>(), s);
@@ -617,6 +642,7 @@ static umcp_status check_status(umcp_mesh *m) {
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
   if (st & kStatusNonFinite) return fail(UMCP_ERR_NONFINITE, "non-finite energy (the reference stops with \"nan en.\")");
   if (st & kStatusDiverged) return fail(UMCP_ERR_DIVERGED, "energy rose above the divergence threshold");
+  if (st & kStatusTimeout) return fail(UMCP_ERR_TIMEOUT, "a tensor-core wait in the face pass gave up");
   return UMCP_OK;
 }
 
@@ -704,7 +730,7 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
          nf * B.ncp * 4 + (size_t)B.npt * B.ncp * 8;
     if (f32) b += 2 * nf * B.npt * 4 + nf * 3 * 4;
     slots += nf * B.ncp;
-    nblocks += f32 ? face_blocks<float>((int)nf, B.ncp, B.npt) : face_blocks<double>((int)nf, B.ncp, B.npt);
+    nblocks += group_block_rows(precision, B.ncp, B.npt, (int)nf);
   };
   group(PL.regular, PL.reg_faces.size());
   for (int val : {5, 7}) {
@@ -1123,7 +1149,9 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
     L.dudv = G->dudv;
     L.irregular = G->irregular;
     const FinishArgs &f = (gi + 1 == m->groups.size()) ? fin : none;
-    cudaError_t e = fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
+    cudaError_t e = (fp32 && G->tc) ? launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, rhi, rlo,
+                                                       (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
+                    : fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
                                                (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
                          : launch_faces<double>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
                                                 (double *)(base + off_partial), blockpart, status, G->nblocks, f, s);

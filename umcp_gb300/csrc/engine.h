@@ -32,6 +32,7 @@ struct DevBuf {
 
 struct Group {
   int ncp = 0, npt = 0, nfaces = 0, slot_base = 0, irregular = 0;
+  bool tc = false;                  // regular faces of the precision form on the tensor cores
   int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
   double dudv = 0.5;
   DevBuf cp, g0, rr0, comp, basis, weight, dest;
@@ -147,6 +148,12 @@ umcp_status make_step_args(const umcp_mesh *m, const umcp_integrator *it, StepAr
 // first); a batch rebuilds its tables after a job's mesh changed.
 void batch_forget_mesh(umcp_batch *b, umcp_mesh *m);
 void batch_mesh_changed(umcp_batch *b);
+
+// Block-partial rows of a group's face launch, and the rows its footprint
+// reserves (the larger of the two kernels' grids, so the footprint does not
+// depend on the kernel choice).
+int group_blocks(int precision, bool tc, int ncp, int npt, int nfaces);
+int group_block_rows(int precision, int ncp, int npt, int nfaces);
 
 inline uint32_t pack_cp(int v, const int8_t img[3]) {
   int code = (img[0] + 1) + 3 * (img[1] + 1) + 9 * (img[2] + 1);

@@ -85,6 +85,21 @@ __device__ __forceinline__ T dot(const Vec3<T> &a, const Vec3<T> &b) {
   return a.x * b.x + a.y * b.y + a.z * b.z;
 }
 
+// FP32 reciprocals for the pointwise step: the hardware estimates refined by
+// one Newton step (y <- y (3 - x y^2) / 2 for 1/sqrt(x), y <- y (2 - x y) for
+// 1/x), about 1 ulp, instead of the longer correctly rounded sequences.
+__device__ __forceinline__ float rsqrt_nr(float x) {
+  const float y = rsqrtf(x);
+  return y * (1.5f - 0.5f * x * y * y);
+}
+__device__ __forceinline__ float rcp_nr(float x) {
+  const float y = __fdividef(1.f, x);
+  return y * (2.f - x * y);
+}
+// a / b: a division in FP64; a times the reciprocal ib already formed in FP32
+__device__ __forceinline__ double qdiv(double a, double b, double) { return a / b; }
+__device__ __forceinline__ float qdiv(float a, float, float ib) { return a * ib; }
+
 // Pointwise energy and adjoint at one quadrature point. Returns energy parts
 // (area, curvature, angle) and writes dE/d{Ru,Rv,Suu,Suv,Svv} into Kb, and
 // the angle-term part of dE/d{Ru,Rv} into Kreg (needed only for the box-scale
@@ -98,33 +113,50 @@ __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T r
   T W = dot(m, m);
   T E11 = dot(Ru, Ru), E12 = dot(Ru, Rv), E22 = dot(Rv, Rv);
   T l = dot(m, Suu), k = dot(m, Suv), n = dot(m, Svv);
-  T g = sqrt(W);
-  T iW = T(1) / W;
-  T ig3 = iW / g;  // W^-3/2
+  // g = sqrt(W), 1/W, W^-3/2, sqrt(E11 E22) and the reciprocals of g, g0,
+  // sqrt(E11 E22), E11, E22 (FP32: from two reciprocal square roots and one
+  // reciprocal; FP64: divisions, ib unused)
+  T g, iW, ig3, sEE, ig = 0, ig0 = 0, isEE = 0, iE11 = 0, iE22 = 0;
+  if constexpr (sizeof(T) == 4) {
+    ig = rsqrt_nr(W);
+    g = W * ig;
+    iW = ig * ig;
+    ig3 = iW * ig;
+    isEE = rsqrt_nr(E11 * E22);
+    sEE = E11 * E22 * isEE;
+    iE11 = E22 * isEE * isEE;
+    iE22 = E11 * isEE * isEE;
+    ig0 = rcp_nr(g0);
+  } else {
+    g = sqrt(W);
+    iW = T(1) / W;
+    ig3 = iW / g;  // W^-3/2
+    sEE = sqrt(E11 * E22);
+  }
   T Tt = l * E22 - T(2) * k * E12 + n * E11;
   T Q = l * n - k * k;
   T H = -Tt * ig3;
   T Kg = Q * iW * iW - T(kSafety * 0.25);
   T dH = H - Hbar;
-  T sEE = sqrt(E11 * E22);
-  T val = E12 / sEE;
+  T val = qdiv(E12, sEE, isEE);
   T dv = val - rr0;
   T dg = g - g0;
   *ec = T(0.25) * kc * w * (P2 * dH * dH + Pres) + dudv * g0 * w * kg * Kg;
-  *ea = dudv * w * KA * dg * dg / g0;
+  *ea = qdiv(dudv * w * KA * dg * dg, g0, ig0);
   *er = k_reg * dv * dv;
   // adjoints
   T Hb = T(0.5) * kc * w * P2 * dH;
   T Kb_ = dudv * g0 * w * kg;
-  T gb = T(2) * dudv * w * KA * dg / g0;
+  T gb = qdiv(T(2) * dudv * w * KA * dg, g0, ig0);
   T vb = T(2) * k_reg * dv;
   T Tb = -Hb * ig3;
   T Qb = Kb_ * iW * iW;
-  T Wb = Hb * T(1.5) * Tt * ig3 * iW - T(2) * Kb_ * Q * iW * iW * iW + gb / (T(2) * g);
+  T Wb = Hb * T(1.5) * Tt * ig3 * iW - T(2) * Kb_ * Q * iW * iW * iW + qdiv(gb, T(2) * g, T(0.5) * ig);
   T lb = Tb * E22 + Qb * n;
   T kb = T(-2) * Tb * E12 - T(2) * Qb * k;
   T nb = Tb * E11 + Qb * l;
-  T rE11 = T(-0.5) * vb * val / E11, rE12 = vb / sEE, rE22 = T(-0.5) * vb * val / E22;
+  T rE11 = qdiv(T(-0.5) * vb * val, E11, iE11), rE12 = qdiv(vb, sEE, isEE),
+    rE22 = qdiv(T(-0.5) * vb * val, E22, iE22);
   T E11b = Tb * n + rE11;
   T E12b = T(-2) * Tb * k + rE12;
   T E22b = Tb * l + rE22;

@@ -9,7 +9,7 @@
 namespace umcp {
 
 // Status bits written by kernels into the mesh's device status word.
-enum : int { kStatusNonFinite = 1, kStatusDiverged = 2 };
+enum : int { kStatusNonFinite = 1, kStatusDiverged = 2, kStatusTimeout = 4 };
 
 // Where and how the block partials of a face pass are summed (see
 // launch_finish). done: device counter of finished blocks, zero between
@@ -73,6 +73,14 @@ template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
                          const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
                          int *status, int grid, const FinishArgs &fin, cudaStream_t s);
+
+// The regular faces of the precision form on the tensor cores (face_tc_kernel):
+// the same outputs as launch_faces<float> for ncp 12 / npt 15, in 128-face
+// tiles; grid from face_blocks_tc.
+int face_blocks_tc(int nfaces);
+cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev::SurfaceParams &P, const double *r,
+                            const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
+                            int grid, const FinishArgs &fin, cudaStream_t s);
 
 // hi[i] + lo[i] = r[i] to about 2^-48 relative (the precision form's positions).
 cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s);

@@ -1,5 +1,6 @@
 // Kernels of the membrane-surface hot path. See kernels.cuh for the model
 // and launch.h for the contracts.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -364,6 +365,533 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
       __threadfence();
       static_assert(sizeof(sm.Tc) >= sizeof(double) * 6 * NT, "finish scratch must fit in the transpose buffer");
       finish_sums<NT>(fin, blockpart, reinterpret_cast<double(*)[NT]>(&sm.Tc[0][0][0]));
+      if (threadIdx.x == 0) *fin.done = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- tensor-core face pass
+//
+// Regular faces in the precision form, with the two basis contractions on the
+// 5th-generation tensor cores (tcgen05, kind::tf32, 3xTF32 splits) and the
+// pointwise energy and adjoint on the FP32 pipes. A CTA owns a tile of 128
+// faces (the MMA's M; face = TMEM lane) and 256 threads: thread (face, half)
+// takes the half-th quadrature point of each 2-point chunk.
+//
+// Affine centring. The box splines reproduce affine functions, so with the
+// patch frame Eu = X2 - X0, Ev = X1 - X0 (control points 2 and 1 sit at
+// lattice (1,0) and (0,1)) and X'_x = X_x - X0 - u_x Eu - v_x Ev:
+//   Ru = Eu + sum b_u X',  Rv = Ev + sum b_v X',  S.. = sum b_.. X'.
+// X' is of the size of the curvature, not of the patch, so the TF32 split
+// errors scale with the curvature terms themselves.
+//
+// Per chunk j (points 2j, 2j+1):
+//   GEMM1_j  D1[f, n] = sum_x X'[f, x] B1_j[n, x]      n = 8 h + k (point 2j+h, kind k)
+//   pointwise: K -> energy terms, adjoint Kb (tcgen05.ld from D1, tcgen05.st into A2)
+//   GEMM2_j  D2[f, x] += sum_n A2[f, n] B2_j[x, n]    (A from tensor memory)
+// GEMM2_j and GEMM1_{j+1} are issued together behind one commit.
+namespace tc {
+// Tensor-core form of the regular-face pass (precision form, 12 control
+// points, 15 quadrature points). A CTA owns a tile of 128 faces, one face per
+// TMEM lane, and evaluates its points in four chunks of four; thread half h
+// (threads 128 h .. 128 h + 127) evaluates points 4 j + 2 h and 4 j + 2 h + 1
+// of chunk j and owns control points 8 h .. 8 h + 7 (those below 12).
+//
+// Per chunk, with fp16 operands split in two (x = hi + lo, about 22 bits) and
+// FP32 accumulation in TMEM:
+//   GEMM1  D1[face][n] = sum_k X'[face][k] B1[n][k]   per coordinate, K = 32, N = 48
+//   GEMM2  D2[face][n] = sum_k Kb[face][k] B2[n][k]   per coordinate, K = 48, N = 32
+// X' are the affine-centred control points, Kb the pointwise adjoints. The
+// three products of a split (hi hi, lo hi, hi lo) come out of one pass:
+// A = [a_hi | a_lo] along K and B's columns [b_hi | b_lo] along N, the lo-lo
+// block left zero. Each instruction costs about the same time whatever its N,
+// so the contractions are laid out for the fewest instructions: 6 (GEMM1) +
+// 9 (GEMM2) per chunk, 60 per tile.
+//
+// Scaling: every A row is scaled by a power of two that puts its largest
+// magnitude in [2^13, 2^14) (per face, coordinate and, for Kb, chunk), the
+// basis by 2^8, so neither fp16 half of an operand leaves fp16's normal range
+// in a way that costs accuracy. D2 is read back per chunk and summed in
+// registers, which lets each chunk's Kb carry its own scale.
+constexpr int kThreads = 256, kFaces = 128, kNpt = 15, kNcp = 12, kChunks = 4;
+constexpr int kN1 = 48, kK1 = 32, kN2 = 32, kK2 = 48;
+constexpr int kSbo1 = kK1 / 8 * 128, kSbo2 = kK2 / 8 * 128;  // bytes between 8-row core-matrix groups
+constexpr uint32_t kTmemCols = 256, kD1 = 0, kD2 = 3 * kN1;  // TMEM column bases
+constexpr float kBasisScale = 256.f, kInvBasisScale = 1.f / 256.f;
+// lattice position of control point x in the regular patch (ceff order)
+__constant__ int kLatU[12] = {0, 0, 1, 1, 0, -1, -1, -1, 0, 1, 2, 2};
+__constant__ int kLatV[12] = {0, 1, 0, -1, -1, 0, 1, 2, 2, 1, 0, -1};
+
+struct Smem {
+  uint4 A1[3][kFaces * kK1 / 8];  // X' (hi at k 0..11, lo at k 16..27), K-major core matrices of 8 rows x 16 B
+  uint4 A2[3][kFaces * kK2 / 8];  // Kb: thread half h's slots at k 24 h .. 24 h + 23
+  uint4 B1[kChunks][kN1 * kK1 / 8];
+  uint4 B2[kChunks][kN2 * kK2 / 8];
+  float xmax[2][3][kFaces];       // per-row maxima exchanged between the two thread halves
+  float W[16];
+  uint64_t mbar;
+  uint32_t tmem;
+  int abort;
+};
+constexpr size_t kSmemBytes = sizeof(Smem) + 1024;
+
+// byte offset of element (row, k) of a K-major fp16 operand whose 8-row groups are sbo bytes apart
+__host__ __device__ constexpr int core_off(int row, int k, int sbo) {
+  return (row >> 3) * sbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+// GEMM1 column of thread half h's slot s (s < 20): slots 0..15 at 16 h + s,
+// slots 16..19 at 32 + 8 h + s - 16, so both halves read them with one x16
+// and one x8 load at aligned columns.
+__host__ __device__ constexpr int d1_col(int h, int s) { return s < 16 ? 16 * h + s : 32 + 8 * h + (s - 16); }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: K-major, no swizzle, 128 B between K-adjacent core matrices
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+// instruction descriptor: D F32, A and B F16, both K-major, M = 128
+__host__ __device__ constexpr uint32_t idesc(uint32_t n) { return (1u << 4) | ((n >> 3) << 17) | ((128u >> 4) << 24); }
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+               ::"r"(d), "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void commit(uint64_t *mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)));
+}
+// Bounded wait on the mbarrier's phase; false when it gave up.
+__device__ __forceinline__ bool wait_phase(uint64_t *mbar, uint32_t phase) {
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 24) && !done; ++it)
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(smem_u32(mbar)), "r"(phase));
+  return done != 0;
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
+
+// TMEM loads of 16 + 8 and 8 + 8 consecutive columns of this warp's 32 lanes;
+// the wait is inside the same statement, so no use of a result can move above it.
+__device__ __forceinline__ void ld16_8(uint32_t ta, uint32_t tb, float v[24]) {
+  uint32_t r[24];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%24];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%25];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+      : "r"(ta), "r"(tb));
+#pragma unroll
+  for (int i = 0; i < 24; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void ld8_8(uint32_t ta, uint32_t tb, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(ta), "r"(tb));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 2^e with m * 2^e in [2^13, 2^14) for a finite m > 0 (and its inverse); for
+// m = 0 or tiny m the largest scale whose inverse is a normal float; an
+// infinite or NaN m gives a small scale, so the values stay non-finite.
+__device__ __forceinline__ void pow2_scale(float m, float &s, float &inv) {
+  const int e = (int)((__float_as_uint(m) >> 23) & 0xFFu);
+  const int f = e == 0 ? 253 : min(253, 267 - e);  // biased exponent of the scale
+  s = __uint_as_float((uint32_t)f << 23);
+  inv = __uint_as_float((uint32_t)(254 - f) << 23);
+}
+__device__ __forceinline__ uint32_t pack2(__half a, __half b) {
+  return (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
+}
+// x (already scaled) = hi + lo in fp16
+__device__ __forceinline__ void split16(float x, __half &hi, __half &lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
+}
+
+// CTA set-up: mbarrier, TMEM, the basis operands of every chunk, the weights.
+__device__ void setup(Smem &sm, const double *__restrict__ basis, const double *__restrict__ weight) {
+  const int tid = threadIdx.x;
+  // fp16 hi or lo part of the scaled basis value of point p, derivative d, control point x
+  auto bval = [&](int p, int d, int x, bool lo) -> __half {
+    const double b = basis[((size_t)p * 5 + d) * kNcp + x] * (double)kBasisScale;
+    const __half hi = __float2half_rn((float)b);
+    return lo ? __float2half_rn((float)(b - (double)__half2float(hi))) : hi;
+  };
+  __half *b1 = reinterpret_cast<__half *>(&sm.B1[0][0]);
+  for (int e = tid; e < kChunks * kN1 * kK1; e += kThreads) {
+    const int j = e / (kN1 * kK1), n = (e / kK1) % kN1, k = e % kK1;
+    const int h = n < 32 ? n >> 4 : (n - 32) >> 3, s = n < 32 ? n & 15 : 16 + ((n - 32) & 7);
+    const int x = k & 15;
+    __half v = __float2half_rn(0.f);
+    if (s < 20 && x < kNcp) {
+      const int q = (s % 10) / 5, d = s % 5, p = 4 * j + 2 * h + q;
+      if (p < kNpt) {
+        if (s < 10) v = bval(p, d, x, false);  // (a_hi + a_lo) b_hi
+        else if (k < 16) v = bval(p, d, x, true);  // a_hi b_lo
+      }
+    }
+    b1[(size_t)j * kN1 * kK1 + core_off(n, k, kSbo1) / 2] = v;
+  }
+  __half *b2 = reinterpret_cast<__half *>(&sm.B2[0][0]);
+  for (int e = tid; e < kChunks * kN2 * kK2; e += kThreads) {
+    const int j = e / (kN2 * kK2), n = (e / kK2) % kN2, k = e % kK2;
+    const int x = n & 15, h = k / 24, s = k % 24;
+    __half v = __float2half_rn(0.f);
+    if (x < kNcp && s < 20) {
+      const int q = (s % 10) / 5, d = s % 5, p = 4 * j + 2 * h + q;
+      if (p < kNpt) {
+        if (s < 10) v = bval(p, d, x, n >= 16);  // a_hi rows: [b_hi | b_lo]
+        else if (n < 16) v = bval(p, d, x, false);  // a_lo rows: [b_hi | 0]
+      }
+    }
+    b2[(size_t)j * kN2 * kK2 + core_off(n, k, kSbo2) / 2] = v;
+  }
+  if (tid < 16) sm.W[tid] = tid < kNpt ? (float)weight[tid] : 0.f;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sm.mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    sm.abort = 0;
+  }
+  if ((tid >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  fence_before();
+  __syncthreads();
+  fence_after();
+}
+
+__device__ void teardown(Smem &sm, uint32_t phase, bool pending) {
+  // An aborted tile may leave MMAs in flight: give them a bounded wait before
+  // the tensor memory they write is freed.
+  if (pending && threadIdx.x == 0) wait_phase(&sm.mbar, phase);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(sm.tmem), "r"(kTmemCols));
+}
+
+__device__ __forceinline__ void issue_gemm1(Smem &sm, uint32_t tmem, int j) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int ks = 0; ks < kK1 / 16; ++ks)
+      mma(tmem + kD1 + kN1 * c, sdesc(smem_u32(sm.A1[c]) + 256 * ks, kSbo1), sdesc(smem_u32(sm.B1[j]) + 256 * ks, kSbo1),
+          idesc(kN1), ks);
+}
+__device__ __forceinline__ void issue_gemm2(Smem &sm, uint32_t tmem, int j) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int ks = 0; ks < kK2 / 16; ++ks)
+      mma(tmem + kD2 + kN2 * c, sdesc(smem_u32(sm.A2[c]) + 256 * ks, kSbo2), sdesc(smem_u32(sm.B2[j]) + 256 * ks, kSbo2),
+          idesc(kN2), ks);
+}
+
+// Adds chunk D2 (scaled by inv, per coordinate) into G: the hi- and lo-basis columns of this thread's control points.
+__device__ __forceinline__ void gather_d2(uint32_t tmem, uint32_t lane_base, int h, const float inv[3], float G[3][8]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float v[16];
+    ld8_8(tmem + lane_base + kD2 + kN2 * c + 8 * h, tmem + lane_base + kD2 + kN2 * c + 16 + 8 * h, v);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) G[c][i] += (v[i] + v[8 + i]) * inv[c];
+  }
+}
+
+// One tile of up to 128 faces [first, first + count) of source S. Returns
+// false if a wait gave up (the CTA then stops).
+__device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const float alpha[3], const float ialpha[3],
+                     const Moduli<float> &mod, float dudv, int first, int count, float *__restrict__ partial,
+                     HalfWarpSums<float> &acc, uint32_t &phase) {
+  const int tid = threadIdx.x, fs = tid & (kFaces - 1), h = tid >> 7;
+  const uint32_t tmem = sm.tmem, lane_base = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
+  const bool active = fs < count;
+  const int f = first + fs;
+  const int nx = h == 0 ? 8 : kNcp - 8;  // control points of this thread
+  float Eu[3] = {0, 0, 0}, Ev[3] = {0, 0, 0}, sA[3], iA[3];
+  float P2 = 0, Hbar = 0, Pres = 0;
+  {
+    float xp[8][3];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) xp[i][0] = xp[i][1] = xp[i][2] = 0.f;
+    if (active) {
+      const uint32_t *cp = S.cp + (size_t)f * kNcp;
+      // the corner (control point 0) is in the home image: coordinates are relative to its hi/lo pair
+      const int v0 = (int)(__ldg(&cp[0]) & kVertexMask);
+      float chi[3], clo[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        chi[c] = S.rhi[3 * (size_t)v0 + c];
+        clo[c] = S.rlo[3 * (size_t)v0 + c];
+      }
+      auto local = [&](uint32_t packed, float out[3]) {
+        const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+        const int im[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            float t, e;
+            two_sum(sh, (float)im[d] * P.box_hi[d][c], t, e);
+            sh = t;
+            she += e;
+            shl += (float)im[d] * P.box_lo[d][c];
+          }
+          float s1, e1, s2, e2;
+          const float hi = S.rhi[3 * (size_t)v + c], lo = S.rlo[3 * (size_t)v + c];
+          two_sum(hi, sh, s1, e1);
+          two_sum(s1, -chi[c], s2, e2);
+          out[c] = alpha[c] * (s2 + ((e1 + e2) + ((lo - clo[c]) + (she + shl))));
+        }
+      };
+      local(__ldg(&cp[1]), Ev);  // lattice (0,1)
+      local(__ldg(&cp[2]), Eu);  // lattice (1,0)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (i < nx) {
+          const int x = 8 * h + i;
+          float xl[3];
+          local(__ldg(&cp[x]), xl);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) xp[i][c] = xl[c] - (float)kLatU[x] * Eu[c] - (float)kLatV[x] * Ev[c];
+        }
+      }
+      P2 = S.compf[3 * (size_t)f];
+      Hbar = S.compf[3 * (size_t)f + 1];
+      Pres = S.compf[3 * (size_t)f + 2];
+    }
+    // one scale per face and coordinate, from the largest |X'| of both halves
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float m = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) m = fmaxf(m, fabsf(xp[i][c]));
+      sm.xmax[h][c][fs] = m;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pow2_scale(fmaxf(sm.xmax[0][c][fs], sm.xmax[1][c][fs]), sA[c], iA[c]);
+      uint32_t whi[4], wlo[4];
+#pragma unroll
+      for (int i = 0; i < 8; i += 2) {
+        __half h0, l0, h1, l1;
+        split16(xp[i][c] * sA[c], h0, l0);
+        split16(xp[i + 1][c] * sA[c], h1, l1);
+        whi[i / 2] = pack2(h0, h1);
+        wlo[i / 2] = pack2(l0, l1);
+      }
+      sm.A1[c][core_off(fs, 8 * h, kSbo1) / 16] = make_uint4(whi[0], whi[1], whi[2], whi[3]);
+      sm.A1[c][core_off(fs, 16 + 8 * h, kSbo1) / 16] = make_uint4(wlo[0], wlo[1], wlo[2], wlo[3]);
+      iA[c] *= kInvBasisScale;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (tid == 0) {
+    issue_gemm1(sm, tmem, 0);
+    commit(&sm.mbar);
+  }
+  float e3[3] = {0, 0, 0}, G[3][8], iK[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) G[c][i] = 0.f;
+  bool ok = true;
+#pragma unroll 1
+  for (int j = 0; j < kChunks; ++j) {
+    float g0[2] = {1.f, 1.f}, rr0[2] = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int p = 4 * j + 2 * h + q;
+      if (active && p < kNpt) {
+        g0[q] = S.g0f[(size_t)f * kNpt + p];
+        rr0[q] = S.rr0f[(size_t)f * kNpt + p];
+      }
+    }
+    ok = wait_phase(&sm.mbar, phase) && ok;
+    phase ^= 1u;
+    fence_after();
+    if (j > 0) gather_d2(tmem, lane_base, h, iK, G);
+    // the five contractions of both points, per coordinate: slot hi + slot lo
+    Vec3<float> K[2][5];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float v[24];
+      ld16_8(tmem + lane_base + kD1 + kN1 * c + 16 * h, tmem + lane_base + kD1 + kN1 * c + 32 + 8 * h, v);
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          const int shi = 5 * q + d, slo = 10 + 5 * q + d;
+          const float val = (v[shi] + v[slo]) * iA[c];
+          (c == 0 ? K[q][d].x : c == 1 ? K[q][d].y : K[q][d].z) = val;
+        }
+    }
+    float kbv[3][2][5], km[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int p = 4 * j + 2 * h + q;
+      K[q][0].x += Eu[0]; K[q][0].y += Eu[1]; K[q][0].z += Eu[2];
+      K[q][1].x += Ev[0]; K[q][1].y += Ev[1]; K[q][1].z += Ev[2];
+      Vec3<float> Kb[5], Kreg[2];
+      if (active && p < kNpt) {
+        float ea = 0, ec = 0, er = 0;
+        point_adjoint<float>(K[q], sm.W[p], g0[q], rr0[q], dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg,
+                             &ea, &ec, &er, Kb, Kreg);
+        e3[0] += ea; e3[1] += ec; e3[2] += er;
+      } else {
+#pragma unroll
+        for (int d = 0; d < 5; ++d) Kb[d] = {0.f, 0.f, 0.f};
+      }
+#pragma unroll
+      for (int d = 0; d < 5; ++d) {
+        kbv[0][q][d] = Kb[d].x;
+        kbv[1][q][d] = Kb[d].y;
+        kbv[2][q][d] = Kb[d].z;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int d = 0; d < 5; ++d) km[c] = fmaxf(km[c], fabsf(kbv[c][q][d]));
+      sm.xmax[h][c][fs] = km[c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float sK;
+      pow2_scale(fmaxf(sm.xmax[0][c][fs], sm.xmax[1][c][fs]), sK, iK[c]);
+      iK[c] *= kInvBasisScale;
+      __half hv[10], lv[10];
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int d = 0; d < 5; ++d) split16(kbv[c][q][d] * sK, hv[5 * q + d], lv[5 * q + d]);
+      const __half z = __float2half_rn(0.f);
+      // slots 0..9 hi, 10..19 lo, 20..23 zero
+      uint4 *row = sm.A2[c];
+      row[core_off(fs, 24 * h, kSbo2) / 16] =
+          make_uint4(pack2(hv[0], hv[1]), pack2(hv[2], hv[3]), pack2(hv[4], hv[5]), pack2(hv[6], hv[7]));
+      row[core_off(fs, 24 * h + 8, kSbo2) / 16] =
+          make_uint4(pack2(hv[8], hv[9]), pack2(lv[0], lv[1]), pack2(lv[2], lv[3]), pack2(lv[4], lv[5]));
+      row[core_off(fs, 24 * h + 16, kSbo2) / 16] =
+          make_uint4(pack2(lv[6], lv[7]), pack2(lv[8], lv[9]), pack2(z, z), pack2(z, z));
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+      issue_gemm2(sm, tmem, j);
+      if (j + 1 < kChunks) issue_gemm1(sm, tmem, j + 1);
+      commit(&sm.mbar);
+    }
+  }
+  ok = wait_phase(&sm.mbar, phase) && ok;
+  phase ^= 1u;
+  if (__syncthreads_or(!ok)) return false;
+  fence_after();
+  gather_d2(tmem, lane_base, h, iK, G);
+  // ---- gradient partials of this thread's control points and dE/dalpha;
+  // X' comes back from the GEMM1 operand (hi + lo), the lattice part from Eu, Ev
+  float da[3] = {0, 0, 0};
+  if (active) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const uint4 wh = sm.A1[c][core_off(fs, 8 * h, kSbo1) / 16], wl = sm.A1[c][core_off(fs, 16 + 8 * h, kSbo1) / 16];
+      const uint32_t hw[4] = {wh.x, wh.y, wh.z, wh.w}, lw[4] = {wl.x, wl.y, wl.z, wl.w};
+      const float ia = iA[c] * kBasisScale;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (i < nx) {
+          const int x = 8 * h + i;
+          const __half hh = __ushort_as_half((unsigned short)(hw[i / 2] >> (16 * (i & 1))));
+          const __half ll = __ushort_as_half((unsigned short)(lw[i / 2] >> (16 * (i & 1))));
+          const float xl = (__half2float(hh) + __half2float(ll)) * ia + (float)kLatU[x] * Eu[c] + (float)kLatV[x] * Ev[c];
+          const int dst = __ldg(&S.dest[(size_t)f * kNcp + x]);
+          partial[3 * (size_t)dst + c] = alpha[c] * G[c][i];
+          da[c] += G[c][i] * xl * ialpha[c];
+        }
+      }
+    }
+  }
+  acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+  acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
+  // the next tile overwrites A1, A2 and the maxima, and its MMAs D1 and D2: everyone is done with them
+  fence_before();
+  __syncthreads();
+  fence_after();
+  return true;
+}
+
+// Fixed-order block sum of the six per-thread sums into out[6] (global). The
+// reduction buffer lies over the Kb operand, which no MMA reads any more.
+__device__ void block_sums(Smem &sm, const HalfWarpSums<float> &acc, double *out) {
+  double(*red)[6] = reinterpret_cast<double(*)[6]>(&sm.A2[0][0]);
+  for (int q = 0; q < 6; ++q) red[threadIdx.x][q] = acc.get(q);
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double s = 0;
+    for (int t = 0; t < kThreads; ++t) s += red[t][threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+static_assert(sizeof(double) * 6 * kThreads <= sizeof(uint4) * 3 * kFaces * kK2 / 8, "reduction buffer");
+}  // namespace tc
+
+// Single mesh: persistent CTAs over the 128-face tiles of the regular group.
+__global__ void __launch_bounds__(tc::kThreads, 2)
+    face_tc_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
+                   const float *__restrict__ rhi, const float *__restrict__ rlo, float *__restrict__ partial,
+                   double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
+  extern __shared__ uint8_t tc_smem_raw[];
+  tc::Smem &sm = *reinterpret_cast<tc::Smem *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~(uintptr_t)1023);
+  tc::setup(sm, L.basis, L.weight);
+  const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
+  const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+  const Moduli<float> mod(P);
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
+  HalfWarpSums<float> acc;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int ntiles = (L.nfaces + tc::kFaces - 1) / tc::kFaces;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int first = t * tc::kFaces;
+    ok = tc::tile(sm, src, P, alpha, ialpha, mod, (float)L.dudv, first, min(tc::kFaces, L.nfaces - first), partial,
+                  acc, phase);
+  }
+  if (!ok && threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+  tc::teardown(sm, phase, !ok);
+  tc::block_sums(sm, acc, blockpart + 6 * (size_t)(L.block_base + blockIdx.x));
+  if (fin.done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      finish_sums<tc::kThreads>(fin, blockpart, reinterpret_cast<double(*)[tc::kThreads]>(&sm.A2[0][0]));
       if (threadIdx.x == 0) *fin.done = 0u;
     }
   }
@@ -1137,5 +1665,37 @@ cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s) {
 }
 template cudaError_t launch_geo_grad<double>(const GeoArgs &, double *, cudaStream_t);
 template cudaError_t launch_geo_grad<float>(const GeoArgs &, float *, cudaStream_t);
+
+}  // namespace umcp
+
+namespace umcp {
+
+int face_blocks_tc(int nfaces) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  const int tiles = (nfaces + dev::tc::kFaces - 1) / dev::tc::kFaces;
+  const int cap = 2 * sms;  // two CTAs per SM (shared memory and tensor memory)
+  return tiles < 1 ? 1 : (tiles < cap ? tiles : cap);
+}
+
+cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev::SurfaceParams &P, const double *r,
+                            const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
+                            int grid, const FinishArgs &fin, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(dev::face_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)dev::tc::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dev::face_tc_kernel<<<grid, dev::tc::kThreads, dev::tc::kSmemBytes, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart,
+                                                                           status, fin);
+  return cudaGetLastError();
+}
 
 }  // namespace umcp

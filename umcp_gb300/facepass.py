@@ -25,11 +25,14 @@ def main() -> None:
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--vesicles", type=int, default=0)
     ap.add_argument("--tile-faces", type=int, default=128)
+    ap.add_argument("--face-kernel", default="simt", choices=["tc", "simt"],
+                    help="regular faces of the FP32 form on the tensor cores or the SIMT kernel")
     args = ap.parse_args()
     if args.vesicles:
         return batch_main(args)
     prec = U.FP32_CENTRED if args.precision == "fp32" else U.FP64
-    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=prec)
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=prec,
+                   face_kernel=U.TENSOR_CORES if args.face_kernel == "tc" else U.SIMT)
     with tempfile.TemporaryDirectory() as td:
         path = Path(td) / "m.mesh"
         if args.icosphere:
