@@ -67,10 +67,10 @@ L2_BYTES = 129 * 1024 * 1024
 SM_COUNT, FP32_LANES_PER_SM = 152, 128
 # DRAM bytes per face of the batched face launches, from the ncu capture of
 # the first 64 vesicles of the workload (dram__bytes_read.sum +
-# dram__bytes_write.sum of the regular and valence-5 launches: 98.61 + 26.83
-# + 2.18 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled from
+# dram__bytes_write.sum of the regular and valence-5 launches: 98.78 + 26.00
+# + 2.17 + 0.00 MB over 392,960 faces); the benchmark's pass is scaled from
 # it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 127.63e6 / 392960
+BATCH_FACE_DRAM_BYTES_PER_FACE = 126.95e6 / 392960
 
 
 def parse_args():

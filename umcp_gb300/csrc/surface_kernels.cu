@@ -471,21 +471,8 @@ __device__ __forceinline__ bool wait_phase(uint64_t *mbar, uint32_t phase) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
 
-// TMEM loads of 16 + 8 and 8 + 8 consecutive columns of this warp's 32 lanes;
-// the wait is inside the same statement, so no use of a result can move above it.
-__device__ __forceinline__ void ld16_8(uint32_t ta, uint32_t tb, float v[24]) {
-  uint32_t r[24];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%24];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%25];\n"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
-      : "r"(ta), "r"(tb));
-#pragma unroll
-  for (int i = 0; i < 24; ++i) v[i] = __uint_as_float(r[i]);
-}
+// TMEM loads of 8 + 8 consecutive columns of this warp's 32 lanes; the wait is
+// inside the same statement, so no use of a result can move above it.
 __device__ __forceinline__ void ld8_8(uint32_t ta, uint32_t tb, float v[16]) {
   uint32_t r[16];
   asm volatile(
@@ -499,6 +486,23 @@ __device__ __forceinline__ void ld8_8(uint32_t ta, uint32_t tb, float v[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// The GEMM1 results of this thread's two points, all three coordinates: per
+// coordinate c, 16 + 8 columns at ta[c], tb[c], with one wait.
+__device__ __forceinline__ void ld_d1(const uint32_t ta[3], const uint32_t tb[3], float v[3][24]) {
+  uint32_t r[72];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%72];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%73];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39}, [%74];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40,%41,%42,%43,%44,%45,%46,%47}, [%75];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%76];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%64,%65,%66,%67,%68,%69,%70,%71}, [%77];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63]), "=r"(r[64]), "=r"(r[65]), "=r"(r[66]), "=r"(r[67]), "=r"(r[68]), "=r"(r[69]), "=r"(r[70]), "=r"(r[71])
+      : "r"(ta[0]), "r"(tb[0]), "r"(ta[1]), "r"(tb[1]), "r"(ta[2]), "r"(tb[2]));
+#pragma unroll
+  for (int i = 0; i < 72; ++i) v[i / 24][i % 24] = __uint_as_float(r[i]);
+}
 // 2^e with m * 2^e in [2^13, 2^14) for a finite m > 0 (and its inverse); for
 // m = 0 or tiny m the largest scale whose inverse is a normal float; an
 // infinite or NaN m gives a small scale, so the values stay non-finite.
@@ -508,13 +512,21 @@ __device__ __forceinline__ void pow2_scale(float m, float &s, float &inv) {
   s = __uint_as_float((uint32_t)f << 23);
   inv = __uint_as_float((uint32_t)(254 - f) << 23);
 }
-__device__ __forceinline__ uint32_t pack2(__half a, __half b) {
-  return (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
+// (a, b) as an fp16 pair, a in the low half
+__device__ __forceinline__ uint32_t cvt2(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
 }
-// x (already scaled) = hi + lo in fp16
-__device__ __forceinline__ void split16(float x, __half &hi, __half &lo) {
-  hi = __float2half_rn(x);
-  lo = __float2half_rn(x - __half2float(hi));
+// x0, x1 (already scaled) = hi + lo: hi rounded to 11 significant bits by
+// Veltkamp's split (factor 2^13 + 1; explicitly rounded operations, so
+// nothing is contracted), exact in fp16; lo = x - hi, exact in FP32 and
+// rounded to fp16.
+__device__ __forceinline__ void split_pair(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+  const float g0 = __fmul_rn(x0, 8193.f), g1 = __fmul_rn(x1, 8193.f);
+  const float h0 = __fsub_rn(g0, __fsub_rn(g0, x0)), h1 = __fsub_rn(g1, __fsub_rn(g1, x1));
+  hi = cvt2(h0, h1);
+  lo = cvt2(__fsub_rn(x0, h0), __fsub_rn(x1, h1));
 }
 
 // CTA set-up: mbarrier, TMEM, the basis operands of every chunk, the weights.
@@ -688,13 +700,7 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       pow2_scale(fmaxf(sm.xmax[0][c][fs], sm.xmax[1][c][fs]), sA[c], iA[c]);
       uint32_t whi[4], wlo[4];
 #pragma unroll
-      for (int i = 0; i < 8; i += 2) {
-        __half h0, l0, h1, l1;
-        split16(xp[i][c] * sA[c], h0, l0);
-        split16(xp[i + 1][c] * sA[c], h1, l1);
-        whi[i / 2] = pack2(h0, h1);
-        wlo[i / 2] = pack2(l0, l1);
-      }
+      for (int i = 0; i < 8; i += 2) split_pair(xp[i][c] * sA[c], xp[i + 1][c] * sA[c], whi[i / 2], wlo[i / 2]);
       sm.A1[c][core_off(fs, 8 * h, kSbo1) / 16] = make_uint4(whi[0], whi[1], whi[2], whi[3]);
       sm.A1[c][core_off(fs, 16 + 8 * h, kSbo1) / 16] = make_uint4(wlo[0], wlo[1], wlo[2], wlo[3]);
       iA[c] *= kInvBasisScale;
@@ -725,16 +731,23 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
         rr0[q] = S.rr0f[(size_t)f * kNpt + p];
       }
     }
-    ok = wait_phase(&sm.mbar, phase) && ok;
+    // warp 0 polls the mbarrier; the other warps sleep at the barrier
+    ok = !__syncthreads_or((tid >> 5) == 0 && !wait_phase(&sm.mbar, phase)) && ok;
     phase ^= 1u;
     fence_after();
     if (j > 0) gather_d2(tmem, lane_base, h, iK, G);
     // the five contractions of both points, per coordinate: slot hi + slot lo
     Vec3<float> K[2][5];
+    float v3[3][24];
+    {
+      const uint32_t t0 = tmem + lane_base + kD1;
+      const uint32_t ta[3] = {t0 + 16 * h, t0 + kN1 + 16 * h, t0 + 2 * kN1 + 16 * h};
+      const uint32_t tb[3] = {t0 + 32 + 8 * h, t0 + kN1 + 32 + 8 * h, t0 + 2 * kN1 + 32 + 8 * h};
+      ld_d1(ta, tb, v3);
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      float v[24];
-      ld16_8(tmem + lane_base + kD1 + kN1 * c + 16 * h, tmem + lane_base + kD1 + kN1 * c + 32 + 8 * h, v);
+      const float *v = v3[c];
 #pragma unroll
       for (int q = 0; q < 2; ++q)
 #pragma unroll
@@ -781,20 +794,17 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       float sK;
       pow2_scale(fmaxf(sm.xmax[0][c][fs], sm.xmax[1][c][fs]), sK, iK[c]);
       iK[c] *= kInvBasisScale;
-      __half hv[10], lv[10];
+      // slots 0..9 hi, 10..19 lo, 20..23 zero; slot 5 q + d is point q's derivative d
+      uint32_t hw[5], lw[5];
 #pragma unroll
-      for (int q = 0; q < 2; ++q)
-#pragma unroll
-        for (int d = 0; d < 5; ++d) split16(kbv[c][q][d] * sK, hv[5 * q + d], lv[5 * q + d]);
-      const __half z = __float2half_rn(0.f);
-      // slots 0..9 hi, 10..19 lo, 20..23 zero
+      for (int t = 0; t < 5; ++t) {
+        const int s0 = 2 * t, s1 = 2 * t + 1;
+        split_pair(kbv[c][s0 / 5][s0 % 5] * sK, kbv[c][s1 / 5][s1 % 5] * sK, hw[t], lw[t]);
+      }
       uint4 *row = sm.A2[c];
-      row[core_off(fs, 24 * h, kSbo2) / 16] =
-          make_uint4(pack2(hv[0], hv[1]), pack2(hv[2], hv[3]), pack2(hv[4], hv[5]), pack2(hv[6], hv[7]));
-      row[core_off(fs, 24 * h + 8, kSbo2) / 16] =
-          make_uint4(pack2(hv[8], hv[9]), pack2(lv[0], lv[1]), pack2(lv[2], lv[3]), pack2(lv[4], lv[5]));
-      row[core_off(fs, 24 * h + 16, kSbo2) / 16] =
-          make_uint4(pack2(lv[6], lv[7]), pack2(lv[8], lv[9]), pack2(z, z), pack2(z, z));
+      row[core_off(fs, 24 * h, kSbo2) / 16] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      row[core_off(fs, 24 * h + 8, kSbo2) / 16] = make_uint4(hw[4], lw[0], lw[1], lw[2]);
+      row[core_off(fs, 24 * h + 16, kSbo2) / 16] = make_uint4(lw[3], lw[4], 0u, 0u);
     }
     asm volatile("fence.proxy.async.shared::cta;");
     fence_before();
@@ -806,9 +816,9 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       commit(&sm.mbar);
     }
   }
-  ok = wait_phase(&sm.mbar, phase) && ok;
+  ok = !__syncthreads_or((tid >> 5) == 0 && !wait_phase(&sm.mbar, phase)) && ok;
   phase ^= 1u;
-  if (__syncthreads_or(!ok)) return false;
+  if (!ok) return false;
   fence_after();
   gather_d2(tmem, lane_base, h, iK, G);
   // ---- gradient partials of this thread's control points and dE/dalpha;
