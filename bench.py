@@ -318,6 +318,77 @@ def planar_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int) -> dict:
             "vertex_steps_per_s": plan.nv * K / total, "ms_per_step": total * 1e3 / K, "steps": K}
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
+
+
+def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_gbs: float) -> dict:
+    """Langevin with the limit-surface mass matrix on a 40,962-vertex vesicle
+    (icosahedron subdivided 6x, R 1000 A, noise N(0, 2 A), kc 20 kT, c0 0),
+    global area and volume restraints (K_area 0.2 kcal/mol/A^2 on the total
+    area, K_volume 0.01 kcal/mol/A^6 on the enclosed volume, targets the start
+    state), gamma 1/ps, FP32 form with M^-1 applied in FP32 each step.
+
+    The time step: a thermal displacement of 0.05 A per step would take
+    dt = 0.05 / sqrt(kT <M^-1_ii>) (about 120 AKMA units here), far beyond the
+    stability limits of the leapfrog with friction (gamma dt < 1) and of the
+    volume restraint's breathing mode, whose frequency is
+    omega = sqrt(K_volume A^2 / M_total); dt = 0.25 / omega is used, and the
+    line states both."""
+    t0 = time.perf_counter()
+    plan, prm = W.large_vesicle(tmpdir, U.FP32_CENTRED)
+    mesh = U.Mesh(ctx, plan, prm)
+    t1 = time.perf_counter()
+    mi = mesh.mass_build(plan)
+    t2 = time.perf_counter()
+    it_th, minv, dt_thermal = W.langevin_mass_integrator(mesh, plan.nv, 1004)
+    omega = math.sqrt(0.01 * mi.area0 ** 2 / (mi.mass_per_point * mi.points))
+    dt = min(dt_thermal, 0.25 / omega)
+    it = U.integrator(U.LANGEVIN, time_step=dt * W.AKMA_TIME_S, gamma=it_th.gamma, seed=1004,
+                      divergence_threshold=1e5, use_mass=1)
+    mesh.restraints_set(K_area=0.2, K_volume=0.01)
+    r0, _ = mesh.state_get()
+    e_warm = mesh.run(it, 0, 32)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    mesh.run_async(it, 32, K)
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    energies = mesh.energies(K)
+    r1, _ = mesh.state_get()
+    # the M^-1 apply alone: 8 bytes per nonzero (FP32 value, column) plus the row pointers and vectors
+    n3 = 3 * plan.nv
+    a = torch.randn(n3, dtype=torch.float64, device="cuda")
+    b = torch.zeros_like(a)
+    torch.cuda.synchronize()
+    mesh.mass_apply_device(a.data_ptr(), b.data_ptr())
+    reps = 20
+    e0.record(stream)
+    for _ in range(reps):
+        mesh.mass_apply_device(a.data_ptr(), b.data_ptr())
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    ms_apply = e0.elapsed_time(e1) / reps
+    if mi.dense:
+        apply_bytes = 4.0 * plan.nv * plan.nv + 8.0 * n3 * 2 + 4.0 * n3
+    else:
+        apply_bytes = 8.0 * mi.nnz_inverse + 4.0 * (plan.nv + 1) + 8.0 * n3 * 2 + 4.0 * n3
+    gbs = apply_bytes / (ms_apply * 1e-3) / 1e9
+    return {"workload": "Langevin with the limit-surface M^-1 on a 40,962-vertex vesicle (R 1000 A, noise 2 A, "
+                        "kc 20 kT), area and volume restraints, gamma 1/ps, FP32 form",
+            "vertex_steps_per_s": plan.nv * K / sec, "ms_per_step": sec * 1e3 / K, "steps": K,
+            "energies_finite": bool(np.all(np.isfinite(energies)) and np.all(np.isfinite(e_warm))),
+            "energy_first_last": [float(e_warm[0]), float(energies[-1])],
+            "rms_displacement_A": float(np.sqrt(np.mean((r1[:-3] - r0[:-3]) ** 2))),
+            "time_step_akma": dt, "thermal_0p05A_time_step_akma": dt_thermal, "volume_mode_omega_per_akma": omega,
+            "plan_s": t1 - t0, "mass_build_s": t2 - t1, "minv_dense": bool(mi.dense), "minv_nnz": int(mi.nnz_inverse),
+            "minv_fill": mi.nnz_inverse / plan.nv ** 2,
+            "minv_apply": {"ms": ms_apply, "bytes": apply_bytes, "gbs": gbs, "hbm_frac": gbs / peak_gbs,
+                           "storage": "FP32 values, int32 columns (CSR)" if not mi.dense else "FP32 dense"}}
+
+
 def engine_arm(args) -> None:
     rank, world, local = dist_env()
     import torch
@@ -430,8 +501,14 @@ def engine_arm(args) -> None:
             b64.poll()
             s64 = time_batch(b64, ctx, stream, torch, K64)
             e64_first = np.array([m.energies(1)[0] for m in meshes64])
+            _, fl64, _ = face_pass_work([pl for pl, _ in pp64], 8)
             var["batched_fp64"] = {"vertex_steps_per_s": nv_total * K64 / s64, "steps": K64,
-                                   "ms_per_step": s64 * 1e3 / K64}
+                                   "ms_per_step": s64 * 1e3 / K64,
+                                   "fp64_tflops": fl64 * K64 / s64 / 1e12,
+                                   "fp64_frac": fl64 * K64 / s64 / 1e12 / FP64_NOMINAL_TFLOPS,
+                                   "fp64_peak_note": "face-pass flops of the whole step over its time, against the "
+                                                     "nominal 1.25 TFLOP/s dense FP64 of a GB300: the plain path is "
+                                                     "bound by the FP64 pipe, not by HBM"}
             del b64
             # FP32 form against FP64 on the same states
             gerr = []
@@ -460,6 +537,8 @@ def engine_arm(args) -> None:
             var["batched_fp32_over_plain_fp64"] = value / var["plain_fp64_one_by_one"]["vertex_steps_per_s"]
             del meshes64
             var["planar128_fp32"] = planar_variant(ctx, U, W, torch, stream, tmp / "planar", 300)
+            var["langevin_mass_40962"] = langevin_mass_variant(ctx, U, W, torch, stream, tmp / "large", 2000,
+                                                               peaks["hbm_gbs"])
             out["variants"] = var
         if args.serve_seconds > 0:
             out["serving"] = serving_run(ctx, U, W, args.serve_seconds, args.serve_rate, 1005, tmp / "serve")

@@ -228,7 +228,10 @@ typedef struct {
   int dense;            /* 1: M^-1 kept dense (fill >= 30%), 0: CSR */
 } umcp_mass_info;
 umcp_status umcp_mass_build(umcp_mesh *mesh, const umcp_plan *plan, const umcp_mass_opts *opts, umcp_mass_info *info);
-/* The installed M^-1 as a dense nv x nv row-major array. */
+/* The installed M^-1 as a dense nv x nv row-major array. Meshes of the
+ * precision form (UMCP_FP32_CENTRED) store and apply M^-1 in FP32 (rounded
+ * once from the FP64 inverse; sums compensated, scaling in FP64); their
+ * values come back FP32-rounded. */
 umcp_status umcp_mass_get(umcp_mesh *mesh, double *dense);
 /* AltSparseCartMatVecIncrScale (src/parallel.C:1028-1075):
  * out[3i+c] += scale/alpha_c^2 * (scalev ? scalev[c*nrow+i] : 1) * sum_k val[k] in[3 col[k]+c]. */

@@ -120,3 +120,31 @@ def test_leapfrog_with_built_mass_matches_oracle(kind):
         r[:-3] = rv
     assert np.max(np.abs(r_gpu - r)) <= 1e-9 * np.max(np.abs(r))
     assert np.max(np.abs(p_gpu - p)) <= 1e-9 * max(np.max(np.abs(p)), 1e-300)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rel_tol", [1e-20, 0.02])
+def test_precision_form_applies_the_inverse_in_fp32(rel_tol):
+    """A mesh of the FP32 form keeps M^-1 rounded once to FP32 (dense, or CSR
+    when truncation leaves it sparse) and applies it with compensated FP32
+    sums: within 1e-6 of sum_j |M^-1_ij| |x_j| of the FP64 apply."""
+    ctx = U.Context(0)
+    plan, prm, _ = load_case("ico3_plain")
+    _, prm32, _ = load_case("ico3_plain", U.FP32_CENTRED)
+    m64 = U.Mesh(ctx, plan, prm)
+    i64 = m64.mass_build(plan, rel_tol=rel_tol)
+    m32 = U.Mesh(ctx, plan, prm32)
+    i32 = m32.mass_build(plan, rel_tol=rel_tol)
+    assert (i32.dense, i32.nnz_inverse) == (i64.dense, i64.nnz_inverse) and i32.dense == (rel_tol < 0.01)
+    g = m64.mass_get()
+    assert np.array_equal(m32.mass_get(), g.astype(np.float32).astype(np.float64))
+    rng = np.random.default_rng(3)
+    vin = rng.normal(0, 1, 3 * plan.nv)
+    base = rng.normal(0, 1, 3 * plan.nv)
+    scalev = rng.uniform(0.5, 2.0, 3 * plan.nv)
+    bound = (np.abs(g) @ np.abs(vin.reshape(-1, 3))).reshape(-1)
+    for sv, scale, al in [(None, 1.0, (1, 1, 1)), (scalev, -0.7, (1.01, 0.98, 1.2))]:
+        want = m64.mass_apply(vin, base.copy(), sv, scale, al)
+        got = m32.mass_apply(vin, base.copy(), sv, scale, al)
+        f = abs(scale) / np.min(np.asarray(al)) ** 2 * (1.0 if sv is None else sv.reshape(3, -1).T.reshape(-1))
+        assert np.all(np.abs(got - want) <= 1e-6 * f * bound + 1e-12 * np.abs(base))

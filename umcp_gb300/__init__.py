@@ -486,6 +486,13 @@ class Mesh:
                                          _dp(sv), scale, _dp(a)))
         return vout
 
+    def mass_apply_device(self, d_in: int, d_out: int, d_scalev: int = 0, scale: float = 1.0,
+                          alphas=(1.0, 1.0, 1.0)) -> None:
+        """out (+)= M^-1 in on device pointers (3 nv doubles each), queued on the context's stream."""
+        a = np.asarray(alphas, dtype=np.float64)
+        _check(library().umcp_mass_apply_device(self._h, C.c_void_p(d_in), C.c_void_p(d_out),
+                                                C.c_void_p(d_scalev or None), scale, _dp(a)))
+
     def state_set(self, r: np.ndarray, p: np.ndarray | None = None) -> None:
         _check(library().umcp_state_set(self._h, _dp(np.ascontiguousarray(r, dtype=np.float64)),
                                         _dp(None if p is None else np.ascontiguousarray(p, dtype=np.float64))))

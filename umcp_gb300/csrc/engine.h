@@ -90,10 +90,12 @@ struct umcp_mesh {
   double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
   double *h_stage2 = nullptr; // pinned, 3*nv doubles
   uint64_t *h_cnt = nullptr;  // pinned, 2 counters
-  // effective inverse mass: CSR (mrow, mcol, mval) or dense row-major (mdense)
+  // effective inverse mass: CSR (mrow, mcol, mval) or dense row-major (mdense);
+  // FP64 values, or FP32 ones for meshes of the precision form (mass_f32),
+  // whose apply reads an FP32 copy of its input (min32, 3 nv floats)
   int mrows = 0;
-  umcp::DevBuf mrow, mcol, mval, alphas, mdense;
-  bool mass_dense = false;
+  umcp::DevBuf mrow, mcol, mval, alphas, mdense, min32;
+  bool mass_dense = false, mass_f32 = false;
   // captured step sequences, by length (1 and kGraphChunk steps)
   struct CachedGraph {
     cudaGraphExec_t exec = nullptr;
@@ -117,7 +119,7 @@ struct umcp_mesh {
                                     &G->rr0f, &G->compf, &G->basis_w})
         b += x->bytes;
     for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
-                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &geo_block, &gterm,
+                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &min32, &geo_block, &gterm,
                                   &geo_done})
       b += x->bytes;
     return b;

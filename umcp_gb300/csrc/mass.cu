@@ -135,16 +135,71 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
   }
 }
 
+// dense_apply_kernel on FP32 values and an FP32 input: Kahan-compensated FP32
+// sums per thread, the block reduction and the scaling in FP64.
+__global__ void dense_apply32_kernel(int n, const float *__restrict__ A, const double *__restrict__ scalev,
+                                     double scale, const double *__restrict__ alphas, const float *__restrict__ in,
+                                     double *__restrict__ out, int accumulate) {
+  __shared__ double red[3][8];
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const float *row = A + (size_t)i * n;
+    float s[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const float m = row[j];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float y = m * in[3 * (size_t)j + q] - c[q], t = s[q] + y;
+        c[q] = (t - s[q]) - y;
+        s[q] = t;
+      }
+    }
+    double a[3] = {(double)s[0] - c[0], (double)s[1] - c[1], (double)s[2] - c[2]};
+    for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) a[q] += __shfl_xor_sync(0xffffffffu, a[q], off);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red[0][w] = a[0]; red[1][w] = a[1]; red[2][w] = a[2]; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      const int q = threadIdx.x;
+      double t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[q][k];
+      const double al = alphas ? alphas[q] : 1.0;
+      double f = scale / (al * al);
+      if (scalev) f *= scalev[(size_t)q * n + i];
+      const double v = f * t;
+      out[3 * (size_t)i + q] = accumulate ? out[3 * (size_t)i + q] + v : v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void dense_to_f32_kernel(size_t total, const double *__restrict__ A, float *__restrict__ B) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    B[e] = (float)A[e];
+}
+
 }  // namespace
 
 cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double scale, const double *alphas,
                                    const double *in, double *out, int accumulate, cudaStream_t s) {
+  if (m->mass_f32) {
+    cudaError_t e = launch_to_f32(3 * (size_t)m->mrows, in, m->min32.as<float>(), s);
+    if (e != cudaSuccess) return e;
+    if (!m->mass_dense)
+      return launch_spmv32(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<float>(), scalev, scale, alphas,
+                           m->min32.as<float>(), out, accumulate, s);
+  }
   if (m->mass_dense) {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
     const int grid = m->mrows < sms * 8 ? m->mrows : sms * 8;
-    dense_apply_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<double>(), scalev, scale, alphas, in, out,
-                                            accumulate);
+    if (m->mass_f32)
+      dense_apply32_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<float>(), scalev, scale, alphas,
+                                                m->min32.as<float>(), out, accumulate);
+    else
+      dense_apply_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<double>(), scalev, scale, alphas, in, out,
+                                              accumulate);
     return cudaGetLastError();
   }
   return launch_spmv(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<double>(), scalev, scale, alphas, in,
@@ -221,9 +276,18 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
   UMCP_CUDA(cudaStreamSynchronize(s));
 
   const double fill = (double)kept / ((double)n * n);
+  // the precision form keeps M^-1 in FP32 (rounded once from the FP64 inverse)
+  const bool f32 = m->precision == UMCP_FP32_CENTRED;
   if (fill >= 0.3) {
-    std::swap(m->mdense.p, A.p);
-    std::swap(m->mdense.bytes, A.bytes);
+    if (f32) {
+      UMCP_CUDA(m->mdense.alloc((size_t)n * n * sizeof(float)));
+      dense_to_f32_kernel<<<sms * 8, 256, 0, s>>>((size_t)n * n, A.as<double>(), m->mdense.as<float>());
+      UMCP_CUDA(cudaGetLastError());
+      UMCP_CUDA(cudaStreamSynchronize(s));
+    } else {
+      std::swap(m->mdense.p, A.p);
+      std::swap(m->mdense.bytes, A.bytes);
+    }
     m->mass_dense = true;
     UMCP_CUDA(m->mrow.alloc(0));
     UMCP_CUDA(m->mcol.alloc(0));
@@ -243,10 +307,13 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
     }
     UMCP_CUDA(upload(m->mrow, rp));
     UMCP_CUDA(upload(m->mcol, cl));
-    UMCP_CUDA(upload(m->mval, vl));
+    if (f32) UMCP_CUDA(upload(m->mval, std::vector<float>(vl.begin(), vl.end())));
+    else UMCP_CUDA(upload(m->mval, vl));
     UMCP_CUDA(m->mdense.alloc(0));
     m->mass_dense = false;
   }
+  m->mass_f32 = f32;
+  UMCP_CUDA(m->min32.alloc(f32 ? 3 * (size_t)n * sizeof(float) : 0));
   m->mrows = n;
   if (info) {
     memset(info, 0, sizeof(*info));
@@ -267,7 +334,13 @@ extern "C" umcp_status umcp_mass_get(umcp_mesh *m, double *dense) {
   UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
   const int n = m->mrows;
   if (m->mass_dense) {
-    UMCP_CUDA(cudaMemcpy(dense, m->mdense.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (m->mass_f32) {
+      std::vector<float> a((size_t)n * n);
+      UMCP_CUDA(cudaMemcpy(a.data(), m->mdense.p, a.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t e = 0; e < a.size(); ++e) dense[e] = a[e];
+    } else {
+      UMCP_CUDA(cudaMemcpy(dense, m->mdense.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
     return UMCP_OK;
   }
   std::vector<int> rp((size_t)n + 1);
@@ -276,7 +349,13 @@ extern "C" umcp_status umcp_mass_get(umcp_mesh *m, double *dense) {
   std::vector<double> vl((size_t)rp[n]);
   if (rp[n] > 0) {
     UMCP_CUDA(cudaMemcpy(cl.data(), m->mcol.p, cl.size() * sizeof(int), cudaMemcpyDeviceToHost));
-    UMCP_CUDA(cudaMemcpy(vl.data(), m->mval.p, vl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (m->mass_f32) {
+      std::vector<float> v32(vl.size());
+      UMCP_CUDA(cudaMemcpy(v32.data(), m->mval.p, v32.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < vl.size(); ++k) vl[k] = v32[k];
+    } else {
+      UMCP_CUDA(cudaMemcpy(vl.data(), m->mval.p, vl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    }
   }
   memset(dense, 0, (size_t)n * n * sizeof(double));
   for (int i = 0; i < n; ++i)

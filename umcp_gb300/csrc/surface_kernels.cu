@@ -1487,6 +1487,54 @@ __global__ void spmv_kernel(int nrow, const int *__restrict__ row_ptr, const int
   }
 }
 
+// spmv_kernel on FP32 values and an FP32 copy of the input (the precision
+// form's inverse mass): Kahan-compensated FP32 sums per lane, the cross-lane
+// sum and the scaling in FP64. Reads 8 bytes per nonzero instead of 12 and
+// keeps the FP64 pipe out of the loop.
+__global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const int *__restrict__ col,
+                              const float *__restrict__ val, const double *__restrict__ scalev, double scale,
+                              const double *__restrict__ alphas, const float *__restrict__ in,
+                              double *__restrict__ out, int accumulate) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double f[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double a = alphas ? alphas[c] : 1.0;
+    f[c] = scale / (a * a);
+  }
+  for (int i = warp; i < nrow; i += nwarps) {
+    HalfWarpSums<float> acc;
+    for (int k = row_ptr[i] + lane; k < row_ptr[i + 1]; k += 32) {
+      const float v = val[k];
+      const int j = col[k];
+      acc.add(0, v * in[3 * (size_t)j]);
+      acc.add(1, v * in[3 * (size_t)j + 1]);
+      acc.add(2, v * in[3 * (size_t)j + 2]);
+    }
+    double s[3] = {acc.get(0), acc.get(1), acc.get(2)};
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], off);
+    if (lane == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        double o = s[c] * f[c];
+        if (scalev) o *= scalev[(size_t)c * nrow + i];
+        if (accumulate) out[3 * (size_t)i + c] += o;
+        else out[3 * (size_t)i + c] = o;
+      }
+    }
+  }
+}
+
+__global__ void to_f32_kernel(size_t n, const double *__restrict__ in, float *__restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 }  // namespace dev
 
 static int grid_for(int n, int per_block) {
@@ -1586,6 +1634,25 @@ cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const 
   dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, rhi, rlo, status);
   return cudaGetLastError();
 }
+cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
+                          double scale, const double *alphas, const float *in, double *out, int accumulate,
+                          cudaStream_t s) {
+  if (nrow <= 0) return cudaSuccess;
+  int warps_per_block = 8;
+  int grid = grid_for(nrow, warps_per_block);
+  if (grid > 152 * 16) grid = 152 * 16;
+  dev::spmv32_kernel<<<grid, 32 * warps_per_block, 0, s>>>(nrow, row_ptr, col, val, scalev, scale, alphas, in, out,
+                                                          accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(size_t n, const double *in, float *out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  size_t g = (n + 255) / 256;
+  dev::to_f32_kernel<<<(int)(g < 152 * 8 ? g : 152 * 8), 256, 0, s>>>(n, in, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const double *val, const double *scalev,
                         double scale, const double *alphas, const double *in, double *out, int accumulate,
                         cudaStream_t s) {

@@ -85,3 +85,38 @@ def planar_plan(tmpdir: Path, nx: int, ny: int, seed: int, precision: int, kc_kT
     U.generate_planar(path, nx, ny, a, kc_kT, seed)
     prm = U.params(kc=U.kc_from_kT(kc_kT, temperature), KA=0.215, temperature=temperature, precision=precision)
     return U.Plan(path, prm), prm
+
+
+AKMA_TIME_S = 0.04888e-12  # one AKMA time unit in seconds (the engine's time_step conversion)
+
+
+def large_vesicle(tmpdir: Path, precision: int, level: int = 6, radius: float = 1000.0, sigma: float = 2.0,
+                  kc_kT: float = 20.0, seed: int = 1004, temperature: float = 298.0):
+    """The Langevin-with-mass workload: an icosahedron subdivided `level` times
+    (40,962 vertices at 6), radius 1000 A, radial noise N(0, 2 A), kc 20 kT,
+    c0 = 0."""
+    tmpdir.mkdir(parents=True, exist_ok=True)
+    path = tmpdir / "large_vesicle.mesh"
+    U.generate_icosphere(path, level, radius, sigma, seed)
+    prm = U.params(kc=U.kc_from_kT(kc_kT, temperature), KA=0.215, temperature=temperature, precision=precision)
+    return U.Plan(path, prm), prm
+
+
+def langevin_mass_integrator(mesh, nv: int, seed: int, rms_step: float = RMS_STEP_A, gamma_per_ps: float = 1.0,
+                             temperature: float = 298.0, samples: int = 8):
+    """Langevin leapfrog with the installed M^-1 and a time step whose thermal
+    displacement sqrt(kT <M^-1_ii>) dt is rms_step; <M^-1_ii> is the mean
+    diagonal entry over `samples` vertices spread over the mesh."""
+    kT = U.KCAL_MOL_PER_KT_298 / 298.0 * temperature
+    diag = []
+    for i in np.linspace(0, nv - 1, samples).astype(int):
+        e = np.zeros(3 * nv)
+        e[3 * i] = 1.0
+        out = np.zeros(3 * nv)
+        mesh.mass_apply(e, out)
+        diag.append(out[3 * i])
+    minv = float(np.mean(diag))
+    dt_akma = rms_step / math.sqrt(kT * minv)
+    it = U.integrator(U.LANGEVIN, time_step=dt_akma * AKMA_TIME_S, gamma=gamma_per_ps * AKMA_TIME_S * 1e12,
+                      seed=seed, divergence_threshold=1e5, use_mass=1)
+    return it, minv, dt_akma
