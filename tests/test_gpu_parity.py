@@ -142,10 +142,12 @@ def test_run_graph_chunks_equal_eager_steps(ctx):
     assert np.array_equal(a.state_get()[0], b.state_get()[0])
 
 
-def test_step_host_is_one_run_step(ctx):
-    plan, prm, _ = load_case("ico2_plain")
+@pytest.mark.parametrize("precision", [U.FP64, U.FP32_CENTRED])
+def test_step_host_is_one_run_step(ctx, precision):
+    plan, prm, _ = load_case("ico2_plain", precision)
     it = U.integrator(U.LANGEVIN, time_step=1e-15, gamma=0.001, seed=8)
     a = U.Mesh(ctx, plan, prm)
+    a.run(it, 7, 2)  # the resident state (and its FP32 pairs) moves away from r
     r = plan.positions()
     p = np.zeros(3 * plan.nv)
     for s in range(3):

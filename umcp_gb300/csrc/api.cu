@@ -524,6 +524,7 @@ static GeoArgs geo_args(umcp_mesh *m, const double *d_r) {
     g.basis = Gp->basis.as<double>();
     g.basis_w = Gp->basis_w.as<double>();
     g.weight = Gp->weight.as<double>();
+    g.tab = Gp->geo_tab.as<float>();
     g.ncp = Gp->ncp;
     g.npt = Gp->npt;
     g.ncpp = (Gp->ncp + 3) / 4 * 4;
@@ -535,8 +536,14 @@ static GeoArgs geo_args(umcp_mesh *m, const double *d_r) {
   G.nfaces = base;
   G.nv = m->nv;
   G.r = d_r;
+  G.rhi = m->rhi.as<float>();
+  G.rlo = m->rlo.as<float>();
   for (int d = 0; d < 3; ++d)
-    for (int c = 0; c < 3; ++c) G.box[d][c] = m->P.box[d][c];
+    for (int c = 0; c < 3; ++c) {
+      G.box[d][c] = m->P.box[d][c];
+      G.box_hi[d][c] = m->P.box_hi[d][c];
+      G.box_lo[d][c] = m->P.box_lo[d][c];
+    }
   G.KA = m->rs.KA;
   G.A0 = m->rs.A0;
   G.KV = m->rs.KV;
@@ -560,7 +567,7 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
   GeoArgs GA{};
   if (geo) {
     GA = geo_args(m, d_r);
-    cudaError_t e = launch_geo_sums(GA, s);
+    cudaError_t e = launch_geo_sums(GA, m->precision == UMCP_FP64, s);
     if (e != cudaSuccess) return e;
     fin_geo = *fin_in;
     fin_geo.gterm = m->gterm.as<double>();
@@ -869,6 +876,34 @@ extern "C" umcp_status umcp_restraints_set(umcp_mesh *m, const umcp_restraints *
         if ((c & ~dev::kVertexMask) != home)
           return fail(UMCP_ERR_INVALID, "a volume restraint needs a closed surface (this mesh is periodic)");
     }
+  if (m->precision == UMCP_FP32_CENTRED)
+    for (auto &G : m->groups) {
+      if (G->geo_tab.p || G->nfaces == 0) continue;
+      // FP32 tables of the restraint kernels: the value and first-derivative
+      // rows split as hi + lo, and the point weights
+      const int ncp = G->ncp, npt = G->npt, ncpp = (ncp + 3) / 4 * 4;
+      std::vector<double> basis((size_t)npt * 5 * ncpp), bw((size_t)npt * ncp), w(npt);
+      UMCP_CUDA(cudaMemcpy(basis.data(), G->basis.p, basis.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      UMCP_CUDA(cudaMemcpy(bw.data(), G->basis_w.p, bw.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      UMCP_CUDA(cudaMemcpy(w.data(), G->weight.p, w.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      std::vector<float> tab(geo_tab_floats(ncp, npt));
+      const size_t nrow = (size_t)npt * 3 * ncp;
+      for (int p = 0; p < npt; ++p)
+        for (int k = 0; k < 3; ++k)
+          for (int x = 0; x < ncp; ++x) {
+            const double b = k == 0 ? bw[(size_t)p * ncp + x] : basis[((size_t)p * 5 + (k - 1)) * ncpp + x];
+            const size_t i = ((size_t)p * 3 + k) * ncp + x;
+            tab[i] = (float)b;
+            tab[nrow + i] = (float)(b - (double)tab[i]);
+          }
+      for (int p = 0; p < npt; ++p) {
+        const double cw = G->dudv * w[p], c3 = cw / 3.0;
+        tab[2 * nrow + p] = (float)cw;
+        tab[2 * nrow + npt + p] = (float)c3;
+        tab[2 * nrow + 2 * npt + p] = (float)(c3 - (double)(float)c3);
+      }
+      UMCP_CUDA(upload(G->geo_tab, tab));
+    }
   if (!m->gterm.p) {
     int nblk = geo_blocks(m->nfaces);
     UMCP_CUDA(m->geo_block.alloc((size_t)nblk * kGeoWords * sizeof(double)));
@@ -885,7 +920,11 @@ extern "C" umcp_status umcp_restraints_set(umcp_mesh *m, const umcp_restraints *
   if (R.A0 < 0 || R.V0 < 0) {
     // targets from the resident state: one sums pass with the constants off
     m->rs = umcp_mesh::Restraints{true, 0, 1, 0, 0};
-    UMCP_CUDA(launch_geo_sums(geo_args(m, m->r.as<double>()), s));
+    // the precision form's sums read the hi/lo pairs, which may hold the last evaluated state
+    if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
+      UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
+    m->split_valid = true;
+    UMCP_CUDA(launch_geo_sums(geo_args(m, m->r.as<double>()), m->precision == UMCP_FP64, s));
     double gt[kGeoWords];
     UMCP_CUDA(cudaMemcpyAsync(gt, m->gterm.p, sizeof gt, cudaMemcpyDeviceToHost, s));
     UMCP_CUDA(cudaStreamSynchronize(s));
@@ -1063,6 +1102,7 @@ extern "C" umcp_status umcp_step_host(umcp_mesh *m, const umcp_integrator *it, u
   const size_t nst = 3 * (size_t)m->nv + 3;
   memcpy(m->h_stage, r, nst * sizeof(double));
   UMCP_CUDA(cudaMemcpyAsync(m->r.p, m->h_stage, nst * sizeof(double), cudaMemcpyHostToDevice, s));
+  m->split_valid = false;  // the precision form's hi/lo pairs still hold the previous state
   if (p) {
     memcpy(m->h_stage2, p, (nst - 3) * sizeof(double));
     UMCP_CUDA(cudaMemcpyAsync(m->p.p, m->h_stage2, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, s));

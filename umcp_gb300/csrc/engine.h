@@ -38,6 +38,7 @@ struct Group {
   DevBuf cp, g0, rr0, comp, basis, weight, dest;
   DevBuf basis_w;           // value rows [npt][ncp] (area and volume terms)
   DevBuf g0f, rr0f, compf;  // FP32 copies for the precision form
+  DevBuf geo_tab;           // FP32 restraint tables (GeoGroup::tab), built when restraints are first set
 };
 }  // namespace umcp
 
@@ -116,7 +117,7 @@ struct umcp_mesh {
     size_t b = 0;
     for (auto &G : groups)
       for (const umcp::DevBuf *x : {&G->cp, &G->g0, &G->rr0, &G->comp, &G->basis, &G->weight, &G->dest, &G->g0f,
-                                    &G->rr0f, &G->compf, &G->basis_w})
+                                    &G->rr0f, &G->compf, &G->basis_w, &G->geo_tab})
         b += x->bytes;
     for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
                                   &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &min32, &geo_block, &gterm,

@@ -25,8 +25,8 @@ struct FinishArgs {
   const double *gterm; // global restraint terms to add (NULL: none), see GeoArgs
 };
 
-// Global area and volume of the limit surface and their restraint (one FP64
-// thread per face over every patch type):
+// Global area and volume of the limit surface and their restraint (one
+// half-warp per face over every patch type; V in FP64, see geo_sums_kernel):
 //   A = sum dudv w |Ru x Rv|,  V = 1/3 sum dudv w R.(Ru x Rv)
 //   E_r = 1/2 K_A (A-A0)^2/A0 + 1/2 K_V (V-V0)^2
 // gterm receives {A, V, E_r, dE_r/dA, dE_r/dV, dE_r/dalpha_xyz}.
@@ -36,24 +36,37 @@ struct GeoGroup {
   const double *basis;     // [npt][5][ncpp] rows u,v,uu,uv,vv
   const double *basis_w;   // [npt][ncp] value rows
   const double *weight;    // [npt]
+  // FP32 tables of the precision form: rows w,u,v as hi [npt][3][ncp] then
+  // lo [npt][3][ncp] (row = hi + lo), then cw = dudv w [npt], then
+  // c3 = dudv w / 3 as hi [npt] and lo [npt]
+  const float *tab;
   int ncp, npt, ncpp, nfaces, face_base;
   double dudv;
 };
+// Floats of GeoGroup::tab for a patch type.
+inline size_t geo_tab_floats(int ncp, int npt) { return (size_t)6 * npt * ncp + 3 * (size_t)npt; }
 enum : int { kGeoA = 0, kGeoV, kGeoE, kGeoCA, kGeoCV, kGeoDAlpha, kGeoWords = 8 };
 struct GeoArgs {
   GeoGroup g[3];
   int ngroups, nfaces, nv;
   const double *r;
+  const float *rhi, *rlo;  // r = hi + lo (precision form; read by the FP32 gradient pass)
   double box[3][3];
+  float box_hi[3][3], box_lo[3][3];
   double KA, A0, KV, V0;
   double *block;           // [blocks][8] partial sums
   double *gterm;           // kGeoWords
   unsigned *done;          // finished-block counter (zero between launches)
 };
 constexpr int kGeoThreads = 128;
-inline int geo_blocks(int nfaces) { return nfaces > 0 ? (nfaces + kGeoThreads - 1) / kGeoThreads : 1; }
+// Fixed grid (a function of the face count only, so every sum has a fixed order).
+inline int geo_blocks(int nfaces) {
+  const int b = nfaces > 0 ? (nfaces + 4 * (kGeoThreads / 16) - 1) / (4 * (kGeoThreads / 16)) : 1;  // >= 4 faces per half-warp
+  return b < 152 * 8 ? b : 152 * 8;
+}
 // Sums A, V and their alpha derivatives; the last block writes gterm.
-cudaError_t launch_geo_sums(const GeoArgs &G, cudaStream_t s);
+// alpha64: the area and the box-scale derivatives in FP64 as well (plain path).
+cudaError_t launch_geo_sums(const GeoArgs &G, bool alpha64, cudaStream_t s);
 // partial[slot] += alpha * (dE_r/dA dA/dX + dE_r/dV dV/dX) for every (face, control point).
 template <typename T>
 cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s);

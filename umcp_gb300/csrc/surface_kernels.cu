@@ -1291,87 +1291,85 @@ __global__ void batch_start_kernel(const BatchJob *__restrict__ jobs, const Batc
 }
 
 // ---------------------------------------------------------------- area, volume
+//
+// One half-warp per face, as in the face pass: lanes are control points while
+// the face's local coordinates are formed, then quadrature points. The value
+// and first-derivative basis rows of every patch type sit in shared memory.
+//
+// Precision. The restraint on V is stiff (K_V (V - V0) is a force per unit
+// volume), so V must be exact far below an FP32 ulp of V: on a 1000 A vesicle
+// a 1e-3 A^3 error already moves every vertex's restraint force by about
+// K_V 1e-3 A^3 x 300 A^2. The sums kernel therefore forms R, R_u, R_v and
+// R.(R_u x R_v) in FP64 from FP64 local coordinates (relative to the patch
+// corner, which is added back exactly). The area, whose restraint is soft, and
+// the box-scale derivatives come from FP32 copies in the precision form. The
+// gradient kernel needs only the relative accuracy of any other gradient term
+// and runs in the form's own arithmetic (FP32 local coordinates from the hi/lo
+// pairs, as the face pass forms them).
 
-// One face's limit-surface positions and tangents at its points, FP64, in
-// absolute coordinates (alpha-scaled, lattice images applied).
-struct GeoFace {
-  double X[kMaxCpDev][3];
-  int ncp;
+constexpr int kGeoHW = kGeoThreads / 16;  // faces in flight per block
+constexpr int kGeoPt = 16;                // quadrature points of the largest rule
+
+template <typename T>
+struct GeoBasis {
+  T B[3][kGeoPt][3][kMaxCpDev];  // [group][point][w, u, v][control point]
+  T cw[3][kGeoPt];               // dudv * weight
 };
 
-__device__ __forceinline__ const GeoGroup &geo_group(const GeoArgs &G, int f, int *local) {
-  int k = 0;
-  while (k + 1 < G.ngroups && f >= G.g[k + 1].face_base) ++k;
-  *local = f - G.g[k].face_base;
-  return G.g[k];
-}
-
-__device__ __forceinline__ void geo_load(const GeoArgs &G, const GeoGroup &g, int lf, const double alpha[3],
-                                         GeoFace &F) {
-  F.ncp = g.ncp;
-  for (int x = 0; x < g.ncp; ++x) {
-    const uint32_t packed = g.cp[(size_t)lf * g.ncp + x];
-    const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
-    const int im[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-    for (int c = 0; c < 3; ++c)
-      F.X[x][c] = alpha[c] * (G.r[3 * (size_t)v + c] + im[0] * G.box[0][c] + im[1] * G.box[1][c] + im[2] * G.box[2][c]);
+template <typename T>
+__device__ void stage_geo_basis(const GeoArgs &G, GeoBasis<T> &s) {
+  for (int gi = 0; gi < G.ngroups; ++gi) {
+    const GeoGroup &g = G.g[gi];
+    for (int i = threadIdx.x; i < g.npt * g.ncp; i += blockDim.x) {
+      const int p = i / g.ncp, x = i % g.ncp;
+      s.B[gi][p][0][x] = (T)g.basis_w[(size_t)p * g.ncp + x];
+      s.B[gi][p][1][x] = (T)g.basis[(size_t)p * 5 * g.ncpp + x];
+      s.B[gi][p][2][x] = (T)g.basis[(size_t)p * 5 * g.ncpp + g.ncpp + x];
+    }
+    for (int p = threadIdx.x; p < g.npt; p += blockDim.x) s.cw[gi][p] = (T)(g.dudv * g.weight[p]);
   }
 }
 
-__device__ __forceinline__ void cross3(const double a[3], const double b[3], double o[3]) {
+// Group of global face f (faces are numbered group after group).
+__device__ __forceinline__ int geo_group(const GeoArgs &G, int f, int *local) {
+  int k = 0;
+  while (k + 1 < G.ngroups && f >= G.g[k + 1].face_base) ++k;
+  *local = f - G.g[k].face_base;
+  return k;
+}
+
+// Absolute (alpha-scaled, lattice-image) FP64 position of control point `lane` of face lf.
+__device__ __forceinline__ void geo_abs64(const GeoArgs &G, const GeoGroup &g, int lf, int lane,
+                                          const double alpha[3], double X[3], int *dest) {
+  const uint32_t packed = __ldg(&g.cp[(size_t)lf * g.ncp + lane]);
+  const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+  const int im[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    X[c] = alpha[c] * (G.r[3 * (size_t)v + c] + im[0] * G.box[0][c] + im[1] * G.box[1][c] + im[2] * G.box[2][c]);
+  if (dest) *dest = __ldg(&g.dest[(size_t)lf * g.ncp + lane]);
+}
+
+__device__ __forceinline__ double shfl_d(unsigned mask, double v, int src) { return __shfl_sync(mask, v, src, 16); }
+
+template <typename T>
+__device__ __forceinline__ void cross3(const T a[3], const T b[3], T o[3]) {
   o[0] = a[1] * b[2] - a[2] * b[1];
   o[1] = a[2] * b[0] - a[0] * b[2];
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-// Point p of face F: R, Ru, Rv and the weight dudv w.
-__device__ __forceinline__ void geo_point(const GeoGroup &g, const GeoFace &F, int p, double R[3], double Ru[3],
-                                          double Rv[3]) {
-  for (int c = 0; c < 3; ++c) R[c] = Ru[c] = Rv[c] = 0.0;
-  const double *bu = g.basis + (size_t)p * 5 * g.ncpp, *bv = bu + g.ncpp, *bw = g.basis_w + (size_t)p * g.ncp;
-  for (int x = 0; x < F.ncp; ++x)
-    for (int c = 0; c < 3; ++c) {
-      R[c] += bw[x] * F.X[x][c];
-      Ru[c] += bu[x] * F.X[x][c];
-      Rv[c] += bv[x] * F.X[x][c];
-    }
-}
-
-__global__ void __launch_bounds__(kGeoThreads) geo_sums_kernel(GeoArgs G) {
-  __shared__ double red[kGeoWords][kGeoThreads];
+// Block sums of the per-thread accumulators in a fixed order; the last block
+// to finish sums the block rows (in block order) and forms E_r, dE_r/dA,
+// dE_r/dV and dE_r/dalpha.
+__device__ void geo_finish(const GeoArgs &G, const double acc[kGeoWords], double (*red)[kGeoThreads]) {
   __shared__ bool last;
-  const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
-  double acc[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0};  // A, V, dA/dalpha (3), dV/dalpha (3)
-  const int f = blockIdx.x * kGeoThreads + threadIdx.x;
-  if (f < G.nfaces) {
-    int lf;
-    const GeoGroup &g = geo_group(G, f, &lf);
-    GeoFace F;
-    geo_load(G, g, lf, alpha, F);
-    for (int p = 0; p < g.npt; ++p) {
-      double R[3], Ru[3], Rv[3], m[3];
-      geo_point(g, F, p, R, Ru, Rv);
-      cross3(Ru, Rv, m);
-      const double gg = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-      const double c = g.dudv * g.weight[p];
-      acc[0] += c * gg;
-      acc[1] += c / 3.0 * (R[0] * m[0] + R[1] * m[1] + R[2] * m[2]);
-      // d/dalpha_c through X = alpha Y: the tangents scale with alpha_c
-      double n[3] = {m[0] / gg, m[1] / gg, m[2] / gg}, a1[3], a2[3], v1[3], v2[3];
-      cross3(Rv, n, a1);  // dg/dRu
-      cross3(n, Ru, a2);  // dg/dRv
-      cross3(Rv, R, v1);  // d(R.m)/dRu
-      cross3(R, Ru, v2);  // d(R.m)/dRv
-      for (int k = 0; k < 3; ++k) {
-        acc[2 + k] += c * (a1[k] * Ru[k] + a2[k] * Rv[k]) / alpha[k];
-        acc[5 + k] += c / 3.0 * (m[k] * R[k] + v1[k] * Ru[k] + v2[k] * Rv[k]) / alpha[k];
-      }
-    }
-  }
+#pragma unroll
   for (int q = 0; q < kGeoWords; ++q) red[q][threadIdx.x] = acc[q];
   __syncthreads();
   for (int w = kGeoThreads / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w)
+#pragma unroll
       for (int q = 0; q < kGeoWords; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
     __syncthreads();
   }
@@ -1402,44 +1400,375 @@ __global__ void __launch_bounds__(kGeoThreads) geo_sums_kernel(GeoArgs G) {
   }
 }
 
+// Sums A, V and their alpha derivatives in FP64 (the plain path).
+__global__ void __launch_bounds__(kGeoThreads) geo_sums_kernel(GeoArgs G) {
+  __shared__ GeoBasis<double> sb;
+  __shared__ double Xs[kGeoHW][kMaxCpDev][3];
+  __shared__ double red[kGeoWords][kGeoThreads];
+  stage_geo_basis<double>(G, sb);
+  __syncthreads();
+  const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
+  const double ialpha[3] = {1.0 / alpha[0], 1.0 / alpha[1], 1.0 / alpha[2]};
+  double acc[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0};  // A, V, dA/dalpha (3), dV/dalpha (3)
+  for (int f = blockIdx.x * kGeoHW + hw; f < G.nfaces; f += gridDim.x * kGeoHW) {
+    int lf;
+    const int gi = geo_group(G, f, &lf);
+    const GeoGroup &g = G.g[gi];
+    double X[3] = {0, 0, 0};
+    if (lane < g.ncp) geo_abs64(G, g, lf, lane, alpha, X, nullptr);
+    double X0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) X0[c] = shfl_d(hmask, X[c], 0);
+    if (lane < g.ncp)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Xs[hw][lane][c] = X[c] - X0[c];
+    __syncwarp(hmask);
+    if (lane < g.npt) {
+      double R[3] = {0, 0, 0}, Ru[3] = {0, 0, 0}, Rv[3] = {0, 0, 0};
+      const double *bw = sb.B[gi][lane][0], *bu = sb.B[gi][lane][1], *bv = sb.B[gi][lane][2];
+#pragma unroll
+      for (int x = 0; x < kMaxCpDev; ++x) {
+        if (x < g.ncp) {
+          const double w = bw[x], u = bu[x], v = bv[x];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const double xx = Xs[hw][x][c];
+            R[c] = fma(w, xx, R[c]);
+            Ru[c] = fma(u, xx, Ru[c]);
+            Rv[c] = fma(v, xx, Rv[c]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) R[c] += X0[c];  // back to absolute: the corner is exact in FP64
+      double m[3];
+      cross3(Ru, Rv, m);
+      const double cw = sb.cw[gi][lane], c3 = cw * (1.0 / 3.0);
+      acc[1] += c3 * (R[0] * m[0] + R[1] * m[1] + R[2] * m[2]);
+      const double gg = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]), ig = 1.0 / gg;
+      acc[0] += cw * gg;
+      double n[3] = {m[0] * ig, m[1] * ig, m[2] * ig}, a1[3], a2[3], v1[3], v2[3];
+      cross3(Rv, n, a1);  // dg/dRu
+      cross3(n, Ru, a2);  // dg/dRv
+      cross3(Rv, R, v1);  // d(R.m)/dRu
+      cross3(R, Ru, v2);  // d(R.m)/dRv
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        acc[2 + k] += cw * (a1[k] * Ru[k] + a2[k] * Rv[k]) * ialpha[k];
+        acc[5 + k] += c3 * (m[k] * R[k] + v1[k] * Ru[k] + v2[k] * Rv[k]) * ialpha[k];
+      }
+    }
+    __syncwarp(hmask);
+  }
+  geo_finish(G, acc, red);
+}
+
+// ---- float-float (double-FP32) arithmetic for the precision form's volume.
+// A value is hi + lo with |lo| <= ulp(hi)/2; the error-free transformations
+// are Knuth's two-sum and the FMA two-product (Dekker's product with a fused
+// multiply-add), so the arithmetic stays on the FP32 pipes and carries about
+// 44 bits. Every product and sum inside them is rounded on its own (no
+// contraction into an FMA), as the transformations require.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  float s, e;
+  two_sum(x.hi, y.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+  return ff_fast_two_sum(s, e);
+}
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+// acc += b x, without renormalising acc (call ff_norm once at the end).
+__device__ __forceinline__ void ff_acc(FF &acc, float bh, float bl, float xh, float xl) {
+  const float p = __fmul_rn(bh, xh);
+  float e = __fmaf_rn(bh, xh, -p);
+  e = __fmaf_rn(bh, xl, e);
+  e = __fmaf_rn(bl, xh, e);
+  float s, t;
+  two_sum(acc.hi, p, s, t);
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
+}
+__device__ __forceinline__ FF ff_norm(FF x) { return ff_fast_two_sum(x.hi, x.lo); }
+__device__ __forceinline__ FF ff_of(double x) {
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+
+// The precision form's sums: V from float-float contractions of float-float
+// local coordinates (formed from the FP32 hi/lo position pairs with error-free
+// sums) and summed in float-float per thread; the area and the box-scale
+// derivatives from the FP32 leading parts with Kahan sums. FP64 enters only in
+// the per-block and final sums.
+__global__ void __launch_bounds__(kGeoThreads) geo_sums_ff_kernel(GeoArgs G) {
+  __shared__ float Bh[3][kGeoPt][3][kMaxCpDev], Bl[3][kGeoPt][3][kMaxCpDev];
+  __shared__ FF c3s[3][kGeoPt];
+  __shared__ float cws[3][kGeoPt];
+  __shared__ float Xh[kGeoHW][kMaxCpDev][3], Xl[kGeoHW][kMaxCpDev][3];
+  __shared__ double red[kGeoWords][kGeoThreads];
+  __shared__ FF alpha_s[3];
+  __shared__ float ialpha_s[3];
+  for (int gi = 0; gi < G.ngroups; ++gi) {
+    const GeoGroup &g = G.g[gi];
+    const int nrow = g.npt * 3 * g.ncp;
+    for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+      const int p = i / (3 * g.ncp), k = (i / g.ncp) % 3, x = i % g.ncp;
+      Bh[gi][p][k][x] = g.tab[i];
+      Bl[gi][p][k][x] = g.tab[nrow + i];
+    }
+    for (int p = threadIdx.x; p < g.npt; p += blockDim.x) {
+      cws[gi][p] = g.tab[2 * nrow + p];
+      c3s[gi][p] = FF{g.tab[2 * nrow + g.npt + p], g.tab[2 * nrow + 2 * g.npt + p]};
+    }
+  }
+  if (threadIdx.x < 3) {
+    const double a = G.r[3 * (size_t)G.nv + threadIdx.x];
+    alpha_s[threadIdx.x] = ff_of(a);
+    ialpha_s[threadIdx.x] = 1.f / (float)a;
+  }
+  __syncthreads();
+  const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  const FF alpha[3] = {alpha_s[0], alpha_s[1], alpha_s[2]};
+  const float ialpha[3] = {ialpha_s[0], ialpha_s[1], ialpha_s[2]};
+  // V in float-float; A and the box-scale derivatives with Kahan-compensated FP32 sums
+  FF accV = {0, 0};
+  float ks[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0}, kc[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0};
+  auto kahan = [&](int q, float v) {
+    const float y = v - kc[q], t = ks[q] + y;
+    kc[q] = (t - ks[q]) - y;
+    ks[q] = t;
+  };
+  for (int f = blockIdx.x * kGeoHW + hw; f < G.nfaces; f += gridDim.x * kGeoHW) {
+    int lf;
+    const int gi = geo_group(G, f, &lf);
+    const GeoGroup &g = G.g[gi];
+    // ---- lanes = control points: local coordinates relative to the corner
+    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+    int img[3] = {0, 0, 0};
+    if (lane < g.ncp) {
+      const uint32_t packed = __ldg(&g.cp[(size_t)lf * g.ncp + lane]);
+      const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+      img[0] = code % 3 - 1; img[1] = (code / 3) % 3 - 1; img[2] = code / 9 - 1;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { hi[c] = G.rhi[3 * (size_t)v + c]; lo[c] = G.rlo[3 * (size_t)v + c]; }
+    }
+    FF X0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float ahi = __shfl_sync(hmask, hi[c], 0, 16), alo = __shfl_sync(hmask, lo[c], 0, 16);
+      float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float t, e;
+        two_sum(sh, __fmul_rn((float)img[d], G.box_hi[d][c]), t, e);
+        sh = t;
+        she = __fadd_rn(she, e);
+        shl = __fadd_rn(shl, __fmul_rn((float)img[d], G.box_lo[d][c]));
+      }
+      float s1, e1, s2, e2;
+      two_sum(hi[c], sh, s1, e1);
+      two_sum(s1, -ahi, s2, e2);
+      const float res = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fsub_rn(lo[c], alo), __fadd_rn(she, shl)));
+      const FF xl = ff_mul(alpha[c], ff_fast_two_sum(s2, res));
+      if (lane < g.ncp) { Xh[hw][lane][c] = xl.hi; Xl[hw][lane][c] = xl.lo; }
+      X0[c] = ff_mul(alpha[c], FF{ahi, alo});  // the corner carries no image
+    }
+    __syncwarp(hmask);
+    // ---- lanes = quadrature points
+    if (lane < g.npt) {
+      FF R[3] = {{0, 0}, {0, 0}, {0, 0}}, Ru[3] = {{0, 0}, {0, 0}, {0, 0}}, Rv[3] = {{0, 0}, {0, 0}, {0, 0}};
+#pragma unroll
+      for (int x = 0; x < kMaxCpDev; ++x) {
+        if (x < g.ncp) {
+          const float wh = Bh[gi][lane][0][x], wl = Bl[gi][lane][0][x], uh = Bh[gi][lane][1][x],
+                      ul = Bl[gi][lane][1][x], vh = Bh[gi][lane][2][x], vl = Bl[gi][lane][2][x];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float xh = Xh[hw][x][c], xl = Xl[hw][x][c];
+            ff_acc(R[c], wh, wl, xh, xl);
+            ff_acc(Ru[c], uh, ul, xh, xl);
+            ff_acc(Rv[c], vh, vl, xh, xl);
+          }
+        }
+      }
+      FF Ra[3], m[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Ru[c] = ff_norm(Ru[c]);
+        Rv[c] = ff_norm(Rv[c]);
+        Ra[c] = ff_add(X0[c], ff_norm(R[c]));
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int a = (c + 1) % 3, b = (c + 2) % 3;
+        const FF q = ff_mul(Ru[b], Rv[a]);
+        m[c] = ff_add(ff_mul(Ru[a], Rv[b]), FF{-q.hi, -q.lo});
+      }
+      const FF dot = ff_add(ff_add(ff_mul(Ra[0], m[0]), ff_mul(Ra[1], m[1])), ff_mul(Ra[2], m[2]));
+      const FF vol = ff_mul(c3s[gi][lane], dot);
+      accV = ff_add(accV, vol);
+      // area and box-scale derivatives from the leading parts
+      const float Rf[3] = {Ra[0].hi, Ra[1].hi, Ra[2].hi}, Uf[3] = {Ru[0].hi, Ru[1].hi, Ru[2].hi},
+                  Vf[3] = {Rv[0].hi, Rv[1].hi, Rv[2].hi}, mf[3] = {m[0].hi, m[1].hi, m[2].hi};
+      const float gg2 = mf[0] * mf[0] + mf[1] * mf[1] + mf[2] * mf[2];
+      const float ig = rsqrtf(gg2), gg = gg2 * ig;
+      const float cwf = cws[gi][lane], c3f = c3s[gi][lane].hi;
+      kahan(0, cwf * gg);
+      float n[3] = {mf[0] * ig, mf[1] * ig, mf[2] * ig}, a1[3], a2[3], v1[3], v2[3];
+      cross3(Vf, n, a1);
+      cross3(n, Uf, a2);
+      cross3(Vf, Rf, v1);
+      cross3(Rf, Uf, v2);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        kahan(2 + k, cwf * (a1[k] * Uf[k] + a2[k] * Vf[k]) * ialpha[k]);
+        kahan(5 + k, c3f * (mf[k] * Rf[k] + v1[k] * Uf[k] + v2[k] * Vf[k]) * ialpha[k]);
+      }
+    }
+    __syncwarp(hmask);
+  }
+  double acc[kGeoWords];
+#pragma unroll
+  for (int q = 0; q < kGeoWords; ++q) acc[q] = (double)ks[q] - (double)kc[q];
+  acc[1] = (double)accV.hi + (double)accV.lo;
+  geo_finish(G, acc, red);
+}
+
+// partial[slot] += alpha * dE_r/dX for every (face, control point):
+//   dE_r/dR  = c_V c/3 m,   dE_r/dRu = c_A c (Rv x n) + c_V c/3 (Rv x R),
+//   dE_r/dRv = c_A c (n x Ru) + c_V c/3 (R x Ru),
+// contracted with the w, u, v rows (lanes = points, then lanes = control points).
 template <typename T>
 __global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__restrict__ partial) {
-  const int f = blockIdx.x * kGeoThreads + threadIdx.x;
-  if (f >= G.nfaces) return;
-  const double cA = G.gterm[kGeoCA], cV = G.gterm[kGeoCV];
-  if (cA == 0.0 && cV == 0.0) return;
-  const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
-  int lf;
-  const GeoGroup &g = geo_group(G, f, &lf);
-  GeoFace F;
-  geo_load(G, g, lf, alpha, F);
-  double Gx[kMaxCpDev][3];
-  for (int x = 0; x < F.ncp; ++x) Gx[x][0] = Gx[x][1] = Gx[x][2] = 0.0;
-  for (int p = 0; p < g.npt; ++p) {
-    double R[3], Ru[3], Rv[3], m[3];
-    geo_point(g, F, p, R, Ru, Rv);
-    cross3(Ru, Rv, m);
-    const double gg = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-    const double c = g.dudv * g.weight[p];
-    double n[3] = {m[0] / gg, m[1] / gg, m[2] / gg}, a1[3], a2[3], v1[3], v2[3];
-    cross3(Rv, n, a1);
-    cross3(n, Ru, a2);
-    cross3(Rv, R, v1);
-    cross3(R, Ru, v2);
-    // dE_r/dR, dE_r/dRu, dE_r/dRv at this point
-    double eR[3], eU[3], eV[3];
-    for (int k = 0; k < 3; ++k) {
-      eR[k] = cV * c / 3.0 * m[k];
-      eU[k] = cA * c * a1[k] + cV * c / 3.0 * v1[k];
-      eV[k] = cA * c * a2[k] + cV * c / 3.0 * v2[k];
+  const double cA64 = G.gterm[kGeoCA], cV64 = G.gterm[kGeoCV];
+  if (cA64 == 0.0 && cV64 == 0.0) return;
+  __shared__ GeoBasis<T> sb;
+  __shared__ T Xs[kGeoHW][kMaxCpDev][3];
+  __shared__ T Es[kGeoHW][kGeoPt][9];
+  if constexpr (sizeof(T) == 4) {
+    for (int gi = 0; gi < G.ngroups; ++gi) {
+      const GeoGroup &g = G.g[gi];
+      const int nrow = g.npt * 3 * g.ncp;
+      for (int i = threadIdx.x; i < nrow; i += blockDim.x) sb.B[gi][i / (3 * g.ncp)][(i / g.ncp) % 3][i % g.ncp] = g.tab[i];
+      for (int p = threadIdx.x; p < g.npt; p += blockDim.x) sb.cw[gi][p] = g.tab[2 * nrow + p];
     }
-    const double *bu = g.basis + (size_t)p * 5 * g.ncpp, *bv = bu + g.ncpp, *bw = g.basis_w + (size_t)p * g.ncp;
-    for (int x = 0; x < F.ncp; ++x)
-      for (int k = 0; k < 3; ++k) Gx[x][k] += bw[x] * eR[k] + bu[x] * eU[k] + bv[x] * eV[k];
+  } else {
+    stage_geo_basis<T>(G, sb);
   }
-  for (int x = 0; x < F.ncp; ++x) {
-    const int d = g.dest[(size_t)lf * g.ncp + x];
-    for (int k = 0; k < 3; ++k) partial[3 * (size_t)d + k] = (T)((double)partial[3 * (size_t)d + k] + alpha[k] * Gx[x][k]);
+  __syncthreads();
+  const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  const double a64[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
+  const T alpha[3] = {(T)a64[0], (T)a64[1], (T)a64[2]};
+  const T cA = (T)cA64, cV = (T)cV64;
+  for (int f = blockIdx.x * kGeoHW + hw; f < G.nfaces; f += gridDim.x * kGeoHW) {
+    int lf;
+    const int gi = geo_group(G, f, &lf);
+    const GeoGroup &g = G.g[gi];
+    int dest = 0;
+    T X0[3];
+    if constexpr (sizeof(T) == 8) {
+      double X[3] = {0, 0, 0};
+      if (lane < g.ncp) geo_abs64(G, g, lf, lane, a64, X, &dest);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) X0[c] = shfl_d(hmask, X[c], 0);
+      if (lane < g.ncp)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Xs[hw][lane][c] = X[c] - X0[c];
+    } else {
+      // FP32 coordinates relative to the corner from the hi/lo pairs with
+      // error-free sums, as the face pass forms them.
+      float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+      int img[3] = {0, 0, 0};
+      if (lane < g.ncp) {
+        const uint32_t packed = __ldg(&g.cp[(size_t)lf * g.ncp + lane]);
+        const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+        img[0] = code % 3 - 1; img[1] = (code / 3) % 3 - 1; img[2] = code / 9 - 1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { hi[c] = G.rhi[3 * (size_t)v + c]; lo[c] = G.rlo[3 * (size_t)v + c]; }
+        dest = __ldg(&g.dest[(size_t)lf * g.ncp + lane]);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float ahi = __shfl_sync(hmask, hi[c], 0, 16), alo = __shfl_sync(hmask, lo[c], 0, 16);
+        float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          float t, e;
+          two_sum(sh, (float)img[d] * G.box_hi[d][c], t, e);
+          sh = t;
+          she += e;
+          shl += (float)img[d] * G.box_lo[d][c];
+        }
+        float s1, e1, s2, e2;
+        two_sum(hi[c], sh, s1, e1);
+        two_sum(s1, -ahi, s2, e2);
+        if (lane < g.ncp) Xs[hw][lane][c] = alpha[c] * (s2 + ((e1 + e2) + ((lo[c] - alo) + (she + shl))));
+        X0[c] = alpha[c] * (ahi + alo);  // the corner carries no image (its shift is zero)
+      }
+    }
+    __syncwarp(hmask);
+    if (lane < g.npt) {
+      T R[3] = {0, 0, 0}, Ru[3] = {0, 0, 0}, Rv[3] = {0, 0, 0};
+      const T *bw = sb.B[gi][lane][0], *bu = sb.B[gi][lane][1], *bv = sb.B[gi][lane][2];
+#pragma unroll
+      for (int x = 0; x < kMaxCpDev; ++x) {
+        if (x < g.ncp) {
+          const T w = bw[x], u = bu[x], v = bv[x];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const T xx = Xs[hw][x][c];
+            R[c] += w * xx;
+            Ru[c] += u * xx;
+            Rv[c] += v * xx;
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) R[c] += X0[c];
+      T m[3], n[3], a1[3], a2[3], v1[3], v2[3];
+      cross3(Ru, Rv, m);
+      const T ig = T(1) / sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) n[c] = m[c] * ig;
+      cross3(Rv, n, a1);
+      cross3(n, Ru, a2);
+      cross3(Rv, R, v1);
+      cross3(R, Ru, v2);
+      const T cw = sb.cw[gi][lane], kA = cA * cw, kV = cV * cw * (T(1) / T(3));
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Es[hw][lane][k] = kV * m[k];
+        Es[hw][lane][3 + k] = kA * a1[k] + kV * v1[k];
+        Es[hw][lane][6 + k] = kA * a2[k] + kV * v2[k];
+      }
+    }
+    __syncwarp(hmask);
+    if (lane < g.ncp) {
+      T Gx[3] = {0, 0, 0};
+      for (int p = 0; p < g.npt; ++p) {
+        const T w = sb.B[gi][p][0][lane], u = sb.B[gi][p][1][lane], v = sb.B[gi][p][2][lane];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Gx[k] += w * Es[hw][p][k] + u * Es[hw][p][3 + k] + v * Es[hw][p][6 + k];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) partial[3 * (size_t)dest + k] += alpha[k] * Gx[k];
+    }
+    __syncwarp(hmask);
   }
 }
 
@@ -1729,8 +2058,9 @@ cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, co
 
 namespace umcp {
 
-cudaError_t launch_geo_sums(const GeoArgs &G, cudaStream_t s) {
-  dev::geo_sums_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
+cudaError_t launch_geo_sums(const GeoArgs &G, bool alpha64, cudaStream_t s) {
+  if (alpha64) dev::geo_sums_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
+  else dev::geo_sums_ff_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
   return cudaGetLastError();
 }
 
