@@ -27,6 +27,33 @@ struct FaceSmem {
   Q4<T> Tc[HW][NPT][NCPP + 1];    // point p's contribution to each control point (+1 row pad: no bank conflicts)
   T W[NPT];
   double red[HW][6];
+  __device__ __forceinline__ void *scratch() { return &Tc[0][0][0]; }
+};
+
+// Precision form: control points and per-point contributions are stored
+// coordinate-major, so four control points of one coordinate are one float4
+// and both contractions run as paired FP32 multiply-adds (two control points
+// per instruction).
+//  Xt[hw][c][cp]                 coordinate c of the centred control points
+//  Tc[hw][(c * NPT + p) * TROW + cp]  point p's contribution to control point cp
+// TROW makes the 16-byte row stride odd (conflict-free float4 stores by the
+// point lanes); THW puts the two half-warps of a warp 16 banks apart, so the
+// control-point lanes' scalar reads do not conflict either.
+template <int NCP, int NPT>
+struct FaceSmem<float, NCP, NPT> {
+  static constexpr int NC4 = (NCP + 3) / 4;
+  static constexpr int NCPP = NC4 * 4;
+  static constexpr int HW = FaceCfg<float>::half_warps;
+  static constexpr int TROW = NCPP + ((NC4 % 2 == 0) ? 4 : 0);
+  static constexpr int TSZ = 3 * NPT * TROW;
+  static constexpr int THW = TSZ + (48 - TSZ % 32) % 32;
+  static_assert(THW % 32 == 16 && THW % 4 == 0, "half-warp stride");
+  Q4<float> B[NPT][5][NC4];
+  alignas(16) float Xt[HW][3][NCPP];
+  alignas(16) float Tc[HW][THW];
+  float W[NPT];
+  double red[HW][6];
+  __device__ __forceinline__ void *scratch() { return &Tc[0][0]; }
 };
 
 // Error-free sum: s + e == a + b exactly (Knuth's two-sum).
@@ -163,7 +190,89 @@ __device__ __forceinline__ void stage_basis(FaceSmem<T, NCP, NPT> &sm, const dou
   T *b = &sm.B[0][0][0].x;
   for (int i = threadIdx.x; i < NPT * 5 * NCPP; i += NT) b[i] = (T)basis[i];
   for (int i = threadIdx.x; i < NPT; i += NT) sm.W[i] = (T)weight[i];
-  for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
+  // padding control points stay zero
+  if constexpr (sizeof(T) == 4)
+    for (int i = threadIdx.x; i < HW * 3 * NCPP; i += NT) (&sm.Xt[0][0][0])[i] = 0.f;
+  else
+    for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
+}
+
+// Precision form, lane = quadrature point p: the five contractions, the
+// pointwise energy and adjoint, and p's contribution to every control point.
+// Both contractions use paired FP32 multiply-adds over two control points at
+// once (__ffma2_rn), which halves their instruction count:
+//   K[k]_c = sum_j B[p][k][j] X_c[j]    even j in the pair's first half, odd j
+//                                       in its second; the halves added last
+//   T_c[j] = sum_k B[p][k][j] Kb[k]_c   j, j+1 in one pair, Kb duplicated
+template <int NCP, int NPT>
+__device__ __forceinline__ void point_pass_f32(FaceSmem<float, NCP, NPT> &sm, int hw, int lane,
+                                               const FaceAhead<float> &cur, float dudv, const Moduli<float> &mod,
+                                               bool reg_alpha, float *ea, float *ec, float *er, float dreg[3]) {
+  using S = FaceSmem<float, NCP, NPT>;
+  constexpr int NC4 = S::NC4, TROW = S::TROW;
+  float2 A[5][3];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) A[k][c] = make_float2(0.f, 0.f);
+#pragma unroll 1
+  for (int c4 = 0; c4 < NC4; ++c4) {
+    float4 x[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = *reinterpret_cast<const float4 *>(&sm.Xt[hw][c][4 * c4]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const Q4<float> b = sm.B[lane][k][c4];
+      const float2 b01 = make_float2(b.x, b.y), b23 = make_float2(b.z, b.w);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        A[k][c] = __ffma2_rn(b01, make_float2(x[c].x, x[c].y), A[k][c]);
+        A[k][c] = __ffma2_rn(b23, make_float2(x[c].z, x[c].w), A[k][c]);
+      }
+    }
+  }
+  Vec3<float> K[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
+  Vec3<float> Kb[5], Kreg[2];
+  point_adjoint<float>(K, sm.W[lane], cur.g0, cur.rr0, dudv, cur.P2, cur.Hbar, cur.Pres, mod.kc, mod.KA, mod.kg,
+                       mod.k_reg, ea, ec, er, Kb, Kreg);
+  float2 Kd[5][3];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    Kd[k][0] = make_float2(Kb[k].x, Kb[k].x);
+    Kd[k][1] = make_float2(Kb[k].y, Kb[k].y);
+    Kd[k][2] = make_float2(Kb[k].z, Kb[k].z);
+  }
+  float *tc = &sm.Tc[hw][lane * TROW];
+#pragma unroll 1
+  for (int c4 = 0; c4 < NC4; ++c4) {
+    Q4<float> b[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) b[k] = sm.B[lane][k][c4];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float2 t01 = __fmul2_rn(make_float2(b[0].x, b[0].y), Kd[0][c]);
+      float2 t23 = __fmul2_rn(make_float2(b[0].z, b[0].w), Kd[0][c]);
+#pragma unroll
+      for (int k = 1; k < 5; ++k) {
+        t01 = __ffma2_rn(make_float2(b[k].x, b[k].y), Kd[k][c], t01);
+        t23 = __ffma2_rn(make_float2(b[k].z, b[k].w), Kd[k][c], t23);
+      }
+      *reinterpret_cast<float4 *>(&tc[c * NPT * TROW + 4 * c4]) = make_float4(t01.x, t01.y, t23.x, t23.y);
+    }
+    if (reg_alpha) {
+      // igrad's box-scale derivative takes the angle-term adjoint with one
+      // more alpha factor (src/grad.C:7414-7421).
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float bk0 = (&b[0].x)[j], bk1 = (&b[1].x)[j];
+        dreg[0] += (bk0 * Kreg[0].x + bk1 * Kreg[1].x) * sm.Xt[hw][0][4 * c4 + j];
+        dreg[1] += (bk0 * Kreg[0].y + bk1 * Kreg[1].y) * sm.Xt[hw][1][4 * c4 + j];
+        dreg[2] += (bk0 * Kreg[0].z + bk1 * Kreg[1].z) * sm.Xt[hw][2][4 * c4 + j];
+      }
+    }
+  }
 }
 
 // Energy, adjoint and gradient partials of one face by one half-warp:
@@ -213,13 +322,23 @@ __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, 
       xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl))));
     }
   }
-  if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
+  if constexpr (sizeof(T) == 4) {
+    if (lane < NCP) {
+      sm.Xt[hw][0][lane] = xl[0];
+      sm.Xt[hw][1][lane] = xl[1];
+      sm.Xt[hw][2][lane] = xl[2];
+    }
+  } else {
+    if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
+  }
   __syncwarp(hmask);
 
   // ---- 2. lanes as quadrature points
   T ea = 0, ec = 0, er = 0;
   T dreg[3] = {0, 0, 0};
-  if (lane < NPT) {
+  if constexpr (sizeof(T) == 4) {
+    if (lane < NPT) point_pass_f32<NCP, NPT>(sm, hw, lane, cur, dudv, mod, reg_alpha, &ea, &ec, &er, dreg);
+  } else if (lane < NPT) {
     Vec3<T> K[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) K[k] = {0, 0, 0};
@@ -270,12 +389,23 @@ __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, 
   da[0] = da[1] = da[2] = 0;
   if (lane < NCP) {
     T G0 = 0, G1 = 0, G2 = 0;
+    if constexpr (sizeof(T) == 4) {
+      constexpr int TROW = FaceSmem<T, NCP, NPT>::TROW;
+      const float *tc = &sm.Tc[hw][lane];
 #pragma unroll
-    for (int p = 0; p < NPT; ++p) {
-      const Q4<T> t = sm.Tc[hw][p][lane];
-      G0 += t.x;
-      G1 += t.y;
-      G2 += t.z;
+      for (int p = 0; p < NPT; ++p) {
+        G0 += tc[p * TROW];
+        G1 += tc[(NPT + p) * TROW];
+        G2 += tc[(2 * NPT + p) * TROW];
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < NPT; ++p) {
+        const Q4<T> t = sm.Tc[hw][p][lane];
+        G0 += t.x;
+        G1 += t.y;
+        G2 += t.z;
+      }
     }
     const int d = cur.dest;
     partial[3 * (size_t)d] = alpha[0] * G0;
@@ -364,7 +494,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     if (last) {
       __threadfence();
       static_assert(sizeof(sm.Tc) >= sizeof(double) * 6 * NT, "finish scratch must fit in the transpose buffer");
-      finish_sums<NT>(fin, blockpart, reinterpret_cast<double(*)[NT]>(&sm.Tc[0][0][0]));
+      finish_sums<NT>(fin, blockpart, reinterpret_cast<double(*)[NT]>(sm.scratch()));
       if (threadIdx.x == 0) *fin.done = 0u;
     }
   }
@@ -1180,6 +1310,335 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
   }
 }
 
+// ---------------------------------------------------------------- thread-per-face pass
+//
+// Regular faces of the precision form (12 control points, 15 quadrature
+// points), one face per thread. The thread keeps its face's centred control
+// points X[12][3] and gradient sums G[12][3] in registers and walks the 15
+// points; every thread of a warp reads the same basis row at the same time,
+// so the basis comes out of shared memory as broadcasts (one wavefront per
+// float4) and both contractions are plain multiply-adds on registers:
+//   K[k]_c = sum_j B[p][k][j] X[j]_c          (Ru, Rv, Suu, Suv, Svv)
+//   G[j]_c += sum_k B[p][k][j] Kb[k]_c        (Kb = dE/dK from point_adjoint)
+// Nothing goes through shared memory per face and nothing is shuffled, which
+// removes the transposes and shared-memory traffic of the half-warp form;
+// the FP32 multiply-add pipe is the remaining bound. Energy terms and
+// dE/dalpha are Kahan-summed per thread over its faces and reduced once at
+// the end, in a fixed order.
+namespace tpf {
+constexpr int kNcp = 12, kNpt = 15, kNc4 = 3;
+constexpr int kThreads = 128, kWarps = kThreads / 32, kMinBlocks = 3;
+struct Smem {
+  Q4<float> B[kNpt][5][kNc4];  // basis rows u, v, uu, uv, vv of point p, control points in fours
+  // each thread's centred control points, x[3 j + c] as 9 float4; the
+  // 144-byte stride is an odd number of 16-byte chunks, so the float4 reads
+  // of a warp do not conflict
+  float4 X[kThreads][9];
+  float W[kNpt];
+  double red[kWarps][6];
+};
+// Thread-private float4 in shared memory, stored and loaded through volatile
+// asm so the compiler re-reads it instead of keeping the stored registers
+// alive across the point loop (which is the register pressure this layout
+// exists to avoid).
+__device__ __forceinline__ void st4(float4 *p, float4 v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"((uint32_t)__cvta_generic_to_shared(p)), "f"(v.x),
+               "f"(v.y), "f"(v.z), "f"(v.w));
+}
+__device__ __forceinline__ float4 ld4(const float4 *p) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)));
+  return v;
+}
+}  // namespace tpf
+
+__device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, const double *weight) {
+  float *b = &sm.B[0][0][0].x;
+  for (int i = threadIdx.x; i < tpf::kNpt * 5 * tpf::kNc4 * 4; i += blockDim.x) b[i] = (float)basis[i];
+  for (int i = threadIdx.x; i < tpf::kNpt; i += blockDim.x) sm.W[i] = (float)weight[i];
+}
+
+// Face f's energy terms and dE/dalpha; writes its alpha-scaled gradient
+// partials to the face's slots. vec: cp and dest are 16-byte aligned.
+__device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
+                                         const float alpha[3], const float ialpha[3], const Moduli<float> &mod,
+                                         float dudv, bool vec, float *__restrict__ partial, float e3[3],
+                                         float da[3]) {
+  using namespace tpf;
+  uint32_t cp[kNcp];
+  if (vec) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(S.cp + (size_t)f * kNcp);
+#pragma unroll
+    for (int i = 0; i < kNc4; ++i) {
+      const uint4 v = __ldg(q + i);
+      cp[4 * i] = v.x; cp[4 * i + 1] = v.y; cp[4 * i + 2] = v.z; cp[4 * i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kNcp; ++j) cp[j] = __ldg(&S.cp[(size_t)f * kNcp + j]);
+  }
+  // ---- control points relative to the patch corner (control point 0), in
+  // their lattice images, times alpha; error-free sums on the hi/lo pairs as
+  // in face_compute, so the local coordinates carry full FP32 precision.
+  float X[kNcp][3];
+  float4 *xs = sm.X[threadIdx.x];
+  float ahi[3], alo[3];
+  {
+    const int v0 = (int)(cp[0] & kVertexMask);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { ahi[c] = __ldg(&S.rhi[3 * (size_t)v0 + c]); alo[c] = __ldg(&S.rlo[3 * (size_t)v0 + c]); }
+  }
+#pragma unroll
+  for (int j = 0; j < kNcp; ++j) {
+    const int v = (int)(cp[j] & kVertexMask), code = (int)(cp[j] >> kVertexBits);
+    float hi[3], lo[3], sh[3] = {0.f, 0.f, 0.f}, she[3] = {0.f, 0.f, 0.f}, shl[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { hi[c] = __ldg(&S.rhi[3 * (size_t)v + c]); lo[c] = __ldg(&S.rlo[3 * (size_t)v + c]); }
+    if (code != 13) {  // a periodic image: the lattice shift as hi + lo (each term exact)
+      const int img[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          float t, e;
+          two_sum(sh[c], (float)img[d] * P.box_hi[d][c], t, e);
+          sh[c] = t;
+          she[c] += e;
+          shl[c] += (float)img[d] * P.box_lo[d][c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float s1, e1, s2, e2;
+      two_sum(hi[c], sh[c], s1, e1);
+      two_sum(s1, -ahi[c], s2, e2);
+      X[j][c] = alpha[c] * (s2 + ((e1 + e2) + ((lo[c] - alo[c]) + (she[c] + shl[c]))));
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int q = 4 * i;
+    st4(&xs[i], make_float4(X[q / 3][q % 3], X[(q + 1) / 3][(q + 1) % 3], X[(q + 2) / 3][(q + 2) % 3],
+                            X[(q + 3) / 3][(q + 3) % 3]));
+  }
+  const float P2 = __ldg(&S.compf[3 * (size_t)f]), Hbar = __ldg(&S.compf[3 * (size_t)f + 1]),
+              Pres = __ldg(&S.compf[3 * (size_t)f + 2]);
+  // ---- the quadrature points
+  float G[kNcp][3];
+#pragma unroll
+  for (int j = 0; j < kNcp; ++j) G[j][0] = G[j][1] = G[j][2] = 0.f;
+  float ea = 0.f, ec = 0.f, er = 0.f;
+#pragma unroll 1
+  for (int p = 0; p < kNpt; ++p) {
+    const float g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]), rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
+    float Kf[5][3];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) Kf[k][0] = Kf[k][1] = Kf[k][2] = 0.f;
+#pragma unroll
+    for (int c4 = 0; c4 < kNc4; ++c4) {
+      // control points 4 c4 .. 4 c4 + 3: floats 12 c4 .. 12 c4 + 11
+      const float4 q0 = ld4(&xs[3 * c4]), q1 = ld4(&xs[3 * c4 + 1]), q2 = ld4(&xs[3 * c4 + 2]);
+      const float x[4][3] = {{q0.x, q0.y, q0.z}, {q0.w, q1.x, q1.y}, {q1.z, q1.w, q2.x}, {q2.y, q2.z, q2.w}};
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Q4<float> b = sm.B[p][k][c4];
+        const float bj[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) Kf[k][c] = fmaf(bj[i], x[i][c], Kf[k][c]);
+      }
+    }
+    Vec3<float> K[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) K[k] = {Kf[k][0], Kf[k][1], Kf[k][2]};
+    Vec3<float> Kb[5], Kreg[2];
+    float a, c, r;
+    point_adjoint<float>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a, &c, &r,
+                         Kb, Kreg);
+    ea += a;
+    ec += c;
+    er += r;
+#pragma unroll
+    for (int c4 = 0; c4 < kNc4; ++c4)
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Q4<float> b = sm.B[p][k][c4];
+        const float bj[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          G[4 * c4 + i][0] = fmaf(bj[i], Kb[k].x, G[4 * c4 + i][0]);
+          G[4 * c4 + i][1] = fmaf(bj[i], Kb[k].y, G[4 * c4 + i][1]);
+          G[4 * c4 + i][2] = fmaf(bj[i], Kb[k].z, G[4 * c4 + i][2]);
+        }
+      }
+  }
+  // ---- dE/dalpha_c = sum_j G_jc (X - X_0)_jc (the patch gradient sums to
+  // zero, so coordinates relative to the corner give the same sum); partials
+  {
+    float s[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const float4 q = ld4(&xs[i]);
+      const float v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) s[(4 * i + e) % 3] = fmaf(G[(4 * i + e) / 3][(4 * i + e) % 3], v[e], s[(4 * i + e) % 3]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) da[c] = s[c] * ialpha[c];
+  }
+  int d[kNcp];
+  if (vec) {
+    const int4 *q = reinterpret_cast<const int4 *>(S.dest + (size_t)f * kNcp);
+#pragma unroll
+    for (int i = 0; i < kNc4; ++i) {
+      const int4 v = __ldg(q + i);
+      d[4 * i] = v.x; d[4 * i + 1] = v.y; d[4 * i + 2] = v.z; d[4 * i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kNcp; ++j) d[j] = __ldg(&S.dest[(size_t)f * kNcp + j]);
+  }
+#pragma unroll
+  for (int j = 0; j < kNcp; ++j) {
+    float *o = partial + 3 * (size_t)d[j];
+    o[0] = alpha[0] * G[j][0];
+    o[1] = alpha[1] * G[j][1];
+    o[2] = alpha[2] * G[j][2];
+  }
+  e3[0] = ea; e3[1] = ec; e3[2] = er;
+}
+
+__device__ __forceinline__ bool tpf_vec(const FaceSrc &S) {
+  return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest)) & 15) == 0;
+}
+
+// Sum of q over the warp in a fixed (xor-tree) order.
+__device__ __forceinline__ double warp_sum(double q) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) q += __shfl_xor_sync(0xFFFFFFFFu, q, off);
+  return q;
+}
+
+// Single mesh, regular faces, precision form: persistent grid, warp w of the
+// grid takes faces 32 w .. 32 w + 31, then 32 (w + warps in the grid) ...
+// Writes one block partial of the energy terms and dE/dalpha; the last block
+// to finish sums them (as face_kernel does).
+__global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
+    face_tpf_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
+                    const float *__restrict__ rhi, const float *__restrict__ rlo, float *__restrict__ partial,
+                    double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
+  using namespace tpf;
+  __shared__ Smem sm;
+  __shared__ double scratch[6][kThreads];
+  tpf_stage(sm, L.basis, L.weight);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
+  const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+  const Moduli<float> mod(P);
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
+  const bool vec = tpf_vec(src);
+  const float dudv = (float)L.dudv;
+  HalfWarpSums<float> acc;
+  for (int fb = (blockIdx.x * kWarps + warp) * 32; fb < L.nfaces; fb += gridDim.x * kThreads) {
+    const int f = fb + lane;
+    if (f < L.nfaces) {
+      float e3[3], da[3];
+      tpf_face(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+      acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+      acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
+      if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const double s = warp_sum(acc.get(q));
+    if (lane == 0) sm.red[warp][q] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double s = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) s += sm.red[w][threadIdx.x];
+    blockpart[6 * (size_t)(L.block_base + blockIdx.x) + threadIdx.x] = s;
+  }
+  if (fin.done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      finish_sums<kThreads>(fin, blockpart, scratch);
+      if (threadIdx.x == 0) *fin.done = 0u;
+    }
+  }
+}
+
+// Batched regular faces, precision form: a block takes a tile (faces of one
+// job), its warps 32 faces at a time; writes the tile's three energy sums.
+__global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
+    batch_face_tpf_kernel(const BatchJob *__restrict__ jobs, int group, const BatchTile *__restrict__ tiles,
+                          const int *__restrict__ counts, const double *__restrict__ basis,
+                          const double *__restrict__ weight, double dudv_d, double *__restrict__ tile_sums) {
+  using namespace tpf;
+  __shared__ Smem sm;
+  __shared__ BatchFaceJob sj;
+  __shared__ int s_active;
+  const int ntiles = counts[group], tile_base = counts[3 + group];
+  if ((int)blockIdx.x >= ntiles) return;
+  tpf_stage(sm, basis, weight);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float dudv = (float)dudv_d;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tile = tiles[tile_base + t];
+    __syncthreads();  // the previous tile's readers of sj and sm.red are done
+    {
+      const int *src = reinterpret_cast<const int *>(&jobs[tile.job].f);
+      int *dst = reinterpret_cast<int *>(&sj);
+      for (int i = threadIdx.x; i < (int)(sizeof(BatchFaceJob) / sizeof(int)); i += kThreads) dst[i] = src[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_active = job_active(sj);
+    __syncthreads();
+    HalfWarpSums<float> acc;
+    if (s_active) {
+      const FaceSrc &src = sj.src[group];
+      const SurfaceParams &P = sj.P;
+      const double *r = src.r;
+      const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
+      const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+      const Moduli<float> mod(P);
+      const bool vec = tpf_vec(src);
+      const int end = tile.first + tile.count;
+      for (int fb = tile.first + warp * 32; fb < end; fb += kThreads) {
+        const int f = fb + lane;
+        if (f < end) {
+          float e3[3], da[3];
+          tpf_face(sm, src, P, f, alpha, ialpha, mod, dudv, vec, (float *)sj.partial, e3, da);
+          acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double s = warp_sum(acc.get(q));
+      if (lane == 0) sm.red[warp][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double s = 0;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) s += sm.red[w][threadIdx.x];
+      tile_sums[3 * (size_t)(tile_base + t) + threadIdx.x] = s;
+    }
+  }
+}
+
 // Per job (one warp each): sum its tiles in listed order, record the step's
 // energy in the job's run, flag non-finite or diverging energies (src/hd.C:
 // 1280-1305) for that job only, advance its run index. live[j] tells the
@@ -1888,9 +2347,24 @@ static int face_grid_size(int nfaces) {
   return need < cached ? need : cached;
 }
 
+// The thread-per-face kernel's persistent grid (precision form, regular faces).
+static int face_grid_size_tpf(int nfaces) {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads, 0);
+    cached = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  int need = grid_for(nfaces, dev::tpf::kThreads);
+  return need < cached ? need : cached;
+}
+
 template <typename T>
 int face_blocks(int nfaces, int ncp, int npt) {
   if (nfaces <= 0) return 0;
+  if (sizeof(T) == 4 && ncp == 12 && npt == 15) return face_grid_size_tpf(nfaces);
   if (ncp == 12 && npt == 15) return face_grid_size<T, 12, 15>(nfaces);
   if (ncp == 11 && npt == 16) return face_grid_size<T, 11, 16>(nfaces);
   if (ncp == 13 && npt == 16) return face_grid_size<T, 13, 16>(nfaces);
@@ -1905,6 +2379,13 @@ cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int
                          int *status, int grid, const FinishArgs &fin, cudaStream_t s) {
   if (L.nfaces <= 0) return cudaSuccess;
   constexpr int NT = dev::FaceCfg<T>::threads;
+  if constexpr (sizeof(T) == 4) {
+    if (ncp == 12 && npt == 15) {
+      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status,
+                                                               fin);
+      return cudaGetLastError();
+    }
+  }
   if (ncp == 12 && npt == 15)
     dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
   else if (ncp == 11 && npt == 16)
@@ -2010,6 +2491,13 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
                                const double *basis, const double *weight, int ncp, int npt, double dudv,
                                int irregular, double *tile_sums, int grid, cudaStream_t s) {
   constexpr int NT = dev::FaceCfg<T>::threads;
+  if constexpr (sizeof(T) == 4) {
+    if (ncp == 12 && npt == 15) {
+      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv,
+                                                                     tile_sums);
+      return cudaGetLastError();
+    }
+  }
   if (ncp == 12 && npt == 15)
     dev::batch_face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv, irregular,
                                                           tile_sums);
