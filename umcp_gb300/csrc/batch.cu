@@ -299,13 +299,18 @@ static umcp_status capture(umcp_batch *b, int steps, cudaGraphExec_t *out) {
 // gradient-partial slots and tile sums, which every step rewrites.
 static umcp_status autotune(umcp_batch *b) {
   cudaStream_t s = b->ctx->stream;
-  const int hw = b->precision == UMCP_FP64 ? dev::FaceCfg<double>::half_warps : dev::FaceCfg<float>::half_warps;
+  // FP64: multiples of the half-warp kernel's faces per pass (8 per block of
+  // 64 threads); FP32: multiples of the thread-per-face kernel's 128, up to
+  // 2048, where the per-warp copy pipeline covers more of each tile.
+  const bool f64 = b->precision == UMCP_FP64;
+  const int hw = f64 ? dev::FaceCfg<double>::half_warps : 32;
   cudaEvent_t e0, e1;
   UMCP_CUDA(cudaEventCreate(&e0));
   UMCP_CUDA(cudaEventCreate(&e1));
   int best = 0;
   float best_ms = 0;
-  for (int mult : {1, 2, 4, 8, 16, 32}) {
+  for (int mult : {1, 2, 4, 8, 16, 32, 64}) {
+    if ((f64 && mult > 32) || (!f64 && mult < 4)) continue;
     b->tile_faces = hw * mult;
     umcp_status st = rebuild(b);
     if (st != UMCP_OK) return st;

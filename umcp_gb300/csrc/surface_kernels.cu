@@ -1330,9 +1330,10 @@ constexpr int kNcp = 12, kNpt = 15, kNc4 = 3;
 constexpr int kThreads = 128, kWarps = kThreads / 32, kMinBlocks = 3;
 struct Smem {
   Q4<float> B[kNpt][5][kNc4];  // basis rows u, v, uu, uv, vv of point p, control points in fours
-  // each thread's centred control points, x[3 j + c] as 9 float4; the
-  // 144-byte stride is an odd number of 16-byte chunks, so the float4 reads
-  // of a warp do not conflict
+  // each thread's centred control points, coordinate-major: float4 3 c + q
+  // holds coordinate c of control points 4 q .. 4 q + 3; the 144-byte stride
+  // is an odd number of 16-byte chunks, so the float4 reads of a warp do not
+  // conflict
   float4 X[kThreads][9];
   float W[kNpt];
   double red[kWarps][6];
@@ -1352,6 +1353,49 @@ __device__ __forceinline__ float4 ld4(const float4 *p) {
                : "r"((uint32_t)__cvta_generic_to_shared(p)));
   return v;
 }
+
+// One warp's 32 faces of face tables, copied into shared memory ahead of use
+// with coalesced 16-byte asynchronous copies (the per-point g0/rr0 rows are
+// 60 bytes apart per face, so direct per-thread loads touch a sector per
+// thread). Row r of face lane: cp[12 lane ..], g0/rr0[15 lane + p], comp[3 lane ..].
+struct Stage {
+  uint4 cp[32 * kNcp / 4];
+  float g0[32 * kNpt];
+  float rr0[32 * kNpt];
+  float comp[32 * 3];
+};
+constexpr size_t kStageBytes = sizeof(Stage) * 2 * kWarps;  // double-buffered per warp (dynamic shared memory)
+constexpr size_t kSumBytes = sizeof(float) * 12 * kThreads;    // per-thread Kahan totals (after the stages)
+constexpr int kPrefetchPoint = 7;  // point after which the next faces' positions are prefetched
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
+
+// bytes from src to dst, 16 per lane per round; a short last chunk reads only
+// its own bytes (the rest of the 16 is zero-filled).
+__device__ __forceinline__ void stage_rows(void *dst, const void *src, int bytes, int lane) {
+  for (int o = 16 * lane; o < bytes; o += 512)
+    cp_async16(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, min(16, bytes - o));
+}
+// Queue the copies of faces f0 .. f0 + n - 1 (n <= 32). Needs f0 % 4 == 0 and
+// 16-byte aligned tables (stage_ok).
+__device__ __forceinline__ void stage_issue(Stage &st, const FaceSrc &S, int f0, int n, int lane) {
+  stage_rows(st.cp, S.cp + (size_t)f0 * kNcp, n * kNcp * 4, lane);
+  stage_rows(st.g0, S.g0f + (size_t)f0 * kNpt, n * kNpt * 4, lane);
+  stage_rows(st.rr0, S.rr0f + (size_t)f0 * kNpt, n * kNpt * 4, lane);
+  stage_rows(st.comp, S.compf + (size_t)f0 * 3, n * 12, lane);
+  if (lane < kNcp) prefetch_l2(S.dest + (size_t)f0 * kNcp + 32 * lane);  // read at the faces' end
+}
 }  // namespace tpf
 
 __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, const double *weight) {
@@ -1362,13 +1406,24 @@ __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, co
 
 // Face f's energy terms and dE/dalpha; writes its alpha-scaled gradient
 // partials to the face's slots. vec: cp and dest are 16-byte aligned.
+// STAGED: the face's tables come from cur (row lane) instead of global
+// memory; with next given, the next faces' control-point positions are
+// prefetched into L1 half-way through (every lane of the warp is active then).
+template <bool STAGED>
 __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
                                          const float alpha[3], const float ialpha[3], const Moduli<float> &mod,
                                          float dudv, bool vec, float *__restrict__ partial, float e3[3],
-                                         float da[3]) {
+                                         float da[3], const tpf::Stage *cur = nullptr,
+                                         const tpf::Stage *next = nullptr, int lane = 0) {
   using namespace tpf;
   uint32_t cp[kNcp];
-  if (vec) {
+  if constexpr (STAGED) {
+#pragma unroll
+    for (int i = 0; i < kNc4; ++i) {
+      const uint4 v = cur->cp[kNc4 * lane + i];
+      cp[4 * i] = v.x; cp[4 * i + 1] = v.y; cp[4 * i + 2] = v.z; cp[4 * i + 3] = v.w;
+    }
+  } else if (vec) {
     const uint4 *q = reinterpret_cast<const uint4 *>(S.cp + (size_t)f * kNcp);
 #pragma unroll
     for (int i = 0; i < kNc4; ++i) {
@@ -1418,42 +1473,70 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     }
   }
 #pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    const int q = 4 * i;
-    st4(&xs[i], make_float4(X[q / 3][q % 3], X[(q + 1) / 3][(q + 1) % 3], X[(q + 2) / 3][(q + 2) % 3],
-                            X[(q + 3) / 3][(q + 3) % 3]));
-  }
-  const float P2 = __ldg(&S.compf[3 * (size_t)f]), Hbar = __ldg(&S.compf[3 * (size_t)f + 1]),
-              Pres = __ldg(&S.compf[3 * (size_t)f + 2]);
-  // ---- the quadrature points
-  float G[kNcp][3];
+  for (int c = 0; c < 3; ++c)
 #pragma unroll
-  for (int j = 0; j < kNcp; ++j) G[j][0] = G[j][1] = G[j][2] = 0.f;
-  float ea = 0.f, ec = 0.f, er = 0.f;
+    for (int c4 = 0; c4 < kNc4; ++c4)
+      st4(&xs[kNc4 * c + c4], make_float4(X[4 * c4][c], X[4 * c4 + 1][c], X[4 * c4 + 2][c], X[4 * c4 + 3][c]));
+  float P2, Hbar, Pres;
+  if constexpr (STAGED) {
+    P2 = cur->comp[3 * lane]; Hbar = cur->comp[3 * lane + 1]; Pres = cur->comp[3 * lane + 2];
+  } else {
+    P2 = __ldg(&S.compf[3 * (size_t)f]); Hbar = __ldg(&S.compf[3 * (size_t)f + 1]);
+    Pres = __ldg(&S.compf[3 * (size_t)f + 2]);
+  }
+  // ---- the quadrature points
+  float2 G2[kNcp / 2][3];  // gradient sums of control points 2 i, 2 i + 1 per coordinate
+#pragma unroll
+  for (int i = 0; i < kNcp / 2; ++i) G2[i][0] = G2[i][1] = G2[i][2] = make_float2(0.f, 0.f);
+  float ea = 0.f, ec = 0.f, er = 0.f, dax = 0.f, day = 0.f, daz = 0.f;
 #pragma unroll 1
   for (int p = 0; p < kNpt; ++p) {
-    const float g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]), rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
-    float Kf[5][3];
+    float g0, rr0;
+    if constexpr (STAGED) {
+      g0 = cur->g0[kNpt * lane + p];
+      rr0 = cur->rr0[kNpt * lane + p];
+      if (next && p == kPrefetchPoint) {
+        cp_async_wait<0>();  // the next faces' tables (queued when these faces started) have landed
+        __syncwarp();
 #pragma unroll
-    for (int k = 0; k < 5; ++k) Kf[k][0] = Kf[k][1] = Kf[k][2] = 0.f;
+        for (int i = 0; i < kNc4; ++i) {
+          const uint4 v = next->cp[kNc4 * lane + i];
+          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const size_t o = 3 * (size_t)(w[e] & kVertexMask);
+            prefetch_l1(S.rhi + o);
+            prefetch_l1(S.rlo + o);
+          }
+        }
+      }
+    } else {
+      g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]);
+      rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
+    }
+    // K[k]_c as two partial sums (even, odd control points) in one pair
+    float2 A[5][3];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) A[k][0] = A[k][1] = A[k][2] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int c4 = 0; c4 < kNc4; ++c4) {
-      // control points 4 c4 .. 4 c4 + 3: floats 12 c4 .. 12 c4 + 11
-      const float4 q0 = ld4(&xs[3 * c4]), q1 = ld4(&xs[3 * c4 + 1]), q2 = ld4(&xs[3 * c4 + 2]);
-      const float x[4][3] = {{q0.x, q0.y, q0.z}, {q0.w, q1.x, q1.y}, {q1.z, q1.w, q2.x}, {q2.y, q2.z, q2.w}};
+      float4 x[3];  // coordinate c of control points 4 c4 .. 4 c4 + 3
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] = ld4(&xs[kNc4 * c + c4]);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const Q4<float> b = sm.B[p][k][c4];
-        const float bj[4] = {b.x, b.y, b.z, b.w};
+        const float2 b01 = make_float2(b.x, b.y), b23 = make_float2(b.z, b.w);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) Kf[k][c] = fmaf(bj[i], x[i][c], Kf[k][c]);
+        for (int c = 0; c < 3; ++c) {
+          A[k][c] = __ffma2_rn(b01, make_float2(x[c].x, x[c].y), A[k][c]);
+          A[k][c] = __ffma2_rn(b23, make_float2(x[c].z, x[c].w), A[k][c]);
+        }
       }
     }
     Vec3<float> K[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) K[k] = {Kf[k][0], Kf[k][1], Kf[k][2]};
+    for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
     Vec3<float> Kb[5], Kreg[2];
     float a, c, r;
     point_adjoint<float>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a, &c, &r,
@@ -1462,33 +1545,29 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     ec += c;
     er += r;
 #pragma unroll
-    for (int c4 = 0; c4 < kNc4; ++c4)
+    for (int k = 0; k < 5; ++k) {
+      dax = fmaf(Kb[k].x, K[k].x, dax); day = fmaf(Kb[k].y, K[k].y, day); daz = fmaf(Kb[k].z, K[k].z, daz);
+    }
+    // G[j]_c += sum_k B[p][k][j] Kb[k]_c, control points j, j + 1 in one pair
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 5; ++k) {
+      const float2 kd[3] = {make_float2(Kb[k].x, Kb[k].x), make_float2(Kb[k].y, Kb[k].y),
+                            make_float2(Kb[k].z, Kb[k].z)};
+#pragma unroll
+      for (int c4 = 0; c4 < kNc4; ++c4) {
         const Q4<float> b = sm.B[p][k][c4];
-        const float bj[4] = {b.x, b.y, b.z, b.w};
+        const float2 b01 = make_float2(b.x, b.y), b23 = make_float2(b.z, b.w);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          G[4 * c4 + i][0] = fmaf(bj[i], Kb[k].x, G[4 * c4 + i][0]);
-          G[4 * c4 + i][1] = fmaf(bj[i], Kb[k].y, G[4 * c4 + i][1]);
-          G[4 * c4 + i][2] = fmaf(bj[i], Kb[k].z, G[4 * c4 + i][2]);
+        for (int c = 0; c < 3; ++c) {
+          G2[2 * c4][c] = __ffma2_rn(b01, kd[c], G2[2 * c4][c]);
+          G2[2 * c4 + 1][c] = __ffma2_rn(b23, kd[c], G2[2 * c4 + 1][c]);
         }
       }
-  }
-  // ---- dE/dalpha_c = sum_j G_jc (X - X_0)_jc (the patch gradient sums to
-  // zero, so coordinates relative to the corner give the same sum); partials
-  {
-    float s[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      const float4 q = ld4(&xs[i]);
-      const float v[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-      for (int e = 0; e < 4; ++e) s[(4 * i + e) % 3] = fmaf(G[(4 * i + e) / 3][(4 * i + e) % 3], v[e], s[(4 * i + e) % 3]);
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) da[c] = s[c] * ialpha[c];
   }
+  // ---- dE/dalpha_c: K is linear in the alpha-scaled coordinates, so
+  // alpha_c dE/dalpha_c = sum over points and k of Kb[k]_c K[k]_c
+  da[0] = dax * ialpha[0]; da[1] = day * ialpha[1]; da[2] = daz * ialpha[2];
   int d[kNcp];
   if (vec) {
     const int4 *q = reinterpret_cast<const int4 *>(S.dest + (size_t)f * kNcp);
@@ -1504,9 +1583,8 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
 #pragma unroll
   for (int j = 0; j < kNcp; ++j) {
     float *o = partial + 3 * (size_t)d[j];
-    o[0] = alpha[0] * G[j][0];
-    o[1] = alpha[1] * G[j][1];
-    o[2] = alpha[2] * G[j][2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o[c] = alpha[c] * ((j & 1) ? G2[j / 2][c].y : G2[j / 2][c].x);
   }
   e3[0] = ea; e3[1] = ec; e3[2] = er;
 }
@@ -1514,6 +1592,32 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
 __device__ __forceinline__ bool tpf_vec(const FaceSrc &S) {
   return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest)) & 15) == 0;
 }
+// The face tables can be staged with 16-byte copies.
+__device__ __forceinline__ bool tpf_stage_ok(const FaceSrc &S) {
+  return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest) |
+           reinterpret_cast<uintptr_t>(S.g0f) | reinterpret_cast<uintptr_t>(S.rr0f) |
+           reinterpret_cast<uintptr_t>(S.compf)) & 15) == 0;
+}
+
+// Kahan-compensated FP32 totals of one thread, kept in shared memory (its
+// column of s[12][kThreads]) rather than in registers, which the face loop
+// needs for itself.
+struct SharedSums {
+  float *s;
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int q = 0; q < 12; ++q) s[q * tpf::kThreads] = 0.f;
+  }
+  __device__ __forceinline__ void add(int q, float v) {
+    float sum = s[2 * q * tpf::kThreads], c = s[(2 * q + 1) * tpf::kThreads];
+    const float y = v - c, t = sum + y;
+    s[(2 * q + 1) * tpf::kThreads] = (t - sum) - y;
+    s[2 * q * tpf::kThreads] = t;
+  }
+  __device__ __forceinline__ double get(int q) const {
+    return (double)s[2 * q * tpf::kThreads] - (double)s[(2 * q + 1) * tpf::kThreads];
+  }
+};
 
 // Sum of q over the warp in a fixed (xor-tree) order.
 __device__ __forceinline__ double warp_sum(double q) {
@@ -1532,7 +1636,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
                     double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
   using namespace tpf;
   __shared__ Smem sm;
-  __shared__ double scratch[6][kThreads];
+  extern __shared__ __align__(16) unsigned char tpf_dyn[];
+  Stage *stages = reinterpret_cast<Stage *>(tpf_dyn);  // [warp][2]
   tpf_stage(sm, L.basis, L.weight);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1540,19 +1645,39 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
   const Moduli<float> mod(P);
   const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
-  const bool vec = tpf_vec(src);
+  // the launch wrapper checks that the tables are 16-byte aligned (tpf_stage_ok)
   const float dudv = (float)L.dudv;
-  HalfWarpSums<float> acc;
-  for (int fb = (blockIdx.x * kWarps + warp) * 32; fb < L.nfaces; fb += gridDim.x * kThreads) {
+  const int n = L.nfaces, stride = gridDim.x * kThreads;
+  Stage *st = stages + 2 * warp;
+  SharedSums acc{reinterpret_cast<float *>(tpf_dyn + kStageBytes) + threadIdx.x};
+  acc.zero();
+  // Faces fb .. fb + 31 compute from st[buf] while the next 32 (fb + stride)
+  // are copied into st[buf ^ 1]. Only the last 32 of the mesh can be
+  // partial, and they have no successor, so every lane is active whenever a
+  // next stage exists.
+  int fb = (blockIdx.x * kWarps + warp) * 32, buf = 0;
+  if (fb < n) stage_issue(st[0], src, fb, min(32, n - fb), lane);
+  cp_async_commit();
+  for (; fb < n; fb += stride) {
+    const int nb = fb + stride;
+    if (nb < n) stage_issue(st[buf ^ 1], src, nb, min(32, n - nb), lane);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
     const int f = fb + lane;
-    if (f < L.nfaces) {
+    if (f < n) {
       float e3[3], da[3];
-      tpf_face(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+      tpf_face<true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                     nb < n ? &st[buf ^ 1] : nullptr, lane);
       acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
       acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
       if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
     }
+    __syncwarp();  // st[buf] is rewritten by the next round's copies
+    buf ^= 1;
   }
+  cp_async_wait<0>();
+  __syncthreads();  // the stage buffers double as the finish scratch below
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
     const double s = warp_sum(acc.get(q));
@@ -1573,7 +1698,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     __syncthreads();
     if (last) {
       __threadfence();
-      finish_sums<kThreads>(fin, blockpart, scratch);
+      static_assert(kStageBytes >= sizeof(double) * 6 * kThreads, "finish scratch must fit in the stage buffers");
+      finish_sums<kThreads>(fin, blockpart, reinterpret_cast<double(*)[kThreads]>(tpf_dyn));
       if (threadIdx.x == 0) *fin.done = 0u;
     }
   }
@@ -1589,6 +1715,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   __shared__ Smem sm;
   __shared__ BatchFaceJob sj;
   __shared__ int s_active;
+  extern __shared__ __align__(16) unsigned char tpf_dyn[];
+  Stage *st = reinterpret_cast<Stage *>(tpf_dyn) + 2 * (threadIdx.x >> 5);  // this warp's two stages
   const int ntiles = counts[group], tile_base = counts[3 + group];
   if ((int)blockIdx.x >= ntiles) return;
   tpf_stage(sm, basis, weight);
@@ -1613,14 +1741,40 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
       const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
       const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
       const Moduli<float> mod(P);
-      const bool vec = tpf_vec(src);
       const int end = tile.first + tile.count;
-      for (int fb = tile.first + warp * 32; fb < end; fb += kThreads) {
-        const int f = fb + lane;
-        if (f < end) {
-          float e3[3], da[3];
-          tpf_face(sm, src, P, f, alpha, ialpha, mod, dudv, vec, (float *)sj.partial, e3, da);
-          acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+      float *partial = (float *)sj.partial;
+      if (tpf_stage_ok(src) && tile.first % 4 == 0) {
+        // the single-mesh pipeline within the tile: this warp's next 32 faces
+        // are copied while the current 32 compute
+        int fb = tile.first + warp * 32, buf = 0;
+        if (fb < end) stage_issue(st[0], src, fb, min(32, end - fb), lane);
+        cp_async_commit();
+        for (; fb < end; fb += kThreads) {
+          const int nb = fb + kThreads;
+          if (nb < end) stage_issue(st[buf ^ 1], src, nb, min(32, end - nb), lane);
+          cp_async_commit();
+          cp_async_wait<1>();
+          __syncwarp();
+          const int f = fb + lane;
+          if (f < end) {
+            float e3[3], da[3];
+            tpf_face<true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                           nb < end ? &st[buf ^ 1] : nullptr, lane);
+            acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+          }
+          __syncwarp();
+          buf ^= 1;
+        }
+        cp_async_wait<0>();
+      } else {
+        const bool vec = tpf_vec(src);
+        for (int fb = tile.first + warp * 32; fb < end; fb += kThreads) {
+          const int f = fb + lane;
+          if (f < end) {
+            float e3[3], da[3];
+            tpf_face<false>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+            acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
+          }
         }
       }
     }
@@ -2354,7 +2508,10 @@ static int face_grid_size_tpf(int nfaces) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads, 0);
+    cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads,
+                                                  dev::tpf::kStageBytes + dev::tpf::kSumBytes);
     cached = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   }
   int need = grid_for(nfaces, dev::tpf::kThreads);
@@ -2381,8 +2538,19 @@ cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int
   constexpr int NT = dev::FaceCfg<T>::threads;
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
-      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status,
-                                                               fin);
+      const uintptr_t al = reinterpret_cast<uintptr_t>(L.cp) | reinterpret_cast<uintptr_t>(dest) |
+                           reinterpret_cast<uintptr_t>(L.g0f) | reinterpret_cast<uintptr_t>(L.rr0f) |
+                           reinterpret_cast<uintptr_t>(L.compf);
+      if (al & 15) return cudaErrorMisalignedAddress;  // the kernel stages the tables with 16-byte copies
+      static bool attr = false;
+      if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
+        if (e != cudaSuccess) return e;
+        attr = true;
+      }
+      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes + dev::tpf::kSumBytes, s>>>(
+          L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
       return cudaGetLastError();
     }
   }
@@ -2493,8 +2661,15 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
   constexpr int NT = dev::FaceCfg<T>::threads;
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
-      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(jobs, group, tiles, counts, basis, weight, dudv,
-                                                                     tile_sums);
+      static bool attr = false;
+      if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(dev::batch_face_tpf_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dev::tpf::kStageBytes);
+        if (e != cudaSuccess) return e;
+        attr = true;
+      }
+      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes, s>>>(
+          jobs, group, tiles, counts, basis, weight, dudv, tile_sums);
       return cudaGetLastError();
     }
   }
