@@ -67,10 +67,10 @@ L2_BYTES = 129 * 1024 * 1024
 SM_COUNT, FP32_LANES_PER_SM = 152, 128
 # DRAM bytes per face of the batched face launches, from the ncu capture of
 # the first 64 vesicles of the workload (dram__bytes_read.sum +
-# dram__bytes_write.sum of the regular and valence-5 launches: 98.78 + 26.00
-# + 2.17 + 0.00 MB over 392,960 faces); the benchmark's pass is scaled from
+# dram__bytes_write.sum of the regular and valence-5 launches: 97.51 + 23.80
+# + 2.17 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled from
 # it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 126.95e6 / 392960
+BATCH_FACE_DRAM_BYTES_PER_FACE = 123.50e6 / 392960
 
 
 def parse_args():
@@ -458,7 +458,8 @@ def engine_arm(args) -> None:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"],
                      "traffic": (BATCH_FACE_DRAM_BYTES_PER_FACE * nfaces) if BATCH_FACE_DRAM_BYTES_PER_FACE else None,
-                     "kernel": "batch_face_kernel (regular, valence-5 and valence-7 launches of one step)",
+                     "kernel": "batch_face_tpf_kernel (regular faces) and batch_face_kernel (valence-5 and "
+                               "valence-7 faces): the face launches of one step",
                      "launch_ms": face_ms, "algorithmic_bytes_per_launch": byts, "peak_source": peaks["source"],
                      "compute": {"fp32_tflops": flops / (face_ms / 1e3) / 1e12, "fp32_simt_peak_tflops": fp32_peak,
                                  "frac": flops / (face_ms / 1e3) / 1e12 / fp32_peak,
