@@ -303,7 +303,9 @@ umcp_status umcp_mesh_energies(umcp_mesh *mesh, double *energies, int64_t n);
  * one fused gather + update. */
 typedef struct umcp_batch umcp_batch;
 typedef struct {
-  int tile_faces;     /* faces per tile (one block's unit of work); 0: chosen by timing at the first run */
+  int tile_faces;     /* faces per tile of regular faces (one block's unit of work); 0: chosen by timing at the
+                         first run. Irregular faces use tiles of at most 4 faces per half-warp (32 in the FP32
+                         form, 16 in FP64). */
   int blocks_per_sm;  /* cap on the persistent face grid; 0: the occupancy limit */
 } umcp_batch_opts;
 typedef struct {

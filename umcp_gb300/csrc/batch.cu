@@ -150,13 +150,18 @@ static umcp_status rebuild(umcp_batch *b) {
   std::vector<BatchTile> tiles, vtiles;
   std::vector<std::vector<int>> per_job(b->jobs.size());
   for (const Job &J : b->jobs) jt.push_back(job_entry(J));
+  // Irregular faces (a few dozen per closed vesicle) go in tiles of at most
+  // four faces per half-warp of their kernel, so that they spread over the
+  // grid instead of queueing on one block per job.
+  const int hw = b->precision == UMCP_FP64 ? dev::FaceCfg<double>::half_warps : dev::FaceCfg<float>::half_warps;
   for (int t = 0; t < kTypes; ++t) {
     b->counts[kCountTileBase + t] = (int)tiles.size();
+    const int tft = t == 0 ? tf : std::min(tf, 4 * hw);
     for (size_t j = 0; j < b->jobs.size(); ++j) {
       const int nf = jt[j].f.src[t].nfaces;
-      for (int first = 0; first < nf; first += tf) {
+      for (int first = 0; first < nf; first += tft) {
         per_job[j].push_back((int)tiles.size());
-        tiles.push_back(BatchTile{(int)j, first, std::min(tf, nf - first)});
+        tiles.push_back(BatchTile{(int)j, first, std::min(tft, nf - first)});
       }
     }
     b->counts[kCountTiles + t] = (int)tiles.size() - b->counts[kCountTileBase + t];
