@@ -432,11 +432,14 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   }
   m->nfaces = face_base;
   m->nslots = slot_base;
-  // Vertex-major destination of every (face, control point) slot.
-  std::vector<int> off(ME.nv + 1, 0), dest(slot_base, -1);
-  for (int v = 0; v < ME.nv; ++v) off[v + 1] = off[v] + (int)vslots[v].size();
+  // Destination of every (face, control point) slot in the interleaved
+  // numbering: the k-th slot of vertex v at loc[2 v] + 32 k, in ascending
+  // order of (face, control point), which is the order the gather sums them.
+  std::vector<int> counts(ME.nv), off, dest(slot_base, -1);
+  for (int v = 0; v < ME.nv; ++v) counts[v] = (int)vslots[v].size();
+  m->nslot_cap = (int)interleave_slots(counts, &off);
   for (int v = 0; v < ME.nv; ++v)
-    for (size_t k = 0; k < vslots[v].size(); ++k) dest[vslots[v][k]] = off[v] + (int)k;
+    for (size_t k = 0; k < vslots[v].size(); ++k) dest[vslots[v][k]] = off[2 * (size_t)v] + 32 * (int)k;
   for (auto &G : m->groups) {
     std::vector<int> d(dest.begin() + G->slot_base, dest.begin() + G->slot_base + (size_t)G->nfaces * G->ncp);
     UMCP_CUDA(upload(G->dest, d));
@@ -446,7 +449,7 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   UMCP_CUDA(m->blockpart.alloc((size_t)(block_rows > 0 ? block_rows : 1) * 6 * sizeof(double)));
   UMCP_CUDA(cudaMemset(m->blockpart.p, 0, m->blockpart.bytes));
   const size_t elem = (m->precision == UMCP_FP64) ? sizeof(double) : sizeof(float);
-  UMCP_CUDA(m->partial.alloc((size_t)slot_base * 3 * elem));
+  UMCP_CUDA(m->partial.alloc((size_t)m->nslot_cap * 3 * elem));
   const size_t nst = 3 * (size_t)ME.nv + 3;
   UMCP_CUDA(m->r.alloc(nst * sizeof(double)));
   UMCP_CUDA(m->g.alloc(nst * sizeof(double)));
@@ -500,6 +503,29 @@ extern "C" umcp_status umcp_mesh_set_params(umcp_mesh *mesh, const umcp_params *
   mesh->drop_graphs();
   if (mesh->batch) batch_mesh_changed(mesh->batch);  // its job entry holds the parameters
   return UMCP_OK;
+}
+
+// Slot numbering of the gradient partials. Vertices go in groups of 32 (one
+// warp of the gather); slot k of vertex 32 g + t is base_g + 32 k + t, and
+// base_g advances by 32 times the group's largest slot count. A warp's gather
+// then reads 32 consecutive slots per k instead of 32 strided runs. Fills
+// loc[2 v] = base_g + t and loc[2 v + 1] = count of v; returns the slots to
+// allocate (the padding slots are neither written nor read).
+size_t umcp::interleave_slots(const std::vector<int> &counts, std::vector<int> *loc) {
+  const size_t nv = counts.size();
+  loc->assign(2 * nv, 0);
+  size_t base = 0;
+  for (size_t g0 = 0; g0 < nv; g0 += 32) {
+    const size_t g1 = std::min(nv, g0 + 32);
+    int most = 0;
+    for (size_t v = g0; v < g1; ++v) most = std::max(most, counts[v]);
+    for (size_t v = g0; v < g1; ++v) {
+      (*loc)[2 * v] = (int)(base + (v - g0));
+      (*loc)[2 * v + 1] = counts[v];
+    }
+    base += 32 * (size_t)most;
+  }
+  return base;
 }
 
 int umcp::group_blocks(int precision, bool tc, int ncp, int npt, int nfaces) {
@@ -729,14 +755,19 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
   const Plan &PL = plan->plan;
   const size_t nv = (size_t)plan->mesh.nv, nst = 3 * nv + 3;
   const bool f32 = precision == UMCP_FP32_CENTRED;
-  size_t b = 0, slots = 0;
+  size_t b = 0;
   int nblocks = 0;
+  std::vector<int> counts(nv, 0), loc;
+  for (const Face &F : PL.reg_faces)
+    for (int x = 0; x < PL.regular.ncp; ++x) ++counts[F.cp[x]];
+  for (const Face &F : PL.irr_faces)
+    for (int x = 0; x < PL.irregular[F.valence].ncp; ++x) ++counts[F.cp[x]];
+  const size_t slots = interleave_slots(counts, &loc);
   auto group = [&](const PatchBasis &B, size_t nf) {
     const size_t ncpp = (size_t)(B.ncp + 3) / 4 * 4;
     b += nf * B.ncp * 4 + 2 * nf * B.npt * 8 + nf * 3 * 8 + (size_t)B.npt * 5 * ncpp * 8 + B.weight.size() * 8 +
          nf * B.ncp * 4 + (size_t)B.npt * B.ncp * 8;
     if (f32) b += 2 * nf * B.npt * 4 + nf * 3 * 4;
-    slots += nf * B.ncp;
     nblocks += group_block_rows(precision, B.ncp, B.npt, (int)nf);
   };
   group(PL.regular, PL.reg_faces.size());
@@ -745,7 +776,7 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
     for (const Face &F : PL.irr_faces) nf += F.valence == val;
     if (nf) group(PL.irregular[val], nf);
   }
-  b += (nv + 1) * 4;                                  // off
+  b += 2 * nv * 4;                                    // slot locations
   b += (size_t)std::max(nblocks, 1) * 6 * 8;          // blockpart
   b += slots * 3 * (f32 ? 4 : 8);                     // partial
   b += 3 * nst * 8 + 2 * 3 * nv * 8;                  // r, g, r_eval; p, qdot
@@ -1158,7 +1189,7 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
   // layout: [status, done] | block partials | gradient partials | FP32 position pairs
   const size_t off_flags = 0, off_block = 256;
   const size_t off_partial = off_block + align256((size_t)m->nblocks * 6 * sizeof(double));
-  const size_t off_hi = off_partial + align256((size_t)m->nslots * 3 * esize);
+  const size_t off_hi = off_partial + align256((size_t)m->nslot_cap * 3 * esize);
   const size_t off_lo = off_hi + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
   const size_t need = off_lo + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
   if (need > kStaticScratchBytes)

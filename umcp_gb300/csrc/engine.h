@@ -68,6 +68,7 @@ inline void ctx_release(umcp_ctx *c) {
 struct umcp_mesh {
   umcp_ctx *ctx = nullptr;
   int nv = 0, nfaces = 0, nslots = 0;
+  int nslot_cap = 0;  // partial slots allocated: nslots plus the padding of the interleaved numbering
   int precision = UMCP_FP64;
   umcp::dev::SurfaceParams P{};
   std::vector<std::unique_ptr<umcp::Group>> groups;
@@ -156,6 +157,7 @@ void batch_mesh_changed(umcp_batch *b);
 // reserves (the larger of the two kernels' grids, so the footprint does not
 // depend on the kernel choice).
 int group_blocks(int precision, bool tc, int ncp, int npt, int nfaces);
+size_t interleave_slots(const std::vector<int> &counts, std::vector<int> *loc);
 int group_block_rows(int precision, int ncp, int npt, int nfaces);
 
 inline uint32_t pack_cp(int v, const int8_t img[3]) {

@@ -103,7 +103,8 @@ cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo,
 // flags (src/hd.C:1280-1305), cnt[1] += 1.
 cudaError_t launch_finish(const FinishArgs &F, const double *blockpart, cudaStream_t s);
 
-// Per vertex: g[3v+c] += sum of its partial slots [off[v], off[v+1]).
+// Per vertex: g[3v+c] += sum of its partial slots off[2v] + 32 k, k < off[2v+1]
+// (32 vertices interleaved per group, see interleave_slots).
 template <typename T>
 cudaError_t launch_gather(int nv, const T *partial, const int *off, double *g, cudaStream_t s);
 
@@ -143,7 +144,7 @@ struct BatchFaceJob {
 };
 struct BatchJob {
   BatchFaceJob f;
-  const int *off;          // vertex slot offsets
+  const int *off;          // vertex slot locations {first slot, count} (interleaved numbering)
   double *r, *p;           // state
   float *rhi, *rlo;        // FP32 hi/lo pairs of r (precision form), else NULL
   double *E, *parts;       // energy (and parts) of the latest step

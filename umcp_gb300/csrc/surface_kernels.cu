@@ -1058,26 +1058,33 @@ __global__ void finish_kernel(FinishArgs F, const double *__restrict__ blockpart
 
 // Sum of a vertex's gradient partials in slot order: FP64 in the plain path,
 // FP32 with Kahan compensation in the precision form.
+// Sum of vertex v's gradient partials: its slots are loc[2 v] + 32 k for
+// k < loc[2 v + 1] (32 vertices interleaved, so the 32 lanes of a warp read
+// consecutive slots), summed in k order (FP64, or Kahan FP32).
 template <typename T>
-__device__ __forceinline__ void vertex_gradient(const T *__restrict__ partial, const int *__restrict__ off, int v,
+__device__ __forceinline__ void vertex_gradient(const T *__restrict__ partial, const int *__restrict__ loc, int v,
                                                 double gg[3]) {
+  const int base = loc[2 * (size_t)v], n = loc[2 * (size_t)v + 1];
   if constexpr (sizeof(T) == 8) {
     double a0 = 0, a1 = 0, a2 = 0;
-    for (int s = off[v]; s < off[v + 1]; ++s) {
-      a0 += partial[3 * (size_t)s];
-      a1 += partial[3 * (size_t)s + 1];
-      a2 += partial[3 * (size_t)s + 2];
+    for (int k = 0; k < n; ++k) {
+      const size_t s = (size_t)base + 32 * (size_t)k;
+      a0 += partial[3 * s];
+      a1 += partial[3 * s + 1];
+      a2 += partial[3 * s + 2];
     }
     gg[0] = a0; gg[1] = a1; gg[2] = a2;
   } else {
     float s3[3] = {0, 0, 0}, c3[3] = {0, 0, 0};
-    for (int s = off[v]; s < off[v + 1]; ++s)
+    for (int k = 0; k < n; ++k) {
+      const size_t s = (size_t)base + 32 * (size_t)k;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float y = partial[3 * (size_t)s + c] - c3[c], t = s3[c] + y;
+        const float y = partial[3 * s + c] - c3[c], t = s3[c] + y;
         c3[c] = (t - s3[c]) - y;
         s3[c] = t;
       }
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) gg[c] = (double)s3[c] - (double)c3[c];
   }
