@@ -809,7 +809,7 @@ extern "C" umcp_status umcp_mass_set(umcp_mesh *m, int nrow, const int *row_ptr,
   m->mass_f32 = m->precision == UMCP_FP32_CENTRED;  // the precision form applies M^-1 in FP32
   if (m->mass_f32) UMCP_CUDA(upload(m->mval, std::vector<float>(val, val + nnz)));
   else UMCP_CUDA(upload(m->mval, std::vector<double>(val, val + nnz)));
-  UMCP_CUDA(m->min32.alloc(m->mass_f32 ? 3 * (size_t)nrow * sizeof(float) : 0));
+  UMCP_CUDA(m->min32.alloc(m->mass_f32 ? (size_t)nrow * sizeof(float4) : 0));
   UMCP_CUDA(m->mdense.alloc(0));
   m->mass_dense = false;
   m->mrows = nrow;

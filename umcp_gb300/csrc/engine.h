@@ -94,7 +94,7 @@ struct umcp_mesh {
   uint64_t *h_cnt = nullptr;  // pinned, 2 counters
   // effective inverse mass: CSR (mrow, mcol, mval) or dense row-major (mdense);
   // FP64 values, or FP32 ones for meshes of the precision form (mass_f32),
-  // whose apply reads an FP32 copy of its input (min32, 3 nv floats)
+  // whose apply reads an FP32 copy of its input (min32, nv float4 {x, y, z, 0})
   int mrows = 0;
   umcp::DevBuf mrow, mcol, mval, alphas, mdense, min32;
   bool mass_dense = false, mass_f32 = false;

@@ -187,12 +187,13 @@ int batch_face_blocks(int ncp, int npt);
 
 // out[3i+c] (+)= scale/alpha_c^2 * (scalev ? scalev[c*nrow+i] : 1) * sum_k val[k] in[3 col[k]+c].
 // accumulate=0 overwrites out. alphas: device pointer to 3 doubles (or NULL = 1).
-// launch_spmv on FP32 values and an FP32 input (spmv32_kernel).
+// launch_spmv on FP32 values and an FP32 input packed as float4 {x, y, z, 0}
+// per row (spmv32_kernel).
 cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
-                          double scale, const double *alphas, const float *in, double *out, int accumulate,
+                          double scale, const double *alphas, const float4 *in, double *out, int accumulate,
                           cudaStream_t s);
-// out[i] = (float)in[i], i < n.
-cudaError_t launch_to_f32(size_t n, const double *in, float *out, cudaStream_t s);
+// out[i] = {(float)in[3i], (float)in[3i+1], (float)in[3i+2], 0}, i < n.
+cudaError_t launch_to_f32x4(int n, const double *in, float4 *out, cudaStream_t s);
 cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const double *val, const double *scalev,
                         double scale, const double *alphas, const double *in, double *out, int accumulate,
                         cudaStream_t s);

@@ -138,7 +138,7 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
 // dense_apply_kernel on FP32 values and an FP32 input: Kahan-compensated FP32
 // sums per thread, the block reduction and the scaling in FP64.
 __global__ void dense_apply32_kernel(int n, const float *__restrict__ A, const double *__restrict__ scalev,
-                                     double scale, const double *__restrict__ alphas, const float *__restrict__ in,
+                                     double scale, const double *__restrict__ alphas, const float4 *__restrict__ in4,
                                      double *__restrict__ out, int accumulate) {
   __shared__ double red[3][8];
   for (int i = blockIdx.x; i < n; i += gridDim.x) {
@@ -146,9 +146,11 @@ __global__ void dense_apply32_kernel(int n, const float *__restrict__ A, const d
     float s[3] = {0, 0, 0}, c[3] = {0, 0, 0};
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
       const float m = row[j];
+      const float4 x4 = in4[j];
+      const float x[3] = {x4.x, x4.y, x4.z};
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        const float y = m * in[3 * (size_t)j + q] - c[q], t = s[q] + y;
+        const float y = m * x[q] - c[q], t = s[q] + y;
         c[q] = (t - s[q]) - y;
         s[q] = t;
       }
@@ -184,11 +186,11 @@ __global__ void dense_to_f32_kernel(size_t total, const double *__restrict__ A, 
 cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double scale, const double *alphas,
                                    const double *in, double *out, int accumulate, cudaStream_t s) {
   if (m->mass_f32) {
-    cudaError_t e = launch_to_f32(3 * (size_t)m->mrows, in, m->min32.as<float>(), s);
+    cudaError_t e = launch_to_f32x4(m->mrows, in, m->min32.as<float4>(), s);
     if (e != cudaSuccess) return e;
     if (!m->mass_dense)
       return launch_spmv32(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<float>(), scalev, scale, alphas,
-                           m->min32.as<float>(), out, accumulate, s);
+                           m->min32.as<float4>(), out, accumulate, s);
   }
   if (m->mass_dense) {
     int sms = 152;
@@ -196,7 +198,7 @@ cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double sc
     const int grid = m->mrows < sms * 8 ? m->mrows : sms * 8;
     if (m->mass_f32)
       dense_apply32_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<float>(), scalev, scale, alphas,
-                                                m->min32.as<float>(), out, accumulate);
+                                                m->min32.as<float4>(), out, accumulate);
     else
       dense_apply_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<double>(), scalev, scale, alphas, in, out,
                                               accumulate);
@@ -313,7 +315,7 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
     m->mass_dense = false;
   }
   m->mass_f32 = f32;
-  UMCP_CUDA(m->min32.alloc(f32 ? 3 * (size_t)n * sizeof(float) : 0));
+  UMCP_CUDA(m->min32.alloc(f32 ? (size_t)n * sizeof(float4) : 0));
   m->mrows = n;
   if (info) {
     memset(info, 0, sizeof(*info));

@@ -2436,13 +2436,16 @@ __global__ void spmv_kernel(int nrow, const int *__restrict__ row_ptr, const int
   }
 }
 
-// spmv_kernel on FP32 values and an FP32 copy of the input (the precision
-// form's inverse mass): Kahan-compensated FP32 sums per lane, the cross-lane
-// sum and the scaling in FP64. Reads 8 bytes per nonzero instead of 12 and
-// keeps the FP64 pipe out of the loop.
+// spmv_kernel on FP32 values and an FP32 copy of the input packed as one
+// float4 per row {x, y, z, 0} (the precision form's inverse mass), so each
+// nonzero gathers its input with one 16-byte load. kSpmvUnroll nonzeros per
+// lane per round have their loads in flight together. Kahan-compensated FP32 sums
+// per lane, the cross-lane sum and the scaling in FP64. Reads 8 bytes per
+// nonzero instead of 12 and keeps the FP64 pipe out of the loop.
+constexpr int kSpmvUnroll = 4;
 __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const int *__restrict__ col,
                               const float *__restrict__ val, const double *__restrict__ scalev, double scale,
-                              const double *__restrict__ alphas, const float *__restrict__ in,
+                              const double *__restrict__ alphas, const float4 *__restrict__ in4,
                               double *__restrict__ out, int accumulate) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2455,12 +2458,34 @@ __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const i
   }
   for (int i = warp; i < nrow; i += nwarps) {
     HalfWarpSums<float> acc;
-    for (int k = row_ptr[i] + lane; k < row_ptr[i + 1]; k += 32) {
-      const float v = val[k];
-      const int j = col[k];
-      acc.add(0, v * in[3 * (size_t)j]);
-      acc.add(1, v * in[3 * (size_t)j + 1]);
-      acc.add(2, v * in[3 * (size_t)j + 2]);
+    const int end = row_ptr[i + 1];
+    for (int k0 = row_ptr[i] + lane; k0 < end; k0 += 32 * kSpmvUnroll) {
+      float v[kSpmvUnroll];
+      int j[kSpmvUnroll];
+#pragma unroll
+      for (int u = 0; u < kSpmvUnroll; ++u) {
+        const int k = k0 + 32 * u;
+        v[u] = k < end ? __ldcs(&val[k]) : 0.f;
+        j[u] = k < end ? __ldcs(&col[k]) : 0;
+      }
+      float4 x[kSpmvUnroll];
+#pragma unroll
+      for (int u = 0; u < kSpmvUnroll; ++u) x[u] = __ldg(&in4[j[u]]);
+      // groups of four products summed by plain multiply-adds, each group
+      // added to the compensated total
+#pragma unroll
+      for (int g = 0; g < kSpmvUnroll; g += 4) {
+        float t0 = v[g] * x[g].x, t1 = v[g] * x[g].y, t2 = v[g] * x[g].z;
+#pragma unroll
+        for (int u = g + 1; u < g + 4; ++u) {
+          t0 = fmaf(v[u], x[u].x, t0);
+          t1 = fmaf(v[u], x[u].y, t1);
+          t2 = fmaf(v[u], x[u].z, t2);
+        }
+        acc.add(0, t0);
+        acc.add(1, t1);
+        acc.add(2, t2);
+      }
     }
     double s[3] = {acc.get(0), acc.get(1), acc.get(2)};
 #pragma unroll
@@ -2479,9 +2504,10 @@ __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const i
   }
 }
 
-__global__ void to_f32_kernel(size_t n, const double *__restrict__ in, float *__restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+// Rows of three doubles to float4 {x, y, z, 0}.
+__global__ void to_f32x4_kernel(int n, const double *__restrict__ in, float4 *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = make_float4((float)in[3 * (size_t)i], (float)in[3 * (size_t)i + 1], (float)in[3 * (size_t)i + 2], 0.f);
 }
 
 }  // namespace dev
@@ -2620,7 +2646,7 @@ cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const 
   return cudaGetLastError();
 }
 cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
-                          double scale, const double *alphas, const float *in, double *out, int accumulate,
+                          double scale, const double *alphas, const float4 *in, double *out, int accumulate,
                           cudaStream_t s) {
   if (nrow <= 0) return cudaSuccess;
   int warps_per_block = 8;
@@ -2631,10 +2657,10 @@ cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_to_f32(size_t n, const double *in, float *out, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  size_t g = (n + 255) / 256;
-  dev::to_f32_kernel<<<(int)(g < 152 * 8 ? g : 152 * 8), 256, 0, s>>>(n, in, out);
+cudaError_t launch_to_f32x4(int n, const double *in, float4 *out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = grid_for(n, 256);
+  dev::to_f32x4_kernel<<<g < 152 * 8 ? g : 152 * 8, 256, 0, s>>>(n, in, out);
   return cudaGetLastError();
 }
 
