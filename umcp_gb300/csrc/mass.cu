@@ -14,6 +14,7 @@
 // time so the engine does not depend on the library where no mass matrix is
 // built.
 #include <dlfcn.h>
+#include <stdint.h>
 #include <string.h>
 
 #include <cmath>
@@ -176,6 +177,42 @@ __global__ void dense_apply32_kernel(int n, const float *__restrict__ A, const d
   }
 }
 
+// Kept entries of each row of the truncated inverse (one warp per row).
+__global__ void row_count_kernel(int n, const double *__restrict__ A, int *__restrict__ cnt) {
+  const int lane = threadIdx.x & 31;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+    const double *row = A + (size_t)i * n;
+    int c = 0;
+    for (int j = lane; j < n; j += 32) c += row[j] != 0.0;
+    for (int off = 16; off >= 1; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    if (lane == 0) cnt[i] = c;
+  }
+}
+
+// CSR of the truncated inverse, columns ascending within each row (one warp
+// per row: a ballot over 32 columns at a time gives each kept entry its
+// place). V is double (plain path) or float (precision form, rounded once).
+template <typename V>
+__global__ void row_fill_kernel(int n, const double *__restrict__ A, const int *__restrict__ row_ptr,
+                                int *__restrict__ col, V *__restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+    const double *row = A + (size_t)i * n;
+    int w = row_ptr[i];
+    for (int j0 = 0; j0 < n; j0 += 32) {
+      const int j = j0 + lane;
+      const double a = j < n ? row[j] : 0.0;
+      const unsigned keep = __ballot_sync(0xffffffffu, a != 0.0);
+      if (a != 0.0) {
+        const int at = w + __popc(keep & ((1u << lane) - 1u));
+        col[at] = j;
+        val[at] = (V)a;
+      }
+      w += __popc(keep);
+    }
+  }
+}
+
 __global__ void dense_to_f32_kernel(size_t total, const double *__restrict__ A, float *__restrict__ B) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
     B[e] = (float)A[e];
@@ -295,22 +332,29 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
     UMCP_CUDA(m->mcol.alloc(0));
     UMCP_CUDA(m->mval.alloc(0));
   } else {
-    std::vector<double> h_a((size_t)n * n);
-    UMCP_CUDA(cudaMemcpy(h_a.data(), A.p, A.bytes, cudaMemcpyDeviceToHost));
-    std::vector<int> rp((size_t)n + 1, 0), cl;
-    std::vector<double> vl;
-    for (int i = 0; i < n; ++i) {
-      for (int j = 0; j < n; ++j)
-        if (h_a[(size_t)i * n + j] != 0.0) {
-          cl.push_back(j);
-          vl.push_back(h_a[(size_t)i * n + j]);
-        }
-      rp[(size_t)i + 1] = (int)cl.size();
-    }
+    // CSR on the device: kept entries per row, their prefix sums (on the
+    // host: n + 1 integers), then each row's entries in column order.
+    if (kept > (unsigned long long)INT32_MAX) return fail(UMCP_ERR_UNSUPPORTED, "M^-1 has more than 2^31 nonzeros");
+    DevBuf dcnt;
+    UMCP_CUDA(dcnt.alloc((size_t)n * sizeof(int)));
+    row_count_kernel<<<sms * 8, 256, 0, s>>>(n, A.as<double>(), dcnt.as<int>());
+    UMCP_CUDA(cudaGetLastError());
+    std::vector<int> cnt((size_t)n), rp((size_t)n + 1, 0);
+    UMCP_CUDA(cudaMemcpyAsync(cnt.data(), dcnt.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    UMCP_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) rp[(size_t)i + 1] = rp[i] + cnt[i];
+    if ((unsigned long long)rp[n] != kept) return fail(UMCP_ERR_CUDA, "M^-1 nonzero count mismatch between the truncation and the CSR pass");
     UMCP_CUDA(upload(m->mrow, rp));
-    UMCP_CUDA(upload(m->mcol, cl));
-    if (f32) UMCP_CUDA(upload(m->mval, std::vector<float>(vl.begin(), vl.end())));
-    else UMCP_CUDA(upload(m->mval, vl));
+    UMCP_CUDA(m->mcol.alloc(kept * sizeof(int)));
+    UMCP_CUDA(m->mval.alloc(kept * (f32 ? sizeof(float) : sizeof(double))));
+    if (f32)
+      row_fill_kernel<float><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
+                                                    m->mval.as<float>());
+    else
+      row_fill_kernel<double><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
+                                                     m->mval.as<double>());
+    UMCP_CUDA(cudaGetLastError());
+    UMCP_CUDA(cudaStreamSynchronize(s));
     UMCP_CUDA(m->mdense.alloc(0));
     m->mass_dense = false;
   }
