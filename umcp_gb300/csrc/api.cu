@@ -331,6 +331,67 @@ static void fill_params(umcp_mesh *m, const umcp_params *p) {
   m->P.k_reg = p->k_reg;
 }
 
+namespace {
+// The pinned host staging of the host-pointer calls (state in and out, run
+// counters), allocated at the first such call: meshes run only from the
+// device (batches, servers) never pay for page-locking.
+cudaError_t ensure_pinned(umcp_mesh *m) {
+  if (m->h_pinned) return cudaSuccess;
+  const size_t nst = 3 * (size_t)m->nv + 3;
+  const size_t a = (nst * sizeof(double) + 63) & ~(size_t)63, b = (3 * (size_t)m->nv * sizeof(double) + 63) & ~(size_t)63;
+  cudaError_t e = cudaMallocHost(&m->h_pinned, a + b + 2 * sizeof(uint64_t));
+  if (e != cudaSuccess) return e;
+  unsigned char *h = (unsigned char *)m->h_pinned;
+  m->h_stage = (double *)h;
+  m->h_stage2 = (double *)(h + a);
+  m->h_cnt = (uint64_t *)(h + a + b);
+  return cudaSuccess;
+}
+
+// The device buffers a mesh makes at creation, carved out of one allocation
+// (one cudaMalloc, one host-to-device copy and one memset per mesh instead
+// of some forty calls; a server admits meshes one after another). Sections,
+// in order: contents staged from the host, zero-initialised, uninitialised.
+class MeshArena {
+ public:
+  template <class T>
+  void stage(umcp::DevBuf &b, const std::vector<T> &h) {
+    const size_t at = align(host_.size()), n = h.size() * sizeof(T);
+    host_.resize(at + n);
+    if (n) memcpy(host_.data() + at, h.data(), n);
+    parts_.push_back({&b, 0, at, n});
+  }
+  void zeroed(umcp::DevBuf &b, size_t n) { parts_.push_back({&b, 1, 0, n}); }
+  void uninit(umcp::DevBuf &b, size_t n) { parts_.push_back({&b, 2, 0, n}); }
+  cudaError_t commit(umcp::DevBuf &store) {
+    size_t off[3] = {0, align(host_.size()), 0};
+    size_t zero_end = off[1];
+    for (Part &q : parts_)
+      if (q.section == 1) { q.at = zero_end; zero_end = align(zero_end + q.n); }
+    size_t end = zero_end;
+    for (Part &q : parts_)
+      if (q.section == 2) { q.at = end; end = align(end + q.n); }
+    cudaError_t e = store.alloc(std::max<size_t>(end, 1));
+    if (e != cudaSuccess) return e;
+    unsigned char *base = store.as<unsigned char>();
+    for (Part &q : parts_) q.buf->view(base + q.at, q.n);
+    if (!host_.empty()) e = cudaMemcpy(base, host_.data(), host_.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && zero_end > off[1]) e = cudaMemset(base + off[1], 0, zero_end - off[1]);
+    return e;
+  }
+
+ private:
+  struct Part {
+    umcp::DevBuf *buf;
+    int section;
+    size_t at, n;
+  };
+  static size_t align(size_t x) { return (x + 255) & ~(size_t)255; }
+  std::vector<unsigned char> host_;
+  std::vector<Part> parts_;
+};
+}  // namespace
+
 extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, const umcp_params *prm, umcp_mesh **out) {
   if (!ctx || !plan || !out) return fail(UMCP_ERR_INVALID, "null argument");
   umcp_params defaults;
@@ -369,7 +430,9 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     }
   }
   const int nt = PL.ntypes;
-  std::vector<std::vector<int>> vslots(ME.nv);  // slots touching each vertex, ascending
+  MeshArena arena;
+  std::vector<int> slot_vertex;  // vertex of every (face, control point) slot, in slot order
+  std::vector<int> counts(ME.nv, 0);
   int face_base = 0, slot_base = 0, block_base = 0, block_rows = 0;
   for (const Src &s : srcs) {
     auto G = std::make_unique<Group>();
@@ -387,7 +450,8 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
       const Face &F = s.irr ? PL.irr_faces[f] : PL.reg_faces[f];
       for (int x = 0; x < G->ncp; ++x) {
         cp[(size_t)q * G->ncp + x] = pack_cp(F.cp[x], F.img[x]);
-        vslots[F.cp[x]].push_back(slot_base + q * G->ncp + x);
+        slot_vertex.push_back(F.cp[x]);
+        ++counts[F.cp[x]];
       }
       const std::vector<double> &G0 = s.irr ? PL.irr_g0 : PL.reg_g0, &RR = s.irr ? PL.irr_RuRv0 : PL.reg_RuRv0;
       for (int p = 0; p < G->npt; ++p) {
@@ -409,22 +473,22 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     G->block_base = block_base;
     block_base += G->nblocks;
     block_rows += group_block_rows(prm->precision, G->ncp, G->npt, G->nfaces);
-    UMCP_CUDA(upload(G->cp, cp));
-    UMCP_CUDA(upload(G->g0, g0));
-    UMCP_CUDA(upload(G->rr0, rr0));
-    UMCP_CUDA(upload(G->comp, comp));
-    UMCP_CUDA(upload(G->basis, basis));
+    arena.stage(G->cp, cp);
+    arena.stage(G->g0, g0);
+    arena.stage(G->rr0, rr0);
+    arena.stage(G->comp, comp);
+    arena.stage(G->basis, basis);
     if (prm->precision == UMCP_FP32_CENTRED) {
-      UMCP_CUDA(upload(G->g0f, std::vector<float>(g0.begin(), g0.end())));
-      UMCP_CUDA(upload(G->rr0f, std::vector<float>(rr0.begin(), rr0.end())));
-      UMCP_CUDA(upload(G->compf, std::vector<float>(comp.begin(), comp.end())));
+      arena.stage(G->g0f, std::vector<float>(g0.begin(), g0.end()));
+      arena.stage(G->rr0f, std::vector<float>(rr0.begin(), rr0.end()));
+      arena.stage(G->compf, std::vector<float>(comp.begin(), comp.end()));
     }
-    UMCP_CUDA(upload(G->weight, B.weight));
+    arena.stage(G->weight, B.weight);
     {
       std::vector<double> bw((size_t)G->npt * G->ncp);
       for (int p = 0; p < G->npt; ++p)
         for (int x = 0; x < G->ncp; ++x) bw[(size_t)p * G->ncp + x] = B.at(0, p, x);
-      UMCP_CUDA(upload(G->basis_w, bw));
+      arena.stage(G->basis_w, bw);
     }
     face_base += G->nfaces;
     slot_base += G->nfaces * G->ncp;
@@ -435,47 +499,43 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   // Destination of every (face, control point) slot in the interleaved
   // numbering: the k-th slot of vertex v at loc[2 v] + 32 k, in ascending
   // order of (face, control point), which is the order the gather sums them.
-  std::vector<int> counts(ME.nv), off, dest(slot_base, -1);
-  for (int v = 0; v < ME.nv; ++v) counts[v] = (int)vslots[v].size();
+  std::vector<int> off, dest(slot_base, -1), kth(ME.nv, 0);
   m->nslot_cap = (int)interleave_slots(counts, &off);
-  for (int v = 0; v < ME.nv; ++v)
-    for (size_t k = 0; k < vslots[v].size(); ++k) dest[vslots[v][k]] = off[2 * (size_t)v] + 32 * (int)k;
+  for (int q = 0; q < slot_base; ++q) {
+    const int v = slot_vertex[q];
+    dest[q] = off[2 * (size_t)v] + 32 * kth[v]++;
+  }
   for (auto &G : m->groups) {
     std::vector<int> d(dest.begin() + G->slot_base, dest.begin() + G->slot_base + (size_t)G->nfaces * G->ncp);
-    UMCP_CUDA(upload(G->dest, d));
+    arena.stage(G->dest, d);
   }
-  UMCP_CUDA(upload(m->off, off));
+  arena.stage(m->off, off);
   m->nblocks = block_base;
-  UMCP_CUDA(m->blockpart.alloc((size_t)(block_rows > 0 ? block_rows : 1) * 6 * sizeof(double)));
-  UMCP_CUDA(cudaMemset(m->blockpart.p, 0, m->blockpart.bytes));
+  arena.zeroed(m->blockpart, (size_t)(block_rows > 0 ? block_rows : 1) * 6 * sizeof(double));
   const size_t elem = (m->precision == UMCP_FP64) ? sizeof(double) : sizeof(float);
-  UMCP_CUDA(m->partial.alloc((size_t)m->nslot_cap * 3 * elem));
+  arena.uninit(m->partial, (size_t)m->nslot_cap * 3 * elem);
   const size_t nst = 3 * (size_t)ME.nv + 3;
-  UMCP_CUDA(m->r.alloc(nst * sizeof(double)));
-  UMCP_CUDA(m->g.alloc(nst * sizeof(double)));
-  UMCP_CUDA(m->p.alloc(3 * (size_t)ME.nv * sizeof(double)));
-  UMCP_CUDA(m->qdot.alloc(3 * (size_t)ME.nv * sizeof(double)));
-  UMCP_CUDA(m->E.alloc(sizeof(double)));
-  UMCP_CUDA(m->parts.alloc(3 * sizeof(double)));
-  UMCP_CUDA(m->status.alloc(sizeof(int)));
-  UMCP_CUDA(m->cnt.alloc(2 * sizeof(uint64_t)));
-  UMCP_CUDA(m->r_eval.alloc(nst * sizeof(double)));
-  UMCP_CUDA(m->done.alloc(sizeof(unsigned)));
-  UMCP_CUDA(cudaMemset(m->done.p, 0, sizeof(unsigned)));
-  UMCP_CUDA(m->alphas.alloc(3 * sizeof(double)));
-  UMCP_CUDA(cudaMemset(m->p.p, 0, m->p.bytes));
-  UMCP_CUDA(cudaMemset(m->status.p, 0, sizeof(int)));
-  UMCP_CUDA(cudaMallocHost(&m->h_stage, nst * sizeof(double)));
-  UMCP_CUDA(cudaMallocHost(&m->h_stage2, 3 * (size_t)ME.nv * sizeof(double)));
-  UMCP_CUDA(cudaMallocHost(&m->h_cnt, 2 * sizeof(uint64_t)));
   // Initial state: the plan's positions, alpha = 1.
   std::vector<double> r0(nst);
   std::copy(ME.r.begin(), ME.r.end(), r0.begin());
   r0[3 * ME.nv] = r0[3 * ME.nv + 1] = r0[3 * ME.nv + 2] = 1.0;
-  UMCP_CUDA(cudaMemcpy(m->r.p, r0.data(), nst * sizeof(double), cudaMemcpyHostToDevice));
+  arena.stage(m->r, r0);
+  arena.uninit(m->g, nst * sizeof(double));
+  arena.zeroed(m->p, 3 * (size_t)ME.nv * sizeof(double));
+  arena.uninit(m->qdot, 3 * (size_t)ME.nv * sizeof(double));
+  arena.uninit(m->E, sizeof(double));
+  arena.uninit(m->parts, 3 * sizeof(double));
+  arena.zeroed(m->status, sizeof(int));
+  arena.uninit(m->cnt, 2 * sizeof(uint64_t));
+  arena.uninit(m->r_eval, nst * sizeof(double));
+  arena.zeroed(m->done, sizeof(unsigned));
+  arena.uninit(m->alphas, 3 * sizeof(double));
   if (m->precision == UMCP_FP32_CENTRED) {
-    UMCP_CUDA(m->rhi.alloc(3 * (size_t)ME.nv * sizeof(float)));
-    UMCP_CUDA(m->rlo.alloc(3 * (size_t)ME.nv * sizeof(float)));
+    arena.uninit(m->rhi, 3 * (size_t)ME.nv * sizeof(float));
+    arena.uninit(m->rlo, 3 * (size_t)ME.nv * sizeof(float));
+  }
+  UMCP_CUDA(arena.commit(m->arena));
+  if (m->precision == UMCP_FP32_CENTRED) {
     // On the legacy stream, which does not wait for (or stall) work queued on
     // the context's non-blocking stream, e.g. a batch a server is running.
     UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), 0));
@@ -682,6 +742,7 @@ static umcp_status check_status(umcp_mesh *m) {
 static umcp_status host_energy_grad(umcp_mesh *m, const double *r, double *E, double *terms, double *g) {
   if (!m || !r) return fail(UMCP_ERR_INVALID, "null argument");
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(ensure_pinned(m));
   cudaStream_t s = m->ctx->stream;
   const size_t nst = 3 * (size_t)m->nv + 3;
   memcpy(m->h_stage, r, nst * sizeof(double));
@@ -1085,6 +1146,7 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
   if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
     UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
   m->split_valid = true;  // every step rewrites the pairs of the new positions
+  UMCP_CUDA(ensure_pinned(m));
   m->h_cnt[0] = step0;
   m->h_cnt[1] = 0;
   UMCP_CUDA(cudaMemcpyAsync(m->cnt.p, m->h_cnt, 2 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
@@ -1129,6 +1191,7 @@ extern "C" umcp_status umcp_step_host(umcp_mesh *m, const umcp_integrator *it, u
                                       double *E) {
   if (!m || !it || !r) return fail(UMCP_ERR_INVALID, "null argument");
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  UMCP_CUDA(ensure_pinned(m));
   cudaStream_t s = m->ctx->stream;
   const size_t nst = 3 * (size_t)m->nv + 3;
   memcpy(m->h_stage, r, nst * sizeof(double));

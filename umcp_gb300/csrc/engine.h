@@ -18,14 +18,26 @@ umcp_status set_error(umcp_status s, const std::string &msg);
 
 constexpr int kGraphChunk = 32;  // steps captured per CUDA graph
 
+// A device buffer: owned (cudaMalloc'd here and freed with it) or a view into
+// memory another DevBuf owns (a mesh's creation-time arena). alloc() always
+// leaves it owning a fresh allocation.
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;
-  ~DevBuf() { if (p) cudaFree(p); }
+  bool owned = true;
+  ~DevBuf() { if (p && owned) cudaFree(p); }
   cudaError_t alloc(size_t b) {
-    if (p) { cudaFree(p); p = nullptr; }
+    if (p && owned) cudaFree(p);
+    p = nullptr;
+    owned = true;
     bytes = b;
     return b ? cudaMalloc(&p, b) : cudaSuccess;
+  }
+  void view(void *at, size_t b) {
+    if (p && owned) cudaFree(p);
+    p = b ? at : nullptr;
+    bytes = b;
+    owned = false;
   }
   template <class T> T *as() const { return (T *)p; }
 };
@@ -89,6 +101,8 @@ struct umcp_mesh {
     double KA = 0, A0 = 0, KV = 0, V0 = 0;
   } rs;
   umcp::DevBuf geo_block, gterm, geo_done;
+  umcp::DevBuf arena;         // one allocation holding the buffers made at creation (views into it)
+  void *h_pinned = nullptr;   // one pinned block holding the three below
   double *h_stage = nullptr;  // pinned, 3*nv+3 doubles
   double *h_stage2 = nullptr; // pinned, 3*nv doubles
   uint64_t *h_cnt = nullptr;  // pinned, 2 counters
@@ -129,9 +143,7 @@ struct umcp_mesh {
 
   ~umcp_mesh() {
     drop_graphs();
-    if (h_stage) cudaFreeHost(h_stage);
-    if (h_stage2) cudaFreeHost(h_stage2);
-    if (h_cnt) cudaFreeHost(h_cnt);
+    if (h_pinned) cudaFreeHost(h_pinned);
   }
 };
 

@@ -74,14 +74,31 @@ std::string read_mesh(const std::string &path, Mesh *m) {
     int skip_doubles = 0;
     if (*s == 'P') { body = s + 1; skip_doubles = 15; }
     else if (*s == 'Q') { body = s + 1; }
-    std::istringstream is(body);
-    if (!(is >> id >> x >> y >> z)) continue;
-    for (int q = 0; q < skip_doubles; ++q) { double t; is >> t; }
-    if (!(is >> val)) continue;
+    // whitespace-separated fields: id x y z [15 doubles after 'P'] valence ring...
+    const char *q = body;
+    char *end = nullptr;
+    auto int_field = [&](int *out) {
+      const long v = strtol(q, &end, 10);
+      if (end == q) return false;
+      q = end;
+      *out = (int)v;
+      return true;
+    };
+    auto dbl_field = [&](double *out) {
+      const double v = strtod(q, &end);
+      if (end == q) return false;
+      q = end;
+      *out = v;
+      return true;
+    };
+    if (!int_field(&id) || !dbl_field(&x) || !dbl_field(&y) || !dbl_field(&z)) continue;
+    bool ok = true;
+    for (int k = 0; k < skip_doubles && ok; ++k) { double t; ok = dbl_field(&t); }
+    if (!ok || !int_field(&val)) continue;
     if (val < 5 || val > 7) return "vertex valence must be between 5 and 7";
     std::vector<int> ring;
     int n;
-    while ((int)ring.size() < val && (is >> n)) ring.push_back(n);
+    while ((int)ring.size() < val && int_field(&n)) ring.push_back(n);
     if ((int)ring.size() != val) return "vertex line has fewer neighbours than its valence";
     m->r.push_back(x); m->r.push_back(y); m->r.push_back(z);
     m->valence.push_back(val);
@@ -164,58 +181,82 @@ std::string orient(Mesh *m) {
       }
   }
   if (tris.empty()) return "mesh has no triangles";
-  // Edges with the faces on each side, in creation order.
-  std::map<std::pair<int, int>, int> emap;
+  // Edges with the faces on each side, in creation order. The edge (a, b),
+  // a < b, is found through slot e of a's ring (eslot[nbr_off[a] + e]).
+  std::vector<int> eslot(m->nbr.size(), -1);
   std::vector<Edge> edges;
   for (size_t t = 0; t < tris.size(); ++t) {
     const int *s = tris[t].id;
     int pairs[3][2] = {{s[0], s[1]}, {s[0], s[2]}, {s[1], s[2]}};
     int codes[3] = {2, 1, 0};
     for (int p = 0; p < 3; ++p) {
-      auto key = std::make_pair(pairs[p][0], pairs[p][1]);
-      auto it = emap.find(key);
-      if (it == emap.end()) {
-        Edge e{pairs[p][0], pairs[p][1], {(int)t, -1, -1}, {codes[p], -1, -1}};
-        emap[key] = (int)edges.size();
-        edges.push_back(e);
+      const int a = pairs[p][0], b = pairs[p][1];
+      int &slot = eslot[m->nbr_off[a] + m->find_nbr(a, b)];
+      if (slot < 0) {
+        slot = (int)edges.size();
+        edges.push_back(Edge{a, b, {(int)t, -1, -1}, {codes[p], -1, -1}});
       } else {
-        Edge &e = edges[it->second];
-        int slot = (e.face[1] == -1) ? 1 : 2;
-        e.face[slot] = (int)t;
-        e.code[slot] = codes[p];
+        Edge &e = edges[slot];
+        int k = (e.face[1] == -1) ? 1 : 2;
+        e.face[k] = (int)t;
+        e.code[k] = codes[p];
       }
     }
   }
-  // Propagate senses from triangle 0 (src/interpLib.C:1790-1825).
-  tris[0].sense = m->fix_sense;
-  bool changed = true;
-  while (changed) {
-    changed = false;
-    for (const Edge &e : edges) {
-      int f1 = e.face[0], f2 = e.face[1];
-      if (f1 < 0 || f2 < 0) continue;
-      int s1 = tris[f1].sense, s2 = tris[f2].sense;
-      int rel = compare_sense(e.code[0], e.code[1]);
-      if (s1 && s2) {
-        if (s2 != s1 * rel) return "surface is not orientable";
-      } else if (s1 && !s2) {
-        tris[f2].sense = s1 * rel; changed = true;
-      } else if (!s1 && s2) {
-        tris[f1].sense = s2 * rel; changed = true;
+  // Senses from triangle 0 (src/interpLib.C:1790-1825), across the edges'
+  // first two faces. On a connected orientable surface the senses are fixed
+  // by triangle 0's, so one breadth-first pass gives what repeated sweeps
+  // over the edge list give; every such edge is checked for consistency.
+  {
+    std::vector<std::vector<int>> tedges(tris.size());
+    for (size_t e = 0; e < edges.size(); ++e)
+      if (edges[e].face[0] >= 0 && edges[e].face[1] >= 0) {
+        tedges[edges[e].face[0]].push_back((int)e);
+        tedges[edges[e].face[1]].push_back((int)e);
+      }
+    tris[0].sense = m->fix_sense;
+    std::vector<int> queue(1, 0);
+    for (size_t h = 0; h < queue.size(); ++h) {
+      const int t = queue[h];
+      for (int e : tedges[t]) {
+        const Edge &E = edges[e];
+        const int u = E.face[0] == t ? E.face[1] : E.face[0];
+        const int want = tris[t].sense * compare_sense(E.code[0], E.code[1]);
+        if (!tris[u].sense) {
+          tris[u].sense = want;
+          queue.push_back(u);
+        } else if (tris[u].sense != want) {
+          return "surface is not orientable";
+        }
       }
     }
   }
   // Oriented successor map: for an oriented triangle (a,b,c), around vertex a
   // the ring steps from c to b (the reference's sorted rings list edges[e],
   // edges[e+1] such that (i, edges[e+1], edges[e]) is positively oriented).
-  std::vector<std::map<int, int>> succ(nv);
+  // Vertex a's pairs (c -> b) live in slots nbr_off[a] .. (at most its valence).
+  std::vector<int> skey(m->nbr.size()), sval(m->nbr.size()), scount(nv, 0);
+  auto put = [&](int a, int key, int val) -> bool {
+    const int o = m->nbr_off[a];
+    for (int q = 0; q < scount[a]; ++q)
+      if (skey[o + q] == key) { sval[o + q] = val; return true; }
+    if (scount[a] >= m->valence[a]) return false;
+    skey[o + scount[a]] = key;
+    sval[o + scount[a]] = val;
+    ++scount[a];
+    return true;
+  };
+  auto get = [&](int a, int key) -> int {
+    const int o = m->nbr_off[a];
+    for (int q = 0; q < scount[a]; ++q)
+      if (skey[o + q] == key) return sval[o + q];
+    return -1;
+  };
   for (const Tri &t : tris) {
     if (!t.sense) return "mesh has triangles not reachable from triangle 0";
     int a = t.id[0], b = t.id[1], c = t.id[2];
     if (t.sense < 0) std::swap(b, c);  // oriented cycle a->b->c
-    succ[a][c] = b;
-    succ[b][a] = c;
-    succ[c][b] = a;
+    if (!put(a, c, b) || !put(b, a, c) || !put(c, b, a)) return "a vertex lies on more triangles than its valence";
   }
   for (int i = 0; i < nv; ++i) {
     int val = m->valence[i];
@@ -223,14 +264,13 @@ std::string orient(Mesh *m) {
     int cur = m->nbr_of(i, 0);
     ring.push_back(cur);
     for (int s = 1; s < val; ++s) {
-      auto it = succ[i].find(cur);
-      if (it == succ[i].end()) return "vertex " + std::to_string(i) + " has an open or broken ring";
-      cur = it->second;
+      const int nx = get(i, cur);
+      if (nx < 0) return "vertex " + std::to_string(i) + " has an open or broken ring";
+      cur = nx;
       ring.push_back(cur);
     }
-    auto it = succ[i].find(cur);
-    if (it == succ[i].end() || it->second != ring[0])
-      return "vertex " + std::to_string(i) + " ring does not close";
+    const int nx = get(i, cur);
+    if (nx < 0 || nx != ring[0]) return "vertex " + std::to_string(i) + " ring does not close";
     for (int e = 0; e < val; ++e) m->nbr[m->nbr_off[i] + e] = ring[e];
   }
   return "";
@@ -238,8 +278,28 @@ std::string orient(Mesh *m) {
 
 // ---------------------------------------------------------------- faces
 
-void min_image_shift(const double dr[3], const double box[3][3], int shift[3]) {
+// Squared length under which no lattice shift can shorten a vector: a
+// shift t shortens dr only if |dr| > |t| / 2, so a quarter of the shortest
+// nonzero combination of the box vectors (less a relative margin).
+double min_image_free_r2(const double box[3][3]) {
+  double best = 0.0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        if (!dx && !dy && !dz) continue;
+        double t2 = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          const double t = dx * box[0][c] + dy * box[1][c] + dz * box[2][c];
+          t2 += t * t;
+        }
+        if (best == 0.0 || t2 < best) best = t2;
+      }
+  return 0.25 * best * (1.0 - 1e-9);
+}
+
+void min_image_shift(const double dr[3], const double box[3][3], int shift[3], double free_r2) {
   shift[0] = shift[1] = shift[2] = 0;
+  if (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2] < free_r2) return;
   double tr[3] = {dr[0], dr[1], dr[2]};
   bool done = false;
   while (!done) {
@@ -265,6 +325,7 @@ void min_image_shift(const double dr[3], const double box[3][3], int shift[3]) {
 std::string enumerate_faces(const Mesh &m, std::vector<Face> *regular, std::vector<Face> *irregular) {
   regular->clear();
   irregular->clear();
+  const double free_r2 = min_image_free_r2(m.box);
   for (int i = 0; i < m.nv; ++i) {
     int val = m.valence[i];
     for (int e = 0; e < val; ++e) {
@@ -295,7 +356,7 @@ std::string enumerate_faces(const Mesh &m, std::vector<Face> *regular, std::vect
         const double *r1 = &m.r[3 * f.cp[p]];
         double dr[3] = {r1[0] - r0[0], r1[1] - r0[1], r1[2] - r0[2]};
         int s[3];
-        min_image_shift(dr, m.box, s);
+        min_image_shift(dr, m.box, s, free_r2);
         for (int c = 0; c < 3; ++c) {
           if (s[c] < -1 || s[c] > 1) return "control point more than one box away from its face";
           f.img[p][c] = (int8_t)s[c];

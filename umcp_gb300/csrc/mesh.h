@@ -47,7 +47,11 @@ std::string orient(Mesh *m);
 std::string enumerate_faces(const Mesh &m, std::vector<Face> *regular, std::vector<Face> *irregular);
 
 // Minimum-image lattice shift of dr (greedy search of src/mutil.C:541-599).
-void min_image_shift(const double dr[3], const double box[3][3], int shift[3]);
+// Squared length below which min_image_shift finds no shift for this box.
+double min_image_free_r2(const double box[3][3]);
+// Lattice shift (each -1..1, repeated while it shortens) taking dr to its
+// minimum image; vectors shorter than sqrt(free_r2) return no shift at once.
+void min_image_shift(const double dr[3], const double box[3][3], int shift[3], double free_r2 = 0.0);
 
 // Synthetic meshes. Vesicle: icosahedron Loop-subdivided `level` times (original
 // 12 vertices first), projected to radius R, radial Gaussian noise sigma (Philox
