@@ -474,14 +474,15 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     block_base += G->nblocks;
     block_rows += group_block_rows(prm->precision, G->ncp, G->npt, G->nfaces);
     arena.stage(G->cp, cp);
-    arena.stage(G->g0, g0);
-    arena.stage(G->rr0, rr0);
-    arena.stage(G->comp, comp);
     arena.stage(G->basis, basis);
-    if (prm->precision == UMCP_FP32_CENTRED) {
+    if (prm->precision == UMCP_FP32_CENTRED) {  // the precision form's kernels read only the FP32 copies
       arena.stage(G->g0f, std::vector<float>(g0.begin(), g0.end()));
       arena.stage(G->rr0f, std::vector<float>(rr0.begin(), rr0.end()));
       arena.stage(G->compf, std::vector<float>(comp.begin(), comp.end()));
+    } else {
+      arena.stage(G->g0, g0);
+      arena.stage(G->rr0, rr0);
+      arena.stage(G->comp, comp);
     }
     arena.stage(G->weight, B.weight);
     {
@@ -826,9 +827,10 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
   const size_t slots = interleave_slots(counts, &loc);
   auto group = [&](const PatchBasis &B, size_t nf) {
     const size_t ncpp = (size_t)(B.ncp + 3) / 4 * 4;
-    b += nf * B.ncp * 4 + 2 * nf * B.npt * 8 + nf * 3 * 8 + (size_t)B.npt * 5 * ncpp * 8 + B.weight.size() * 8 +
-         nf * B.ncp * 4 + (size_t)B.npt * B.ncp * 8;
-    if (f32) b += 2 * nf * B.npt * 4 + nf * 3 * 4;
+    b += nf * B.ncp * 4 + (size_t)B.npt * 5 * ncpp * 8 + B.weight.size() * 8 + nf * B.ncp * 4 +
+         (size_t)B.npt * B.ncp * 8;
+    const size_t es = f32 ? 4 : 8;  // g0, reference angles and composition in the form's own type
+    b += 2 * nf * B.npt * es + nf * 3 * es;
     nblocks += group_block_rows(precision, B.ncp, B.npt, (int)nf);
   };
   group(PL.regular, PL.reg_faces.size());

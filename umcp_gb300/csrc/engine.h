@@ -2,6 +2,7 @@
 // of the ABI): device buffers, the context and device mesh objects, and the
 // error helper every entry point reports through.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -61,7 +62,7 @@ struct umcp_batch;
 struct umcp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  int refs = 1;  // the creator's reference plus one per live mesh or batch
+  std::atomic<int> refs{1};  // the creator's reference plus one per live mesh or batch (meshes may be made on several threads)
 };
 
 namespace umcp {

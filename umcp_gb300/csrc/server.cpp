@@ -141,39 +141,67 @@ void umcp_server::builder_main() {
 }
 
 // Creates the meshes of the ready jobs that fit and adds them to the batch.
+// Jobs are taken first come, first served while their footprint fits (up to
+// kAdmitWave at a time); their meshes are created on parallel threads (host
+// tables and uploads; the error text is per thread) and joined to the batch
+// in the order taken.
 void umcp_server::admit_pass() {
+  constexpr size_t kAdmitWave = 16;
   for (;;) {
-    SJob *j;
+    std::vector<SJob *> take;
     {
       std::lock_guard<std::mutex> lk(mu);
-      if (stop || ready_q.empty()) return;
-      j = ready_q.front();
-      if (hbm_used + (double)j->bytes > budget) return;
-      if (o.max_jobs > 0 && (int)running.size() >= o.max_jobs) return;
-      ready_q.pop_front();
-      hbm_used += (double)j->bytes;
-      hbm_peak = std::max(hbm_peak, hbm_used);
+      while (!stop && !ready_q.empty() && take.size() < kAdmitWave) {
+        SJob *j = ready_q.front();
+        if (hbm_used + (double)j->bytes > budget) break;
+        if (o.max_jobs > 0 && (int)(running.size() + take.size()) >= o.max_jobs) break;
+        ready_q.pop_front();
+        hbm_used += (double)j->bytes;
+        hbm_peak = std::max(hbm_peak, hbm_used);
+        take.push_back(j);
+      }
     }
-    umcp_mesh *m = nullptr;
-    umcp_status st = umcp_mesh_create(ctx, j->plan, &j->prm, &m);
-    umcp_mesh_info mi{};
-    if (st == UMCP_OK) st = umcp_mesh_info_get(m, &mi);
-    if (st == UMCP_OK) st = umcp_batch_add(batch, m, &j->it, j->step0, j->n_steps);
-    j->h2d = (double)mi.h2d_bytes;
-    const std::string err = st == UMCP_OK ? std::string() : std::string(umcp_last_error());
-    umcp_plan_destroy(j->plan);
-    j->plan = nullptr;
-    std::lock_guard<std::mutex> lk(mu);
-    if (st != UMCP_OK) {
-      if (m) umcp_mesh_destroy(m);
-      hbm_used -= (double)j->bytes;
-      finish_locked(j, st, err);
-      continue;
+    if (take.empty()) return;
+    struct Made {
+      umcp_mesh *m = nullptr;
+      umcp_status st = UMCP_OK;
+      std::string err;
+    };
+    std::vector<Made> made(take.size());
+    auto create = [&](size_t i) {
+      made[i].st = umcp_mesh_create(ctx, take[i]->plan, &take[i]->prm, &made[i].m);
+      if (made[i].st != UMCP_OK) made[i].err = umcp_last_error();
+    };
+    {
+      std::vector<std::thread> th;
+      for (size_t i = 1; i < take.size(); ++i) th.emplace_back(create, i);
+      create(0);
+      for (auto &t : th) t.join();
     }
-    j->mesh = m;
-    j->state = UMCP_JOB_RUNNING;
-    j->t_admit = now();
-    running.push_back(j);
+    for (size_t i = 0; i < take.size(); ++i) {
+      SJob *j = take[i];
+      umcp_mesh *m = made[i].m;
+      umcp_status st = made[i].st;
+      std::string err = made[i].err;
+      umcp_mesh_info mi{};
+      if (st == UMCP_OK) st = umcp_mesh_info_get(m, &mi);
+      if (st == UMCP_OK) st = umcp_batch_add(batch, m, &j->it, j->step0, j->n_steps);
+      if (st != UMCP_OK && err.empty()) err = umcp_last_error();
+      j->h2d = (double)mi.h2d_bytes;
+      umcp_plan_destroy(j->plan);
+      j->plan = nullptr;
+      std::lock_guard<std::mutex> lk(mu);
+      if (st != UMCP_OK) {
+        if (m) umcp_mesh_destroy(m);
+        hbm_used -= (double)j->bytes;
+        finish_locked(j, st, err);
+        continue;
+      }
+      j->mesh = m;
+      j->state = UMCP_JOB_RUNNING;
+      j->t_admit = now();
+      running.push_back(j);
+    }
   }
 }
 

@@ -2521,23 +2521,21 @@ template <typename T, int NCP, int NPT>
 static int face_grid_size(int nfaces) {
   // Persistent grid: as many blocks as fit on the device at once (a fixed
   // number, so the face-to-block assignment and the sums' order are fixed).
-  static int cached = 0;
-  if (!cached) {
+  static const int cached = [] {  // thread-safe one-time initialisation
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_kernel<T, NCP, NPT>,
                                                   dev::FaceCfg<T>::threads, 0);
-    cached = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  }
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }();
   int need = grid_for(nfaces, dev::FaceCfg<T>::half_warps);
   return need < cached ? need : cached;
 }
 
 // The thread-per-face kernel's persistent grid (precision form, regular faces).
 static int face_grid_size_tpf(int nfaces) {
-  static int cached = 0;
-  if (!cached) {
+  static const int cached = [] {  // thread-safe one-time initialisation (meshes may be made on several threads)
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -2545,8 +2543,8 @@ static int face_grid_size_tpf(int nfaces) {
                          (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads,
                                                   dev::tpf::kStageBytes + dev::tpf::kSumBytes);
-    cached = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  }
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }();
   int need = grid_for(nfaces, dev::tpf::kThreads);
   return need < cached ? need : cached;
 }
@@ -2774,13 +2772,12 @@ template cudaError_t launch_geo_grad<float>(const GeoArgs &, float *, cudaStream
 namespace umcp {
 
 int face_blocks_tc(int nfaces) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
+  static const int sms = [] {
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 152;
+  }();
   const int tiles = (nfaces + dev::tc::kFaces - 1) / dev::tc::kFaces;
   const int cap = 2 * sms;  // two CTAs per SM (shared memory and tensor memory)
   return tiles < 1 ? 1 : (tiles < cap ? tiles : cap);
