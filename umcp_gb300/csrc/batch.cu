@@ -63,6 +63,12 @@ struct umcp_batch {
   size_t prog_jobs = 0;  // jobs whose progress the latest run is copying to h_prog
   // captured steps (kGraphChunk steps and 1 step) for the current capacities
   cudaGraphExec_t g_chunk = nullptr, g_one = nullptr;
+  // The irregular face launches run on a second stream, forked from the
+  // context's stream after the regular launch is queued and joined before the
+  // per-job sums, so they fill the SMs the regular launch's tail leaves idle
+  // (in a captured step, two branches of the graph).
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   void drop_graphs() {
     if (g_chunk) cudaGraphExecDestroy(g_chunk);
     if (g_one) cudaGraphExecDestroy(g_one);
@@ -71,6 +77,9 @@ struct umcp_batch {
   ~umcp_batch() {
     drop_graphs();
     if (h_prog) cudaFreeHost(h_prog);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
   }
 };
 
@@ -252,15 +261,25 @@ static umcp_status start_jobs(umcp_batch *b) {
 template <typename T>
 static cudaError_t queue_faces_t(umcp_batch *b) {
   cudaStream_t s = b->ctx->stream;
-  for (int t = 0; t < kTypes; ++t) {
-    if (!b->have_type[t]) continue;
-    cudaError_t e = launch_batch_faces<T>(b->d_jobs.as<BatchJob>(), t, b->d_tiles.as<BatchTile>(),
-                                          b->d_counts.as<int>(), b->basis[t].as<double>(), b->weight[t].as<double>(),
-                                          kTypeNcp[t], b->npt[t], b->dudv[t], t > 0, b->d_tile_sums.as<double>(),
-                                          b->face_grid[t], s);
-    if (e != cudaSuccess) return e;
+  auto launch = [&](int t, cudaStream_t on) {
+    return launch_batch_faces<T>(b->d_jobs.as<BatchJob>(), t, b->d_tiles.as<BatchTile>(), b->d_counts.as<int>(),
+                                 b->basis[t].as<double>(), b->weight[t].as<double>(), kTypeNcp[t], b->npt[t],
+                                 b->dudv[t], t > 0, b->d_tile_sums.as<double>(), b->face_grid[t], on);
+  };
+  cudaError_t e = cudaSuccess;
+  const bool irregular = b->have_type[1] || b->have_type[2];
+  if (irregular) {
+    // the side stream starts after everything queued on s so far, then runs
+    // beside the regular launch (they write disjoint slots and tile rows)
+    if ((e = cudaEventRecord(b->fork, s)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return e;
   }
-  return cudaSuccess;
+  if (b->have_type[0] && (e = launch(0, s)) != cudaSuccess) return e;
+  if (!irregular) return cudaSuccess;
+  for (int t = 1; t < kTypes; ++t)
+    if (b->have_type[t] && (e = launch(t, b->side)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return e;
+  return cudaStreamWaitEvent(s, b->join, 0);
 }
 
 static cudaError_t queue_faces(umcp_batch *b) {
@@ -345,6 +364,10 @@ extern "C" umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umc
   if (precision != UMCP_FP64 && precision != UMCP_FP32_CENTRED) return fail(UMCP_ERR_INVALID, "unknown precision");
   UMCP_CUDA(cudaSetDevice(ctx->device));
   auto b = std::make_unique<umcp_batch>();
+  UMCP_CUDA(cudaSetDevice(ctx->device));
+  UMCP_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  UMCP_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  UMCP_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
   b->ctx = ctx;
   b->precision = precision;
   if (opts) {
