@@ -290,6 +290,9 @@ extern "C" umcp_status umcp_ctx_create(int device, umcp_ctx **out) {
   auto c = std::make_unique<umcp_ctx>();
   c->device = device;
   UMCP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  UMCP_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  UMCP_CUDA(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+  UMCP_CUDA(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
   *out = c.release();
   return UMCP_OK;
 }
@@ -643,7 +646,10 @@ static GeoArgs geo_args(umcp_mesh *m, const double *d_r) {
 
 // Face launches of an evaluation at d_r. With restraints on, the area and
 // volume sums run first (the face pass's finish adds their energy) and their
-// gradient is added into the partial slots after it.
+// gradient is added into the partial slots after it. The irregular groups run
+// on the ctx's side stream beside the regular group; every block of every
+// launch counts toward the finish (FinishArgs::nblk), so whichever block is
+// the last of all sums the block partials.
 template <typename T>
 static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs *fin_in) {
   cudaStream_t s = m->ctx->stream;
@@ -660,9 +666,15 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
     fin_geo.gterm = m->gterm.as<double>();
     fin = &fin_geo;
   }
+  const bool fork = m->groups.size() > 1;
+  if (fork) {
+    cudaError_t e = cudaEventRecord(m->ctx->fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(m->ctx->side, m->ctx->fork, 0);
+    if (e != cudaSuccess) return e;
+  }
   for (size_t gi = 0; gi < m->groups.size(); ++gi) {
     auto &G = m->groups[gi];
-    const bool last = (gi + 1 == m->groups.size());
+    const cudaStream_t on = (fork && gi > 0) ? m->ctx->side : s;
     dev::FaceLaunch L;
     L.nfaces = G->nfaces;
     L.block_base = G->block_base;
@@ -682,16 +694,21 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
       if (G->tc)
         e = launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
                             m->partial.as<float>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
-                            (last && fin) ? *fin : none, s);
+                            fin ? *fin : none, on);
       else
         e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
                             m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
-                            (last && fin) ? *fin : none, s);
+                            fin ? *fin : none, on);
     } else {
       e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
                           m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
-                          (last && fin) ? *fin : none, s);
+                          fin ? *fin : none, on);
     }
+    if (e != cudaSuccess) return e;
+  }
+  if (fork) {
+    cudaError_t e = cudaEventRecord(m->ctx->join, m->ctx->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, m->ctx->join, 0);
     if (e != cudaSuccess) return e;
   }
   if (geo) return launch_geo_grad<T>(GA, m->partial.as<T>(), s);
@@ -1270,7 +1287,6 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
   UMCP_CUDA(cudaMemsetAsync(base + off_flags, 0, 256, s));
   if (fp32) UMCP_CUDA(launch_split_positions(3 * m->nv, d_r, rhi, rlo, s));
   FinishArgs fin{m->nblocks, d_E, nullptr, d_g ? d_g + 3 * m->nv : nullptr, nullptr, nullptr, 0.0, status, done};
-  FinishArgs none{};
   for (size_t gi = 0; gi < m->groups.size(); ++gi) {
     auto &G = m->groups[gi];
     dev::FaceLaunch L;
@@ -1287,7 +1303,7 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
     L.weight = G->weight.as<double>();
     L.dudv = G->dudv;
     L.irregular = G->irregular;
-    const FinishArgs &f = (gi + 1 == m->groups.size()) ? fin : none;
+    const FinishArgs &f = fin;  // every block of every launch counts toward the finish
     cudaError_t e = (fp32 && G->tc) ? launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, rhi, rlo,
                                                        (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
                     : fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,

@@ -62,6 +62,11 @@ struct umcp_batch;
 struct umcp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // A mesh's irregular face launches run on `side`, forked from `stream`
+  // before the regular launch and joined after it (calls on a ctx are
+  // serialised, so one pair serves every mesh of the ctx).
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   std::atomic<int> refs{1};  // the creator's reference plus one per live mesh or batch (meshes may be made on several threads)
 };
 
@@ -73,6 +78,9 @@ inline umcp_ctx *ctx_retain(umcp_ctx *c) {
 inline void ctx_release(umcp_ctx *c) {
   if (--c->refs > 0) return;
   cudaSetDevice(c->device);
+  if (c->fork) cudaEventDestroy(c->fork);
+  if (c->join) cudaEventDestroy(c->join);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

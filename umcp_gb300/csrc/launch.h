@@ -15,7 +15,8 @@ enum : int { kStatusNonFinite = 1, kStatusDiverged = 2, kStatusTimeout = 4 };
 // launch_finish). done: device counter of finished blocks, zero between
 // launches; when non-null, the last block of that face launch does the sum.
 struct FinishArgs {
-  int nblk;            // block-partial rows to sum (all face launches of the mesh)
+  int nblk;            // block-partial rows to sum: every block of every face launch of the pass, each of
+                       // which counts on `done`; the block that brings it to nblk sums the rows
   double *E, *parts, *galpha;
   double *energies;    // run only: energies[cnt[1]] = E, cnt[1] += 1
   uint64_t *cnt;

@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == (unsigned)fin.nblk - 1u);
     __syncthreads();
     if (last) {
       __threadfence();
@@ -1027,7 +1027,7 @@ __global__ void __launch_bounds__(tc::kThreads, 2)
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == (unsigned)fin.nblk - 1u);
     __syncthreads();
     if (last) {
       __threadfence();
@@ -1701,7 +1701,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) last = (atomicAdd(fin.done, 1u) == (unsigned)fin.nblk - 1u);
     __syncthreads();
     if (last) {
       __threadfence();
