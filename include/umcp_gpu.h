@@ -268,6 +268,30 @@ umcp_status umcp_run(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step0,
 /* Same as umcp_run without waiting: queues the steps on the ctx stream and
  * returns; umcp_ctx_synchronize or a later blocking call observes errors. */
 umcp_status umcp_run_async(umcp_mesh *mesh, const umcp_integrator *it, uint64_t step0, int n_steps);
+
+/* ---- energy minimization ---------------------------------------------------
+ * Replaces Simulation::minimize (src/minimize.C:489-560) for a membrane
+ * without particles, with the reference's L-BFGS (l_bfgs_iteration and
+ * do_linesearch, src/l-bfgs.C:97-404): the vertex positions move, the box
+ * scales alpha stay fixed (the reference zeroes their gradient,
+ * src/minimize.C:321-333). The energy is the mesh's (umcp_energy, with any
+ * restraints set). Starts from and replaces the resident state's positions;
+ * momenta are kept. */
+typedef struct {
+  int max_iterations; /* the reference's nsteps: 100 */
+  int history;        /* stored curvature pairs; 0: min(max_iterations, 3 nv + 6) as the reference */
+  double max_move;    /* the line search's first step moves no coordinate further than this: 1.0 */
+} umcp_minimize_opts;
+typedef struct {
+  int iterations;         /* done (fewer when the newest curvature pair vanishes, as the reference stops) */
+  int evaluations;        /* energy (+gradient) evaluations */
+  double energy_initial, energy_final;
+  double grad_rms;        /* rms of the final gradient over the 3 nv position coordinates */
+} umcp_minimize_info;
+/* opts NULL: the reference's settings. energies (may be NULL): the energy
+ * before the first iteration and after each, max_iterations + 1 values. */
+umcp_status umcp_minimize(umcp_mesh *mesh, const umcp_minimize_opts *opts, double *energies,
+                          umcp_minimize_info *info);
 /* One step of the integrator on HOST state: copies r (3*nv+3) and p (3*nv,
  * may be NULL for zero momenta) in, steps once at step index `step`, copies
  * the new r (and p) back and returns the energy of the pre-step state in *E.

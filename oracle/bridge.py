@@ -187,6 +187,16 @@ def reference_dump(mesh: Path, params_txt: Path, positions: Path | None, prefix:
     return out
 
 
+def reference_min(mesh: Path, params_txt: Path, positions: Path, prefix: Path, timeout: float = 600) -> dict:
+    """Runs the reference's own L-BFGS minimization (ref_driver min: src/l-bfgs.C
+    driven as src/minimize.C drives it for one surface) and returns the energy
+    before and after every iteration and the final state."""
+    cmd = [str(REF_DRIVER), "min", str(mesh), str(params_txt), str(positions), str(prefix)]
+    subprocess.run(cmd, check=True, capture_output=True, timeout=timeout)
+    return {"energies": np.fromfile(f"{prefix}.min_energy.bin", dtype=np.float64),
+            "r": np.fromfile(f"{prefix}.min_positions.bin", dtype=np.float64)}
+
+
 MASS_POINT = np.dtype([("face", "i4"), ("n", "i4"), ("u", "f8"), ("v", "f8"), ("ids", "i4", 13), ("coef", "f8", 13)])
 
 

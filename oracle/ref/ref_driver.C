@@ -18,6 +18,12 @@
  *   ref_driver sub6 - - - <out_prefix>
  *   ref_driver rnrm <mesh> <params> <positions.bin|-> <out_prefix>
  *     surface::evaluateRNRM at 7 fixed (u,v) on every face: face, u, v, R, N
+ *   ref_driver min <mesh> <params> <positions.bin|-> <out_prefix>
+ *     the reference's L-BFGS (src/l-bfgs.C) driven as Simulation::minimize
+ *     drives it for one surface without particles (src/minimize.C:26-140,
+ *     489-560): parameters {alpha, r, alpha}, alpha's gradient zeroed,
+ *     100 iterations, 100 back vectors, max move 1.0; writes the energy
+ *     before and after every iteration and the final positions
  *
  * "mass" sets up the mass points as hd.C does before a dynamics run
  * (src/hd.C:417-481: a 66-point grid per triangle, mass per point from
@@ -41,6 +47,7 @@
 #include "lagrange.h"
 #include "sparse.h"
 #include "units.h"
+#include "l-bfgs.h"
 
 extern double kc, KA, kg, k_reg;
 extern double VA, VC, VR, AVC;
@@ -142,6 +149,33 @@ void fast_sub6_1(double *r_in, double *r_out);
 void fast_sub6_2(double *r_in, double *r_out);
 void fast_sub6_3(double *r_in, double *r_out);
 
+/* Simulation::minimize's objective for one surface without particles
+ * (src/minimize.C:26-140): p = {alpha_x,y,z, r[3 nv], alpha copy}. */
+static surface *min_surface = NULL;
+static int min_nv = 0;
+
+static double min_f(double *p)
+{
+	int nv = min_nv;
+	p[3 + 3 * nv + 0] = p[0];
+	p[3 + 3 * nv + 1] = p[1];
+	p[3 + 3 * nv + 2] = p[2];
+	return min_surface->energy(p + 3, NULL);
+}
+
+static double min_fdf(double *p, double *g)
+{
+	int nv = min_nv, n = 3 * nv + 6;
+	memset(g, 0, sizeof(double) * n);
+	p[3 + 3 * nv + 0] = p[0];
+	p[3 + 3 * nv + 1] = p[1];
+	p[3 + 3 * nv + 2] = p[2];
+	min_surface->grad(p + 3, g + 3);
+	g[0] = g[1] = g[2] = 0;
+	g[3 + 3 * nv + 0] = g[3 + 3 * nv + 1] = g[3 + 3 * nv + 2] = 0;
+	return min_surface->energy(p + 3, NULL);
+}
+
 int main(int argc, char **argv)
 {
 	if (argc >= 6 && !strcmp(argv[1], "sub6")) {
@@ -242,6 +276,40 @@ int main(int argc, char **argv)
 		}
 		fclose(f);
 		printf("mass_per_pt %.17e nuse %d\n", mass_per_pt, nuse);
+		return 0;
+	}
+
+	if (!strcmp(argv[1], "min")) {
+		const int nsteps = 100, n = 3 * nv + 6;
+		min_surface = s;
+		min_nv = nv;
+		double *p = (double *)calloc(n, sizeof(double));
+		double *gp = (double *)calloc(n, sizeof(double));
+		p[0] = r[3 * nv]; p[1] = r[3 * nv + 1]; p[2] = r[3 * nv + 2];
+		memcpy(p + 3, r, sizeof(double) * 3 * nv);
+		min_fdf(p, gp);
+		double mag = 0;
+		for (int i = 0; i < n; i++) mag += gp[i] * gp[i];
+		int use_m = nsteps < n ? nsteps : n;
+		FILE *f = open_out(argv[5], "min_energy.bin", "wb");
+		double e = min_f(p);
+		fwrite(&e, sizeof(double), 1, f);
+		l_bfgs_setup(use_m, n, p, 1.0, min_f, min_fdf);
+		int done = 0;
+		if (mag > 1e-20)
+			for (int x = 0; x < nsteps; x++) {
+				if (!l_bfgs_iteration(p)) break;
+				e = min_f(p);
+				fwrite(&e, sizeof(double), 1, f);
+				done++;
+			}
+		l_bfgs_clear();
+		fclose(f);
+		memcpy(r, p + 3, sizeof(double) * 3 * nv);
+		f = open_out(argv[5], "min_positions.bin", "wb");
+		fwrite(r, sizeof(double), 3 * nv + 3, f);
+		fclose(f);
+		printf("iterations %d E %.17e\n", done, e);
 		return 0;
 	}
 

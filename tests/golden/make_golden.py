@@ -15,6 +15,9 @@ stencils. `--mass` writes <name>.mass.npz for the MASS_CASES instead, from the e
 mesh and params files: the reference's inverse effective mass (dense), its
 mass per point and area0, and the limit-surface weights of the 66 mass
 points of four faces (two regular, two irregular where there are any).
+`--min` writes <name>.min.npz for MIN_CASES: the reference's own L-BFGS
+minimization (100 iterations from the case's evaluation state), the energy
+before and after every iteration and the final state.
 """
 from __future__ import annotations
 
@@ -118,6 +121,19 @@ MASS_CASES = ["ico2_plain", "planar12_deformed"]
 RNRM_CASES = ["ico2_lipids", "planar12_deformed"]
 
 
+MIN_CASES = ["ico2_lipids", "planar12_deformed"]
+
+
+def make_min_case(name: str, work: Path) -> None:
+    """The reference's minimization from the case's evaluation state."""
+    r = np.load(HERE / f"{name}.npz")["r"]
+    pos = work / f"{name}.r.bin"
+    r.tofile(pos)
+    ref = B.reference_min(HERE / f"{name}.mesh", HERE / f"{name}.params", pos, work / name)
+    np.savez_compressed(HERE / f"{name}.min.npz", energies=ref["energies"], r=ref["r"])
+    print(f"{name}: {len(ref['energies']) - 1} iterations, E {ref['energies'][0]:.12g} -> {ref['energies'][-1]:.12g}")
+
+
 def make_rnrm(name: str, work: Path) -> None:
     """The reference's limit points and normals (evaluateRNRM) on every face of
     the case's evaluation state."""
@@ -159,6 +175,10 @@ def main() -> None:
             return
         if "--sub6" in sys.argv:
             make_sub6(Path(td))
+            return
+        if "--min" in sys.argv:
+            for name in MIN_CASES:
+                make_min_case(name, Path(td))
             return
         if "--mass" in sys.argv:
             for name in MASS_CASES:

@@ -92,6 +92,15 @@ class Restraints(C.Structure):
     _fields_ = [("K_area", C.c_double), ("area0", C.c_double), ("K_volume", C.c_double), ("volume0", C.c_double)]
 
 
+class MinimizeOpts(C.Structure):
+    _fields_ = [("max_iterations", C.c_int), ("history", C.c_int), ("max_move", C.c_double)]
+
+
+class MinimizeInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("evaluations", C.c_int), ("energy_initial", C.c_double),
+                ("energy_final", C.c_double), ("grad_rms", C.c_double)]
+
+
 class MassOpts(C.Structure):
     _fields_ = [("mass_scale", C.c_double), ("points_per_edge", C.c_int), ("rel_tol", C.c_double)]
 
@@ -178,6 +187,7 @@ _SIGNATURES = {
     "umcp_mass_apply": [_VP, _D, _D, _D, C.c_double, _D],
     "umcp_mass_apply_device": [_VP, _VP, _VP, _VP, C.c_double, _D],
     "umcp_state_set": [_VP, _D, _D],
+    "umcp_minimize": [_VP, C.POINTER(MinimizeOpts), _D, C.POINTER(MinimizeInfo)],
     "umcp_state_get": [_VP, _D, _D],
     "umcp_run": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int, _D],
     "umcp_run_async": [_VP, C.POINTER(Integrator), C.c_uint64, C.c_int],
@@ -528,6 +538,16 @@ class Mesh:
         """Global area/volume restraints (umcp_restraints_set); area0/volume0 < 0: the resident state's."""
         rs = Restraints(K_area, area0, K_volume, volume0)
         _check(library().umcp_restraints_set(self._h, C.byref(rs)))
+
+    def minimize(self, max_iterations: int = 100, history: int = 0, max_move: float = 1.0):
+        """L-BFGS over the vertex positions from the resident state
+        (umcp_minimize; the reference's Simulation::minimize for a membrane).
+        Returns (energies before and after each iteration, MinimizeInfo)."""
+        e = np.zeros(max_iterations + 1)
+        info = MinimizeInfo()
+        _check(library().umcp_minimize(self._h, C.byref(MinimizeOpts(max_iterations, history, max_move)), _dp(e),
+                                       C.byref(info)))
+        return e[: info.iterations + 1], info
 
     def restraints_clear(self) -> None:
         _check(library().umcp_restraints_set(self._h, None))
