@@ -1,14 +1,18 @@
 // Device kernels of the membrane-surface hot path (sm_103a).
 //
-// face_kernel     one half-warp per face: lanes are quadrature points while
-//                 the five basis contractions, the pointwise energy and
-//                 adjoint, and each point's contribution to every control
-//                 point are formed; then lanes are control points while those
-//                 contributions are summed. Writes per-face gradient partials
-//                 and per-block energy sums; no float atomics.
+// face_tpf_kernel one thread per regular face (precision form): control
+//                 points in thread-private shared memory, basis rows as
+//                 warp-wide broadcasts, gradient sums in registers.
+// face_kernel     one half-warp per face (FP64, and irregular faces): lanes
+//                 are quadrature points while the five basis contractions,
+//                 the pointwise energy and adjoint, and each point's
+//                 contribution to every control point are formed; then lanes
+//                 are control points while those contributions are summed.
+//                 Both write per-face gradient partials and per-block energy
+//                 sums; no float atomics.
 // gather_kernel   per vertex, sums its face partials in a fixed order
-//                 (vertex-major slots), optionally fused with an integrator
-//                 update.
+//                 (slots interleaved by groups of 32 vertices), optionally
+//                 fused with an integrator update.
 // finish_kernel   fixed-order sum of the block partials.
 //
 // The energy model is the reference's surface::fenergy/ifenergy with

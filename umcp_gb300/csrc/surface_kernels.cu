@@ -30,7 +30,8 @@ struct FaceSmem {
   __device__ __forceinline__ void *scratch() { return &Tc[0][0][0]; }
 };
 
-// Precision form: control points and per-point contributions are stored
+// Precision form (the half-warp kernel runs the irregular faces there; the
+// regular ones take face_tpf_kernel): control points and per-point contributions are stored
 // coordinate-major, so four control points of one coordinate are one float4
 // and both contractions run as paired FP32 multiply-adds (two control points
 // per instruction).
@@ -285,7 +286,7 @@ __device__ __forceinline__ void point_pass_f32(FaceSmem<float, NCP, NPT> &sm, in
 //     point, control points broadcast), pointwise energy and adjoint, and the
 //     adjoint's contribution to every control point (written transposed).
 //  3. lanes = control points: sum the contributions over the points; write the
-//     alpha-scaled gradient partial to its vertex-major slot.
+//     alpha-scaled gradient partial to its slot.
 // Returns the face's energy terms and dE/dalpha summed over the half-warp.
 template <typename T, int NCP, int NPT>
 __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, int lane, unsigned hmask,
