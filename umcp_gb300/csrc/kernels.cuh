@@ -108,7 +108,11 @@ __device__ __forceinline__ float qdiv(float a, float, float ib) { return a * ib;
 // (area, curvature, angle) and writes dE/d{Ru,Rv,Suu,Suv,Svv} into Kb, and
 // the angle-term part of dE/d{Ru,Rv} into Kreg (needed only for the box-scale
 // derivative on irregular faces, src/grad.C:7414-7421).
-template <typename T>
+// KG_REG = false: the caller has kg == 0 and k_reg == 0, and the Gaussian
+// curvature and angle terms (zeros then) are left out; results agree with the
+// full form's to rounding (the compiler may fuse a product and sum that the
+// full form keeps apart).
+template <typename T, bool KG_REG = true>
 __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T rr0, T dudv, T P2, T Hbar, T Pres,
                                               T kc, T KA, T kg, T k_reg, T *ea, T *ec, T *er, Vec3<T> Kb[5],
                                               Vec3<T> Kreg[2]) {
@@ -120,16 +124,18 @@ __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T r
   // g = sqrt(W), 1/W, W^-3/2, sqrt(E11 E22) and the reciprocals of g, g0,
   // sqrt(E11 E22), E11, E22 (FP32: from two reciprocal square roots and one
   // reciprocal; FP64: divisions, ib unused)
-  T g, iW, ig3, sEE, ig = 0, ig0 = 0, isEE = 0, iE11 = 0, iE22 = 0;
+  T g, iW, ig3, sEE = 0, ig = 0, ig0 = 0, isEE = 0, iE11 = 0, iE22 = 0;
   if constexpr (sizeof(T) == 4) {
     ig = rsqrt_nr(W);
     g = W * ig;
     iW = ig * ig;
     ig3 = iW * ig;
-    isEE = rsqrt_nr(E11 * E22);
-    sEE = E11 * E22 * isEE;
-    iE11 = E22 * isEE * isEE;
-    iE22 = E11 * isEE * isEE;
+    if constexpr (KG_REG) {
+      isEE = rsqrt_nr(E11 * E22);
+      sEE = E11 * E22 * isEE;
+      iE11 = E22 * isEE * isEE;
+      iE22 = E11 * isEE * isEE;
+    }
     ig0 = rcp_nr(g0);
   } else {
     g = sqrt(W);
@@ -138,32 +144,43 @@ __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T r
     sEE = sqrt(E11 * E22);
   }
   T Tt = l * E22 - T(2) * k * E12 + n * E11;
-  T Q = l * n - k * k;
   T H = -Tt * ig3;
-  T Kg = Q * iW * iW - T(kSafety * 0.25);
   T dH = H - Hbar;
-  T val = qdiv(E12, sEE, isEE);
-  T dv = val - rr0;
   T dg = g - g0;
-  *ec = T(0.25) * kc * w * (P2 * dH * dH + Pres) + dudv * g0 * w * kg * Kg;
+  *ec = T(0.25) * kc * w * (P2 * dH * dH + Pres);
   *ea = qdiv(dudv * w * KA * dg * dg, g0, ig0);
-  *er = k_reg * dv * dv;
+  *er = T(0);
   // adjoints
   T Hb = T(0.5) * kc * w * P2 * dH;
-  T Kb_ = dudv * g0 * w * kg;
   T gb = qdiv(T(2) * dudv * w * KA * dg, g0, ig0);
-  T vb = T(2) * k_reg * dv;
   T Tb = -Hb * ig3;
-  T Qb = Kb_ * iW * iW;
-  T Wb = Hb * T(1.5) * Tt * ig3 * iW - T(2) * Kb_ * Q * iW * iW * iW + qdiv(gb, T(2) * g, T(0.5) * ig);
-  T lb = Tb * E22 + Qb * n;
-  T kb = T(-2) * Tb * E12 - T(2) * Qb * k;
-  T nb = Tb * E11 + Qb * l;
-  T rE11 = qdiv(T(-0.5) * vb * val, E11, iE11), rE12 = qdiv(vb, sEE, isEE),
+  T Wb = Hb * T(1.5) * Tt * ig3 * iW + qdiv(gb, T(2) * g, T(0.5) * ig);
+  T lb = Tb * E22, kb = T(-2) * Tb * E12, nb = Tb * E11;
+  T E11b = Tb * n, E12b = T(-2) * Tb * k, E22b = Tb * l;
+  T rE11 = 0, rE12 = 0, rE22 = 0;
+  if constexpr (KG_REG) {
+    // Gaussian curvature (kg) and the angle regulariser (k_reg), in the
+    // order the full expressions add them
+    T Q = l * n - k * k;
+    T Kg = Q * iW * iW - T(kSafety * 0.25);
+    T val = qdiv(E12, sEE, isEE);
+    T dv = val - rr0;
+    *ec = *ec + dudv * g0 * w * kg * Kg;
+    *er = k_reg * dv * dv;
+    T Kb_ = dudv * g0 * w * kg;
+    T vb = T(2) * k_reg * dv;
+    T Qb = Kb_ * iW * iW;
+    Wb = Hb * T(1.5) * Tt * ig3 * iW - T(2) * Kb_ * Q * iW * iW * iW + qdiv(gb, T(2) * g, T(0.5) * ig);
+    lb = Tb * E22 + Qb * n;
+    kb = T(-2) * Tb * E12 - T(2) * Qb * k;
+    nb = Tb * E11 + Qb * l;
+    rE11 = qdiv(T(-0.5) * vb * val, E11, iE11);
+    rE12 = qdiv(vb, sEE, isEE);
     rE22 = qdiv(T(-0.5) * vb * val, E22, iE22);
-  T E11b = Tb * n + rE11;
-  T E12b = T(-2) * Tb * k + rE12;
-  T E22b = Tb * l + rE22;
+    E11b = Tb * n + rE11;
+    E12b = T(-2) * Tb * k + rE12;
+    E22b = Tb * l + rE22;
+  }
   Kb[2] = {lb * m.x, lb * m.y, lb * m.z};
   Kb[3] = {kb * m.x, kb * m.y, kb * m.z};
   Kb[4] = {nb * m.x, nb * m.y, nb * m.z};

@@ -1417,7 +1417,7 @@ __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, co
 // STAGED: the face's tables come from cur (row lane) instead of global
 // memory; with next given, the next faces' control-point positions are
 // prefetched into L1 half-way through (every lane of the warp is active then).
-template <bool STAGED>
+template <bool STAGED, bool KG_REG>
 __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
                                          const float alpha[3], const float ialpha[3], const Moduli<float> &mod,
                                          float dudv, bool vec, float *__restrict__ partial, float e3[3],
@@ -1547,8 +1547,8 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
     Vec3<float> Kb[5], Kreg[2];
     float a, c, r;
-    point_adjoint<float>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a, &c, &r,
-                         Kb, Kreg);
+    point_adjoint<float, KG_REG>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a,
+                                 &c, &r, Kb, Kreg);
     ea += a;
     ec += c;
     er += r;
@@ -1655,6 +1655,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
   // the launch wrapper checks that the tables are 16-byte aligned (tpf_stage_ok)
   const float dudv = (float)L.dudv;
+  const bool kg_reg = P.kg != 0.0 || P.k_reg != 0.0;  // else the pointwise step leaves those terms out
   const int n = L.nfaces, stride = gridDim.x * kThreads;
   Stage *st = stages + 2 * warp;
   SharedSums acc{reinterpret_cast<float *>(tpf_dyn + kStageBytes) + threadIdx.x};
@@ -1675,8 +1676,12 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     const int f = fb + lane;
     if (f < n) {
       float e3[3], da[3];
-      tpf_face<true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
-                     nb < n ? &st[buf ^ 1] : nullptr, lane);
+      if (kg_reg)
+        tpf_face<true, true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                             nb < n ? &st[buf ^ 1] : nullptr, lane);
+      else
+        tpf_face<true, false>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                              nb < n ? &st[buf ^ 1] : nullptr, lane);
       acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
       acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
       if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
@@ -1751,6 +1756,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
       const Moduli<float> mod(P);
       const int end = tile.first + tile.count;
       float *partial = (float *)sj.partial;
+      const bool kg_reg = P.kg != 0.0 || P.k_reg != 0.0;  // else the pointwise step leaves those terms out
       if (tpf_stage_ok(src) && tile.first % 4 == 0) {
         // the single-mesh pipeline within the tile: this warp's next 32 faces
         // are copied while the current 32 compute
@@ -1766,8 +1772,12 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
           const int f = fb + lane;
           if (f < end) {
             float e3[3], da[3];
-            tpf_face<true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
-                           nb < end ? &st[buf ^ 1] : nullptr, lane);
+            if (kg_reg)
+              tpf_face<true, true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                                   nb < end ? &st[buf ^ 1] : nullptr, lane);
+            else
+              tpf_face<true, false>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+                                    nb < end ? &st[buf ^ 1] : nullptr, lane);
             acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
           }
           __syncwarp();
@@ -1780,7 +1790,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
           const int f = fb + lane;
           if (f < end) {
             float e3[3], da[3];
-            tpf_face<false>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+            if (kg_reg) tpf_face<false, true>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+            else tpf_face<false, false>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
             acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
           }
         }
