@@ -56,6 +56,7 @@ struct umcp_batch {
   int vgrid = 0;
   // device tables
   DevBuf d_jobs, d_tiles, d_vtiles, d_tile_off, d_tile_idx, d_counts, d_live, d_prog, d_start, d_step0, d_tile_sums;
+  DevBuf d_next_tile;  // tile counter of the regular face launch
   size_t cap_jobs = 0, cap_tiles = 0, cap_vtiles = 0;
   // host copies of the counts and the latest progress (pinned)
   int counts[kCountWords] = {};
@@ -264,7 +265,8 @@ static cudaError_t queue_faces_t(umcp_batch *b) {
   auto launch = [&](int t, cudaStream_t on) {
     return launch_batch_faces<T>(b->d_jobs.as<BatchJob>(), t, b->d_tiles.as<BatchTile>(), b->d_counts.as<int>(),
                                  b->basis[t].as<double>(), b->weight[t].as<double>(), kTypeNcp[t], b->npt[t],
-                                 b->dudv[t], t > 0, b->d_tile_sums.as<double>(), b->face_grid[t], on);
+                                 b->dudv[t], t > 0, b->d_tile_sums.as<double>(), b->face_grid[t],
+                                 b->d_next_tile.as<int>(), on);
   };
   cudaError_t e = cudaSuccess;
   const bool irregular = b->have_type[1] || b->have_type[2];
@@ -368,6 +370,7 @@ extern "C" umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umc
   UMCP_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   UMCP_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
   UMCP_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
+  UMCP_CUDA(b->d_next_tile.alloc(sizeof(int)));
   b->ctx = ctx;
   b->precision = precision;
   if (opts) {

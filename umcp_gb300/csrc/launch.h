@@ -167,9 +167,11 @@ constexpr int kVertexTile = 256;  // vertices per vertex tile (one thread each)
 // tile's energy terms. Persistent grid; tiles of stopped or finished jobs are
 // skipped.
 template <typename T>
+// next_tile: a device int the regular FP32 launch hands tiles out from (zeroed
+// by the launch wrapper, on s, before the kernel).
 cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile *tiles, const int *counts,
                                const double *basis, const double *weight, int ncp, int npt, double dudv,
-                               int irregular, double *tile_sums, int grid, cudaStream_t s);
+                               int irregular, double *tile_sums, int grid, int *next_tile, cudaStream_t s);
 // Per job: tile sums in listed order (tile_idx[tile_off[j] .. tile_off[j+1])),
 // energy record, flags, steps done; live[j] and prog[j] = {done, status}.
 cudaError_t launch_batch_reduce(const BatchJob *jobs, const int *counts, int max_jobs, const int *tile_off,

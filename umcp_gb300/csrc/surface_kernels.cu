@@ -1723,11 +1723,12 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
 __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     batch_face_tpf_kernel(const BatchJob *__restrict__ jobs, int group, const BatchTile *__restrict__ tiles,
                           const int *__restrict__ counts, const double *__restrict__ basis,
-                          const double *__restrict__ weight, double dudv_d, double *__restrict__ tile_sums) {
+                          const double *__restrict__ weight, double dudv_d, double *__restrict__ tile_sums,
+                          int *__restrict__ next_tile) {
   using namespace tpf;
   __shared__ Smem sm;
   __shared__ BatchFaceJob sj;
-  __shared__ int s_active;
+  __shared__ int s_active, s_tile;
   extern __shared__ __align__(16) unsigned char tpf_dyn[];
   Stage *st = reinterpret_cast<Stage *>(tpf_dyn) + 2 * (threadIdx.x >> 5);  // this warp's two stages
   const int ntiles = counts[group], tile_base = counts[3 + group];
@@ -1735,9 +1736,16 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   tpf_stage(sm, basis, weight);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float dudv = (float)dudv_d;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // Tiles are handed out by a counter (zeroed before the launch), so blocks
+  // that draw cheap tiles take more; each tile's sums go to its own row, so
+  // the results do not depend on which block took which tile.
+  for (;;) {
+    __syncthreads();  // the previous tile's readers of sj, s_tile and sm.red are done
+    if (threadIdx.x == 0) s_tile = atomicAdd(next_tile, 1);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
     const BatchTile tile = tiles[tile_base + t];
-    __syncthreads();  // the previous tile's readers of sj and sm.red are done
     {
       const int *src = reinterpret_cast<const int *>(&jobs[tile.job].f);
       int *dst = reinterpret_cast<int *>(&sj);
@@ -2700,7 +2708,7 @@ template int batch_face_blocks<float>(int, int);
 template <typename T>
 cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile *tiles, const int *counts,
                                const double *basis, const double *weight, int ncp, int npt, double dudv,
-                               int irregular, double *tile_sums, int grid, cudaStream_t s) {
+                               int irregular, double *tile_sums, int grid, int *next_tile, cudaStream_t s) {
   constexpr int NT = dev::FaceCfg<T>::threads;
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
@@ -2711,8 +2719,11 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
         if (e != cudaSuccess) return e;
         attr = true;
       }
+      if (!next_tile) return cudaErrorInvalidValue;
+      cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
+      if (e != cudaSuccess) return e;
       dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes, s>>>(
-          jobs, group, tiles, counts, basis, weight, dudv, tile_sums);
+          jobs, group, tiles, counts, basis, weight, dudv, tile_sums, next_tile);
       return cudaGetLastError();
     }
   }
@@ -2731,9 +2742,10 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
 }
 template cudaError_t launch_batch_faces<double>(const BatchJob *, int, const BatchTile *, const int *,
                                                 const double *, const double *, int, int, double, int, double *, int,
-                                                cudaStream_t);
+                                                int *, cudaStream_t);
 template cudaError_t launch_batch_faces<float>(const BatchJob *, int, const BatchTile *, const int *, const double *,
-                                               const double *, int, int, double, int, double *, int, cudaStream_t);
+                                               const double *, int, int, double, int, double *, int, int *,
+                                               cudaStream_t);
 
 cudaError_t launch_batch_reduce(const BatchJob *jobs, const int *counts, int max_jobs, const int *tile_off,
                                 const int *tile_idx, const double *tile_sums, int *live, unsigned long long *prog,
