@@ -66,11 +66,11 @@ METRIC = "BD vertex-steps/s"
 L2_BYTES = 129 * 1024 * 1024
 SM_COUNT, FP32_LANES_PER_SM = 152, 128
 # DRAM bytes per face of the batched face launches, from the ncu capture of
-# the first 64 vesicles of the workload (dram__bytes_read.sum +
-# dram__bytes_write.sum of the regular and valence-5 launches: 97.51 + 23.80
-# + 2.17 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled from
-# it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 123.50e6 / 392960
+# the first 64 vesicles of the workload at 512-face tiles (dram__bytes_read.sum
+# + dram__bytes_write.sum of the regular and valence-5 launches: 108.47 +
+# 28.08 + 2.18 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
+# from it by its face count.
+BATCH_FACE_DRAM_BYTES_PER_FACE = 138.74e6 / 392960
 
 
 def parse_args():
