@@ -288,8 +288,9 @@ typedef struct {
   double energy_initial, energy_final;
   double grad_rms;        /* rms of the final gradient over the 3 nv position coordinates */
 } umcp_minimize_info;
-/* opts NULL: the reference's settings. energies (may be NULL): the energy
- * before the first iteration and after each, max_iterations + 1 values. */
+/* opts NULL: the reference's settings. energies (may be NULL, else room for
+ * max_iterations + 1 values): the energy before the first iteration and
+ * after each; only the first info->iterations + 1 are written. */
 umcp_status umcp_minimize(umcp_mesh *mesh, const umcp_minimize_opts *opts, double *energies,
                           umcp_minimize_info *info);
 /* One step of the integrator on HOST state: copies r (3*nv+3) and p (3*nv,
