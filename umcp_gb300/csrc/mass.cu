@@ -136,44 +136,77 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
   }
 }
 
-// dense_apply_kernel on FP32 values and an FP32 input: Kahan-compensated FP32
-// sums per thread, the block reduction and the scaling in FP64.
-__global__ void dense_apply32_kernel(int n, const float *__restrict__ A, const double *__restrict__ scalev,
-                                     double scale, const double *__restrict__ alphas, const float4 *__restrict__ in4,
-                                     double *__restrict__ out, int accumulate) {
-  __shared__ double red[3][8];
-  for (int i = blockIdx.x; i < n; i += gridDim.x) {
-    const float *row = A + (size_t)i * n;
-    float s[3] = {0, 0, 0}, c[3] = {0, 0, 0};
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      const float m = row[j];
-      const float4 x4 = in4[j];
-      const float x[3] = {x4.x, x4.y, x4.z};
+// dense_apply_kernel on FP32 values and an FP32 input packed as one float4
+// per row. One warp takes kDenseRows rows at once, so each coalesced load of
+// the input serves all of them; every lane keeps kDenseAhead columns' loads of
+// each row in flight (the matrix streams from HBM once, with an evict-first
+// hint, while the input stays cached). Kahan-compensated FP32 sums per lane
+// and row, then the lanes' sums in FP64 in a fixed butterfly order, and the
+// scaling in FP64.
+constexpr int kDenseRows = 4;
+constexpr int kDenseAhead = 8;
+constexpr int kDenseThreads = 256;
+__global__ void __launch_bounds__(kDenseThreads) dense_apply32_kernel(int n, const float *__restrict__ A,
+                                                                      const double *__restrict__ scalev, double scale,
+                                                                      const double *__restrict__ alphas,
+                                                                      const float4 *__restrict__ in4,
+                                                                      double *__restrict__ out, int accumulate) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (kDenseThreads / 32);
+  for (int i0 = (blockIdx.x * (kDenseThreads / 32) + (threadIdx.x >> 5)) * kDenseRows; i0 < n;
+       i0 += warps * kDenseRows) {
+    const int nr = n - i0 < kDenseRows ? n - i0 : kDenseRows;
+    float s[kDenseRows][3], c[kDenseRows][3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const float y = m * x[q] - c[q], t = s[q] + y;
-        c[q] = (t - s[q]) - y;
-        s[q] = t;
+    for (int r = 0; r < kDenseRows; ++r)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) s[r][q] = c[r][q] = 0.f;
+    for (int j0 = lane; j0 < n; j0 += 32 * kDenseAhead) {
+      float4 x[kDenseAhead];
+      float m[kDenseRows][kDenseAhead];
+#pragma unroll
+      for (int u = 0; u < kDenseAhead; ++u) {
+        const int j = j0 + 32 * u;
+        x[u] = j < n ? __ldg(&in4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < kDenseRows; ++r)
+          m[r][u] = (j < n && r < nr) ? __ldcs(&A[(size_t)(i0 + r) * n + j]) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < kDenseAhead; ++u) {
+        if (j0 + 32 * u >= n) break;
+        const float xv[3] = {x[u].x, x[u].y, x[u].z};
+#pragma unroll
+        for (int r = 0; r < kDenseRows; ++r)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float y = fmaf(m[r][u], xv[q], -c[r][q]), t = s[r][q] + y;
+            c[r][q] = (t - s[r][q]) - y;
+            s[r][q] = t;
+          }
       }
     }
-    double a[3] = {(double)s[0] - c[0], (double)s[1] - c[1], (double)s[2] - c[2]};
-    for (int off = 16; off >= 1; off >>= 1)
+    double a[kDenseRows][3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) a[q] += __shfl_xor_sync(0xffffffffu, a[q], off);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { red[0][w] = a[0]; red[1][w] = a[1]; red[2][w] = a[2]; }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-      const int q = threadIdx.x;
-      double t = 0;
-      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[q][k];
-      const double al = alphas ? alphas[q] : 1.0;
-      double f = scale / (al * al);
-      if (scalev) f *= scalev[(size_t)q * n + i];
-      const double v = f * t;
-      out[3 * (size_t)i + q] = accumulate ? out[3 * (size_t)i + q] + v : v;
-    }
-    __syncthreads();
+    for (int r = 0; r < kDenseRows; ++r)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        a[r][q] = (double)s[r][q] - (double)c[r][q];
+        for (int off = 16; off >= 1; off >>= 1) a[r][q] += __shfl_xor_sync(0xffffffffu, a[r][q], off);
+      }
+    // lane 3 r + q writes component q of row i0 + r
+#pragma unroll
+    for (int r = 0; r < kDenseRows; ++r)
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        if (lane == 3 * r + q && r < nr) {
+          const int i = i0 + r;
+          const double al = alphas ? alphas[q] : 1.0;
+          double f = scale / (al * al);
+          if (scalev) f *= scalev[(size_t)q * n + i];
+          const double v = f * a[r][q];
+          out[3 * (size_t)i + q] = accumulate ? out[3 * (size_t)i + q] + v : v;
+        }
   }
 }
 
@@ -233,10 +266,12 @@ cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double sc
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
     const int grid = m->mrows < sms * 8 ? m->mrows : sms * 8;
-    if (m->mass_f32)
-      dense_apply32_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<float>(), scalev, scale, alphas,
-                                                m->min32.as<float4>(), out, accumulate);
-    else
+    if (m->mass_f32) {
+      const int groups = (m->mrows + kDenseRows - 1) / kDenseRows, per_block = kDenseThreads / 32;
+      const int blocks = (groups + per_block - 1) / per_block;
+      dense_apply32_kernel<<<blocks < sms * 8 ? blocks : sms * 8, kDenseThreads, 0, s>>>(
+          m->mrows, m->mdense.as<float>(), scalev, scale, alphas, m->min32.as<float4>(), out, accumulate);
+    } else
       dense_apply_kernel<<<grid, 256, 0, s>>>(m->mrows, m->mdense.as<double>(), scalev, scale, alphas, in, out,
                                               accumulate);
     return cudaGetLastError();
