@@ -144,9 +144,9 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
 // and row, then the lanes' sums in FP64 in a fixed butterfly order, and the
 // scaling in FP64.
 constexpr int kDenseRows = 4;
-constexpr int kDenseAhead = 8;
+constexpr int kDenseAhead = 4;
 constexpr int kDenseThreads = 256;
-__global__ void __launch_bounds__(kDenseThreads) dense_apply32_kernel(int n, const float *__restrict__ A,
+__global__ void __launch_bounds__(kDenseThreads, 3) dense_apply32_kernel(int n, const float *__restrict__ A,
                                                                       const double *__restrict__ scalev, double scale,
                                                                       const double *__restrict__ alphas,
                                                                       const float4 *__restrict__ in4,
