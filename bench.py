@@ -92,6 +92,21 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def replica_seed(rank: int) -> int:
+    """Seed of a rank's vesicle set: every rank is an independent replica of the workload."""
+    return WORKLOAD["seed"] + 1000 * rank
+
+
+def over_ranks(x: float, op: str, device) -> float:
+    """x reduced over all ranks ("max" or "sum"), returned on every rank."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -404,7 +419,7 @@ def engine_arm(args) -> None:
     tmp = Path(tempfile.mkdtemp(prefix="umcp_bench_"))
     ctx = U.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device(f"cuda:{local}"))
-    specs = W.vesicle_specs(args.vesicles, WORKLOAD["seed"] + 1000 * rank)
+    specs = W.vesicle_specs(args.vesicles, replica_seed(rank))
     pp32, meshes32 = build_vesicles(specs, tmp / "fp32", U.FP32_CENTRED, ctx, U, W)
     nv_total = sum(m.nv for m in meshes32)
     K, Wu = args.steps, max(args.warmup, 3)
@@ -422,14 +437,14 @@ def engine_arm(args) -> None:
         t_wall0 = time.perf_counter()
         total_s = time_batch(batch, ctx, stream, torch, K)
         t_wall = time.perf_counter() - t_wall0
+    nv_job = nv_total  # vertices of every rank's vesicles (the ranks' sets differ)
     if world > 1:
         torch.distributed.barrier()
-        t = torch.tensor([total_s], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+        total_s = over_ranks(total_s, "max", f"cuda:{local}")  # the job's time is its slowest rank's
+        nv_job = int(over_ranks(nv_total, "sum", f"cuda:{local}"))
     done, status = batch.poll()
     assert np.all(done == Wu + K) and np.all(status == 0), "a vesicle stopped early"
-    value = nv_total * K * world / total_s
+    value = nv_job * K / total_s
 
     # ---- roofline: the batch's face launches alone
     F = 30
@@ -469,6 +484,8 @@ def engine_arm(args) -> None:
         "gpu_launches": info.kernels_per_step * K,
         "wall_s_timed": t_wall,
     }
+    if world > 1:
+        out["config"]["vertices_all_ranks"] = nv_job  # each rank its own replica set; config is rank 0's
     e32_first = np.array([m.energies(1)[0] for m in meshes32])
     del batch
 
