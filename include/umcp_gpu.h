@@ -50,7 +50,7 @@ typedef struct {
   int precision;      /* umcp_precision */
   const char *lipid_directives; /* text holding "lipid library|inner|outer ..." lines, or NULL */
   int face_kernel;    /* precision form, regular faces: 0 FP32 SIMT kernel (default, faster here),
-                         1 tcgen05 tensor-core kernel (3xTF32 contractions) */
+                         1 tcgen05 tensor-core kernel (kind::f16 MMAs on fp16 hi/lo splits) */
 } umcp_params;
 
 /* Sizes of a plan. */
@@ -153,16 +153,26 @@ umcp_status umcp_energy_grad_device(umcp_mesh *mesh, const double *d_r, double *
  * framework's CUDA-graph capture, or under a device-memory budget owned by
  * another runtime). Same inputs and outputs as umcp_energy_grad_device (the
  * mesh's plan tables, made at set-up, plus the caller's d_r, d_E, d_g; g is
- * accumulated); every scratch buffer lives in one 32 MiB file-scope device
- * array that each GPU loading the library holds until exit. Meshes whose
- * scratch exceeds 32 MiB (about 110,000 faces in FP64, 200,000 in the FP32
- * form) are rejected with UMCP_ERR_NOMEM. The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture. All calls on one device share that
- * device's array and it keeps the last call's contents: calls whose work
- * overlaps on the GPU (e.g. from two streams) race. Queued on the mesh's ctx
- * stream; returns without waiting. */
+ * accumulated; d_E may be NULL, the energy then goes to the mesh's own
+ * slot); every scratch buffer lives in one 32 MiB file-scope device array
+ * that each GPU loading the library holds until exit. Meshes whose scratch
+ * exceeds 32 MiB (about 110,000 faces in FP64, 190,000 in the FP32 form) are
+ * rejected with UMCP_ERR_NOMEM. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture. All calls on one device share that device's
+ * array and it keeps the last call's contents: calls whose work overlaps on
+ * the GPU (e.g. from two streams) race. Queued on the mesh's ctx stream;
+ * returns without waiting: a non-finite energy (or a tensor-core wait that
+ * gave up) is recorded in the mesh's status word, which
+ * umcp_mesh_check_status reports. */
 umcp_status umcp_energy_grad_static(umcp_mesh *mesh, const double *d_r, double *d_E, double *d_g);
+/* Waits for the mesh's queued work and reports what its kernels recorded
+ * since the last check: UMCP_ERR_NONFINITE (the reference's "nan en." stop,
+ * src/interpLib.C:3770-3774), UMCP_ERR_DIVERGED (src/hd.C:1280-1305),
+ * UMCP_ERR_TIMEOUT, or UMCP_OK; then clears the record. The status of the
+ * asynchronous device-pointer calls (umcp_energy_grad_device,
+ * umcp_energy_grad_static, umcp_run_async). */
+umcp_status umcp_mesh_check_status(umcp_mesh *mesh);
 /* Queues only the per-face pass (quadrature, pointwise energy and adjoint,
  * per-face gradient partials) on the mesh's resident state, without the
  * per-vertex gather or the sums: the unit a roofline measurement times. */

@@ -61,3 +61,8 @@ def load_case(name: str, precision: int = 0):
 def rel_inf(a: np.ndarray, b: np.ndarray) -> float:
     """max |a-b| / max |b|: the gradient tolerance measure used throughout."""
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    """||a-b||_2 / ||b||_2: the norm-wise gradient measure."""
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

@@ -3,7 +3,11 @@ outputs (golden fixtures) and against the oracle at larger sizes.
 
 Tolerances (written here, used below):
   FP64 plain path: energy |dE|/|E| <= 1e-10; gradient max|dg|/max|g| <= 1e-10.
-  FP32 face-centred form: energy |dE|/|E| <= 1e-6; gradient max|dg|/max|g| <= 2e-5.
+  FP32 face-centred form: energy |dE|/|E| <= 1e-6; gradient max|dg|/max|g| <= 1e-6
+  and ||dg||/||g|| <= 1e-6.
+  FP32 form on the tensor-core kernel (an option, not the default): energy
+  <= 1e-6, gradient max|dg|/max|g| <= 3e-5 (its tangents carry fp16-split
+  rounding into the area strain).
   Integrator steps (FP64, same Philox draws as the oracle): positions to 1e-12
   of the largest coordinate.
 """
@@ -13,13 +17,14 @@ import numpy as np
 import pytest
 
 import umcp_gb300 as U
-from conftest import golden_cases, load_case, rel_inf
+from conftest import golden_cases, load_case, rel_inf, rel_l2
 from oracle import bridge as B
 
 pytestmark = pytest.mark.gpu
 
 E64, G64 = 1e-10, 1e-10
-E32, G32 = 1e-6, 2e-5
+E32, G32 = 1e-6, 1e-6
+GTC = 3e-5
 
 
 @pytest.fixture(scope="module")
@@ -76,13 +81,38 @@ def test_energy_grad_is_deterministic(ctx):
     assert E1 == E2 and np.array_equal(g1, g2)
 
 
-@pytest.mark.parametrize("name", ["ico4_plain", "planar12_deformed", "ico3_deformed"])
+@pytest.mark.parametrize("name", golden_cases())
 def test_fp32_centred_form_error_bound(ctx, name):
     plan, prm, gold = load_case(name, precision=U.FP32_CENTRED)
     mesh = U.Mesh(ctx, plan, prm)
     E, g = mesh.energy_grad(gold["r"])
     assert abs(E - gold["E"]) <= E32 * abs(gold["E"])
     assert rel_inf(g[:-3], gold["grad"][:-3]) <= G32
+    assert rel_l2(g[:-3], gold["grad"][:-3]) <= G32
+
+
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_fp32_centred_form_on_benchmark_vesicles(ctx, tmp_path, level):
+    """Vesicles of the batched benchmark (seed 1003; the first three of each
+    subdivision level), at the reference state, where every area force is
+    zero and any rounding of the strain is all that is left of it, and at a
+    state displaced by N(0, 0.05 A): FP32 against the FP64 path."""
+    from umcp_gb300 import workloads as W
+
+    specs = [s for s in W.vesicle_specs(256, 1003) if s.level == level][:3]
+    for s in specs:
+        plan64, prm64 = W._build_vesicle(s, tmp_path, U.FP64, 298.0)
+        plan32, prm32 = W._build_vesicle(s, tmp_path, U.FP32_CENTRED, 298.0)
+        m64, m32 = U.Mesh(ctx, plan64, prm64), U.Mesh(ctx, plan32, prm32)
+        r0 = plan64.positions()
+        for sigma in (0.0, 0.05):
+            r = r0.copy()
+            r[:-3] += np.random.default_rng(s.seed).normal(0.0, sigma, 3 * plan64.nv)
+            E64_, g64 = m64.energy_grad(r)
+            E32_, g32 = m32.energy_grad(r)
+            assert abs(E32_ - E64_) <= E32 * abs(E64_), (s, sigma)
+            assert rel_inf(g32[:-3], g64[:-3]) <= G32, (s, sigma)
+            assert rel_l2(g32[:-3], g64[:-3]) <= G32, (s, sigma)
 
 
 def test_fp32_centred_form_on_the_planar_benchmark_membrane(ctx, tmp_path):
@@ -97,6 +127,7 @@ def test_fp32_centred_form_on_the_planar_benchmark_membrane(ctx, tmp_path):
     E32_, g32 = U.Mesh(ctx, plan, prm32).energy_grad(r)
     assert abs(E32_ - E64_) <= E32 * abs(E64_)
     assert rel_inf(g32, g64) <= G32
+    assert rel_l2(g32, g64) <= G32
 
 
 def _oracle_run(plan, prm, r, mode, dt, gamma, D, seed, stream, nsteps, mass=None):
@@ -221,16 +252,17 @@ def test_divergence_stops_the_run(ctx):
 
 @pytest.mark.parametrize("name", ["ico3_deformed", "planar12_deformed", "ico4_plain", "ico2_lipids"])
 def test_tensor_core_face_kernel_matches_reference(ctx, name):
-    """The tcgen05 form of the regular-face pass (3xTF32 contractions on
-    affine-centred control points) meets the precision form's bounds against
-    the reference and is deterministic; its meshes run the same integrators."""
+    """The tcgen05 form of the regular-face pass (kind::f16 contractions on
+    affine-centred control points) meets its bounds against the reference
+    (energy as the precision form, gradient GTC) and is deterministic; its
+    meshes run the same integrators."""
     plan, prm, gold = load_case(name, U.FP32_CENTRED)
     prm.face_kernel = U.TENSOR_CORES
     mesh = U.Mesh(ctx, plan, prm)
     r = gold["r"]
     E, g = mesh.energy_grad(r)
     assert abs(E - gold["E"]) <= E32 * abs(gold["E"])
-    assert rel_inf(g[:-3], gold["grad"][:-3]) <= G32 * 1.5
+    assert rel_inf(g[:-3], gold["grad"][:-3]) <= GTC
     E2, g2 = mesh.energy_grad(r)
     assert E2 == E and np.array_equal(g2, g)
     it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.00125, seed=3)

@@ -183,6 +183,7 @@ _SIGNATURES = {
     "umcp_energy_grad": [_VP, _D, _D, _D],
     "umcp_energy_grad_device": [_VP, _VP, _VP, _VP],
     "umcp_energy_grad_static": [_VP, _VP, _VP, _VP],
+    "umcp_mesh_check_status": [_VP],
     "umcp_mass_set": [_VP, C.c_int, _I, _I, _D],
     "umcp_mass_apply": [_VP, _D, _D, _D, C.c_double, _D],
     "umcp_mass_apply_device": [_VP, _VP, _VP, _VP, C.c_double, _D],
@@ -274,7 +275,7 @@ def _ip(a: np.ndarray | None):
 
 
 SIMT = 0          # Params.face_kernel: the FP32 SIMT face kernel (default)
-TENSOR_CORES = 1  # regular faces of the precision form through tcgen05 (3xTF32 contractions)
+TENSOR_CORES = 1  # regular faces of the precision form through tcgen05 (kind::f16 MMAs on fp16 hi/lo splits)
 
 
 def params(kc=14.0, KA=0.215, kg=0.0, k_reg=0.0, temperature=298.0, precision=FP64, lipids: str | None = None,
@@ -481,6 +482,11 @@ class Mesh:
         """As energy_grad_device, with all scratch in the library's static device
         array instead of the mesh's own buffers (no allocation at call time)."""
         _check(library().umcp_energy_grad_static(self._h, C.c_void_p(d_r), C.c_void_p(d_E), C.c_void_p(d_g)))
+
+    def check_status(self) -> None:
+        """Waits for the mesh's queued work; raises UmcpError if a kernel recorded
+        a non-finite energy, a divergence or a timeout since the last check."""
+        _check(library().umcp_mesh_check_status(self._h))
 
     def mass_set(self, row_ptr: np.ndarray, col: np.ndarray, val: np.ndarray) -> None:
         row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int32)

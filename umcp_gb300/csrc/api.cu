@@ -537,12 +537,14 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
   if (m->precision == UMCP_FP32_CENTRED) {
     arena.uninit(m->rhi, 3 * (size_t)ME.nv * sizeof(float));
     arena.uninit(m->rlo, 3 * (size_t)ME.nv * sizeof(float));
+    arena.stage(m->r0, PL.ref_r);  // the state the reference metric g0 was taken at
+    arena.uninit(m->dsp, 3 * (size_t)ME.nv * sizeof(float));
   }
   UMCP_CUDA(arena.commit(m->arena));
   if (m->precision == UMCP_FP32_CENTRED) {
     // On the legacy stream, which does not wait for (or stall) work queued on
     // the context's non-blocking stream, e.g. a batch a server is running.
-    UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), 0));
+    UMCP_CUDA(launch_split_positions(3 * ME.nv, m->r.as<double>(), m->f32pos(), 0));
     UMCP_CUDA(cudaStreamSynchronize(0));
     m->split_valid = true;
   }
@@ -696,12 +698,10 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
                             m->partial.as<float>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
                             fin ? *fin : none, on);
       else
-        e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
-                            m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+        e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->f32pos(), m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
                             fin ? *fin : none, on);
     } else {
-      e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
-                          m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+      e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->f32pos(), m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
                           fin ? *fin : none, on);
     }
     if (e != cudaSuccess) return e;
@@ -724,12 +724,12 @@ static cudaError_t queue_energy_grad(umcp_mesh *m, const double *d_r, double *d_
   cudaError_t e = cudaSuccess;
   if (faces_only) {
     if (sizeof(T) == 4 && !m->split_valid)
-      e = launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s);
+      e = launch_split_positions(3 * m->nv, m->r.as<double>(), m->f32pos(), s);
     m->split_valid = true;
     return e == cudaSuccess ? queue_faces<T>(m, m->r.as<double>(), nullptr) : e;
   }
   if (sizeof(T) == 4) {
-    e = launch_split_positions(3 * m->nv, d_r, m->rhi.as<float>(), m->rlo.as<float>(), s);
+    e = launch_split_positions(3 * m->nv, d_r, m->f32pos(), s);
     m->split_valid = (d_r == m->r.as<double>());
   }
   if (e != cudaSuccess) return e;
@@ -861,7 +861,7 @@ extern "C" umcp_status umcp_plan_device_bytes(const umcp_plan *plan, umcp_ctx *c
   b += slots * 3 * (f32 ? 4 : 8);                     // partial
   b += 3 * nst * 8 + 2 * 3 * nv * 8;                  // r, g, r_eval; p, qdot
   b += 8 + 3 * 8 + 4 + 2 * 8 + 4 + 3 * 8;             // E, parts, status, cnt, done, alphas
-  if (f32) b += 2 * 3 * nv * 4;                       // rhi, rlo
+  if (f32) b += 3 * 3 * nv * 4 + 3 * nv * 8;          // rhi, rlo, dsp; r0
   b += (size_t)n_energies * 8;                        // energy record
   *bytes = b;
   return UMCP_OK;
@@ -945,8 +945,7 @@ extern "C" umcp_status umcp_state_set(umcp_mesh *m, const double *r, const doubl
   const size_t nst = 3 * (size_t)m->nv + 3;
   if (r) UMCP_CUDA(cudaMemcpyAsync(m->r.p, r, nst * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
   if (r && m->precision == UMCP_FP32_CENTRED) {
-    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(),
-                                     m->ctx->stream));
+    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->f32pos(), m->ctx->stream));
     m->split_valid = true;
   }
   if (p) UMCP_CUDA(cudaMemcpyAsync(m->p.p, p, (nst - 3) * sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
@@ -1033,7 +1032,7 @@ extern "C" umcp_status umcp_restraints_set(umcp_mesh *m, const umcp_restraints *
     m->rs = umcp_mesh::Restraints{true, 0, 1, 0, 0};
     // the precision form's sums read the hi/lo pairs, which may hold the last evaluated state
     if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
-      UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
+      UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->f32pos(), s));
     m->split_valid = true;
     UMCP_CUDA(launch_geo_sums(geo_args(m, m->r.as<double>()), m->precision == UMCP_FP64, s));
     double gt[kGeoWords];
@@ -1102,8 +1101,7 @@ static cudaError_t queue_step_t(umcp_mesh *m, const StepArgs &a, int use_mass, d
   if (e != cudaSuccess) return e;
   if (a.kind == 0 || !use_mass)
     return launch_gather_step<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), a, m->cnt.as<uint64_t>(),
-                                 m->r.as<double>(), m->p.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(),
-                                 m->status.as<int>(), s);
+                                 m->r.as<double>(), m->p.as<double>(), m->f32pos(), m->status.as<int>(), s);
   e = cudaMemsetAsync(m->g.p, 0, 3 * (size_t)m->nv * sizeof(double), s);
   if (e == cudaSuccess) e = launch_gather<T>(m->nv, m->partial.as<T>(), m->off.as<int>(), m->g.as<double>(), s);
   if (e == cudaSuccess)
@@ -1111,8 +1109,8 @@ static cudaError_t queue_step_t(umcp_mesh *m, const StepArgs &a, int use_mass, d
   if (e == cudaSuccess)
     e = queue_mass_apply(m, nullptr, 1.0, nullptr, m->p.as<double>(), m->qdot.as<double>(), 0, s);
   if (e == cudaSuccess)
-    e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->rhi.as<float>(),
-                     m->rlo.as<float>(), m->status.as<int>(), s);
+    e = launch_drift(m->nv, a, m->r.as<double>(), m->p.as<double>(), m->qdot.as<double>(), m->f32pos(),
+                     m->status.as<int>(), s);
   return e;
 }
 
@@ -1163,7 +1161,7 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
     if (m->batch) batch_mesh_changed(m->batch);  // so does its batch job entry
   }
   if (m->precision == UMCP_FP32_CENTRED && !m->split_valid)
-    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->rhi.as<float>(), m->rlo.as<float>(), s));
+    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->f32pos(), s));
   m->split_valid = true;  // every step rewrites the pairs of the new positions
   UMCP_CUDA(ensure_pinned(m));
   m->h_cnt[0] = step0;
@@ -1251,7 +1249,8 @@ static void *g_static_scratch_addr[128];  // device address of the array, per de
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, double *d_E, double *d_g) {
-  if (!m || !d_r || !d_E) return fail(UMCP_ERR_INVALID, "null argument");
+  if (!m || !d_r) return fail(UMCP_ERR_INVALID, "null argument");
+  if (!d_E) d_E = m->E.as<double>();  // allocated with the mesh
   if (m->rs.on) return fail(UMCP_ERR_UNSUPPORTED, "the static entry point has no area/volume restraint terms");
   const int dev = m->ctx->device;
   if (dev < 0 || dev >= 128) return fail(UMCP_ERR_INVALID, "device index out of range for the static scratch table");
@@ -1268,24 +1267,32 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
   unsigned char *base = (unsigned char *)g_static_scratch_addr[dev];
   const bool fp32 = (m->precision == UMCP_FP32_CENTRED);
   const size_t esize = fp32 ? sizeof(float) : sizeof(double);
-  // layout: [status, done] | block partials | gradient partials | FP32 position pairs
+  // layout: [status, done] | block partials | gradient partials | FP32 position pairs and displacements
   const size_t off_flags = 0, off_block = 256;
   const size_t off_partial = off_block + align256((size_t)m->nblocks * 6 * sizeof(double));
+  const size_t f32_bytes = fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0;
   const size_t off_hi = off_partial + align256((size_t)m->nslot_cap * 3 * esize);
-  const size_t off_lo = off_hi + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
-  const size_t need = off_lo + (fp32 ? align256((size_t)3 * m->nv * sizeof(float)) : 0);
+  const size_t off_lo = off_hi + f32_bytes, off_dsp = off_lo + f32_bytes;
+  const size_t need = off_dsp + f32_bytes;
   if (need > kStaticScratchBytes)
     return fail(UMCP_ERR_NOMEM, "mesh needs " + std::to_string(need) + " bytes of scratch; the static area holds " +
                                     std::to_string(kStaticScratchBytes) + " bytes");
   int *status = (int *)(base + off_flags);
   unsigned *done = (unsigned *)(base + off_flags + sizeof(int));
   double *blockpart = (double *)(base + off_block);
-  float *rhi = fp32 ? (float *)(base + off_hi) : nullptr, *rlo = fp32 ? (float *)(base + off_lo) : nullptr;
+  F32Pos f32;
+  if (fp32) {
+    f32.hi = (float *)(base + off_hi);
+    f32.lo = (float *)(base + off_lo);
+    f32.r0 = m->r0.as<double>();
+    f32.dsp = (float *)(base + off_dsp);
+  }
+  float *rhi = f32.hi, *rlo = f32.lo;
   cudaStream_t s = m->ctx->stream;
   // The array keeps the previous call's contents: the status word and the
   // finished-block counter must start at zero.
   UMCP_CUDA(cudaMemsetAsync(base + off_flags, 0, 256, s));
-  if (fp32) UMCP_CUDA(launch_split_positions(3 * m->nv, d_r, rhi, rlo, s));
+  if (fp32) UMCP_CUDA(launch_split_positions(3 * m->nv, d_r, f32, s));
   FinishArgs fin{m->nblocks, d_E, nullptr, d_g ? d_g + 3 * m->nv : nullptr, nullptr, nullptr, 0.0, status, done};
   for (size_t gi = 0; gi < m->groups.size(); ++gi) {
     auto &G = m->groups[gi];
@@ -1306,9 +1313,9 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
     const FinishArgs &f = fin;  // every block of every launch counts toward the finish
     cudaError_t e = (fp32 && G->tc) ? launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, rhi, rlo,
                                                        (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
-                    : fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
+                    : fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, f32,
                                                (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
-                         : launch_faces<double>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, rhi, rlo,
+                         : launch_faces<double>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, f32,
                                                 (double *)(base + off_partial), blockpart, status, G->nblocks, f, s);
     if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("face pass: ") + cudaGetErrorString(e));
   }
@@ -1317,5 +1324,18 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
                          : launch_gather<double>(m->nv, (double *)(base + off_partial), m->off.as<int>(), d_g, s);
     if (e != cudaSuccess) return fail(UMCP_ERR_CUDA, std::string("gather: ") + cudaGetErrorString(e));
   }
+  // The next call clears the array's status word: hand its bits (non-finite
+  // energy, a tensor-core wait that gave up) to the mesh's own status word,
+  // where umcp_mesh_check_status reads them.
+  UMCP_CUDA(launch_status_merge(status, m->status.as<int>(), s));
   return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_mesh_check_status(umcp_mesh *m) {
+  if (!m) return fail(UMCP_ERR_INVALID, "null mesh");
+  UMCP_CUDA(cudaSetDevice(m->ctx->device));
+  const umcp_status st = check_status(m);  // synchronizes the mesh's stream
+  UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), m->ctx->stream));
+  UMCP_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return st;
 }

@@ -130,7 +130,7 @@ static BatchJob job_entry(const Job &J) {
     s.g0f = G.g0f.as<float>(); s.rr0f = G.rr0f.as<float>(); s.compf = G.compf.as<float>();
     s.dest = G.dest.as<int>();
     s.r = m->r.as<double>();
-    s.rhi = m->rhi.as<float>(); s.rlo = m->rlo.as<float>();
+    s.rhi = m->rhi.as<float>(); s.rlo = m->rlo.as<float>(); s.dsp = m->dsp.as<float>();
     s.nfaces = G.nfaces;
   }
   e.f.P = m->P;
@@ -144,6 +144,8 @@ static BatchJob job_entry(const Job &J) {
   const bool f32 = m->precision == UMCP_FP32_CENTRED;
   e.rhi = f32 ? m->rhi.as<float>() : nullptr;
   e.rlo = f32 ? m->rlo.as<float>() : nullptr;
+  e.r0 = f32 ? m->r0.as<double>() : nullptr;
+  e.dsp = f32 ? m->dsp.as<float>() : nullptr;
   e.E = m->E.as<double>();
   e.parts = m->parts.as<double>();
   e.energies = m->energies.as<double>();

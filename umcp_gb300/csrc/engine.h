@@ -97,6 +97,7 @@ struct umcp_mesh {
   int nblocks = 0;
   umcp::DevBuf r, g, p, qdot, E, parts, status, cnt;  // cnt: {first step of the run, run index}
   umcp::DevBuf rhi, rlo;  // FP32 hi/lo pairs of r (precision form)
+  umcp::DevBuf r0, dsp;   // precision form: reference state (FP64) and r - r0 (FP32)
   umcp::DevBuf r_eval;    // staging for host-pointer energy/gradient calls (keeps the resident state)
   umcp::DevBuf done;      // finished-block counter of the face pass
   bool split_valid = false;  // rhi/rlo hold the resident state r
@@ -144,10 +145,19 @@ struct umcp_mesh {
                                     &G->rr0f, &G->compf, &G->basis_w, &G->geo_tab})
         b += x->bytes;
     for (const umcp::DevBuf *x : {&partial, &off, &blockpart, &r, &g, &p, &qdot, &E, &parts, &status, &cnt, &rhi,
-                                  &rlo, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &min32, &geo_block, &gterm,
+                                  &rlo, &r0, &dsp, &r_eval, &done, &energies, &mrow, &mcol, &mval, &alphas, &mdense, &min32, &geo_block, &gterm,
                                   &geo_done})
       b += x->bytes;
     return b;
+  }
+
+  // The FP32 position copies the kernels read and write (all NULL in the plain path).
+  umcp::F32Pos f32pos() const {
+    umcp::F32Pos f;
+    if (precision == UMCP_FP32_CENTRED) {
+      f.hi = rhi.as<float>(); f.lo = rlo.as<float>(); f.r0 = r0.as<double>(); f.dsp = dsp.as<float>();
+    }
+    return f;
   }
 
   ~umcp_mesh() {

@@ -73,6 +73,7 @@ struct FaceSrc {
   const int *dest;
   const double *r;
   const float *rhi, *rlo;
+  const float *dsp;  // precision form: r - r0 per coordinate (displacement from the reference state)
   int nfaces;
 };
 
@@ -112,10 +113,19 @@ __device__ __forceinline__ float qdiv(float a, float, float ib) { return a * ib;
 // curvature and angle terms (zeros then) are left out; results agree with the
 // full form's to rounding (the compiler may fuse a product and sum that the
 // full form keeps apart).
+// dR (precision form): {Ru - Ru0, Rv - Rv0}, the tangents' change from the
+// reference state, contracted from the control points' displacements. The
+// area strain g - g0 is then formed without cancellation:
+//   dm = m - m0 = (Ru - Ru0) x Rv0 + Ru x (Rv - Rv0),  W - W0 = dm . (2 m - dm),
+//   g - g0 = (W - W0) / (g + g0)
+// (exactly zero at the reference state). Subtracting g0 from an FP32 g would
+// leave every tangent's rounding in the strain: at and near the reference
+// state that rounding is the whole area force, on coarse patches up to 1e-5
+// of the gradient.
 template <typename T, bool KG_REG = true>
 __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T rr0, T dudv, T P2, T Hbar, T Pres,
                                               T kc, T KA, T kg, T k_reg, T *ea, T *ec, T *er, Vec3<T> Kb[5],
-                                              Vec3<T> Kreg[2]) {
+                                              Vec3<T> Kreg[2], const Vec3<T> *dR = nullptr) {
   const Vec3<T> &Ru = K[0], &Rv = K[1], &Suu = K[2], &Suv = K[3], &Svv = K[4];
   Vec3<T> m = cross(Ru, Rv);
   T W = dot(m, m);
@@ -146,7 +156,18 @@ __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T r
   T Tt = l * E22 - T(2) * k * E12 + n * E11;
   T H = -Tt * ig3;
   T dH = H - Hbar;
-  T dg = g - g0;
+  T dg;
+  if (dR) {
+    const Vec3<T> &a = dR[0], &b = dR[1];
+    const Vec3<T> rv0 = {Rv.x - b.x, Rv.y - b.y, Rv.z - b.z};
+    const Vec3<T> c1 = cross(a, rv0), c2 = cross(Ru, b);
+    const Vec3<T> dm = {c1.x + c2.x, c1.y + c2.y, c1.z + c2.z};
+    const Vec3<T> s = {T(2) * m.x - dm.x, T(2) * m.y - dm.y, T(2) * m.z - dm.z};
+    if constexpr (sizeof(T) == 4) dg = dot(dm, s) * rcp_nr(g + g0);
+    else dg = dot(dm, s) / (g + g0);
+  } else {
+    dg = g - g0;
+  }
   *ec = T(0.25) * kc * w * (P2 * dH * dH + Pres);
   *ea = qdiv(dudv * w * KA * dg * dg, g0, ig0);
   *er = T(0);

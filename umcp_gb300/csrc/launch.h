@@ -72,6 +72,16 @@ cudaError_t launch_geo_sums(const GeoArgs &G, bool alpha64, cudaStream_t s);
 template <typename T>
 cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s);
 
+// The precision form's FP32 copies of the positions (all NULL in the plain
+// path): r = hi + lo to about 2^-48 relative, and dsp = r - r0, the
+// displacement from the reference state r0 (setg0's state), rounded once.
+// The face kernels form the area strain from dsp (see point_adjoint).
+struct F32Pos {
+  float *hi = nullptr, *lo = nullptr;
+  const double *r0 = nullptr;
+  float *dsp = nullptr;
+};
+
 // Persistent grid of the face pass for one patch type (fixed per device and
 // face count, so the order of every sum is fixed).
 template <typename T>
@@ -82,11 +92,11 @@ int face_blocks(int nfaces, int ncp, int npt);
 // (face-centred precision form). partial[dest[f*ncp+x]] receives the
 // alpha-scaled gradient of control point x of face f; blockpart[L.block_base
 // + b] receives block b's sums {E_area, E_curvature, E_angle, dE/dalpha_xyz}.
-// rhi/rlo: FP32 hi/lo pairs of r (used by the float instantiation only).
+// f: the FP32 positions and displacements (read by the float instantiation only).
 template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
-                         const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
-                         int *status, int grid, const FinishArgs &fin, cudaStream_t s);
+                         const double *r, const F32Pos &f, T *partial, double *blockpart, int *status, int grid,
+                         const FinishArgs &fin, cudaStream_t s);
 
 // The regular faces of the precision form on the tensor cores (face_tc_kernel):
 // the same outputs as launch_faces<float> for ncp 12 / npt 15, in 128-face
@@ -96,8 +106,12 @@ cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev
                             const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
                             int grid, const FinishArgs &fin, cudaStream_t s);
 
-// hi[i] + lo[i] = r[i] to about 2^-48 relative (the precision form's positions).
-cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s);
+// The precision form's FP32 positions of r: f.hi[i] + f.lo[i] = r[i] to about
+// 2^-48 relative, f.dsp[i] = r[i] - f.r0[i].
+cudaError_t launch_split_positions(int n, const double *r, const F32Pos &f, cudaStream_t s);
+
+// *dst |= *src on the device (one thread).
+cudaError_t launch_status_merge(const int *src, int *dst, cudaStream_t s);
 
 // Fixed-order sum of F.nblk block partials: E, parts (3), galpha (+= 3). With
 // energies/cnt given (a run): energies[cnt[1]] = E, divergence and non-finite
@@ -121,15 +135,15 @@ struct StepArgs {
   uint32_t stream;
 };
 // Gather fused with the vertex-local update (kind 0; kinds 1/2 with identity mass).
-// rhi/rlo (may be NULL) receive the FP32 hi/lo pairs of the new positions.
+// f (all NULL in the plain path) receives the FP32 positions of the new state.
 template <typename T>
 cudaError_t launch_gather_step(int nv, const T *partial, const int *off, const StepArgs &a, const uint64_t *cnt,
-                               double *r, double *p, float *rhi, float *rlo, const int *status, cudaStream_t s);
+                               double *r, double *p, const F32Pos &f, const int *status, cudaStream_t s);
 // Kinds 1/2 with a mass matrix: kick p (friction, kicks, noise); then
 // qdot = M^-1 p by launch_spmv; then r += qdot AK (and p reset for BD).
 cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *cnt, double *p, const double *g, const int *status,
                         cudaStream_t s);
-cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, float *rhi, float *rlo,
+cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, const F32Pos &f,
                          const int *status, cudaStream_t s);
 
 // One mesh of a batch (device pointers into the mesh's own buffers). The
@@ -148,6 +162,8 @@ struct BatchJob {
   const int *off;          // vertex slot locations {first slot, count} (interleaved numbering)
   double *r, *p;           // state
   float *rhi, *rlo;        // FP32 hi/lo pairs of r (precision form), else NULL
+  const double *r0;        // reference state (precision form)
+  float *dsp;              // r - r0 in FP32 (precision form)
   double *E, *parts;       // energy (and parts) of the latest step
   double *energies;        // the run's recorded energies, indexed by steps done
   double threshold;        // energy rise that flags divergence (<= 0: off)

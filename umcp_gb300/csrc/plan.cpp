@@ -724,6 +724,7 @@ static void reference_points(const Mesh &m, const double *r, const FaceList &fac
 }
 
 void set_reference_state(const Mesh &m, const double *r, Plan *p) {
+  p->ref_r.assign(r, r + 3 * (size_t)m.nv);
   std::vector<double> reg_area, irr_area;
   reference_points(m, r, p->reg_faces, &p->regular, true, &p->reg_g0, &p->reg_RuRv0, &reg_area);
   reference_points(m, r, p->irr_faces, p->irregular, false, &p->irr_g0, &p->irr_RuRv0, &irr_area);

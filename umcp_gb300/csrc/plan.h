@@ -33,6 +33,7 @@ struct Plan {
   std::vector<Face> reg_faces, irr_faces;
   std::vector<double> reg_g0, reg_RuRv0;   // [face*15 + pt]
   std::vector<double> irr_g0, irr_RuRv0;   // [face*16 + pt]
+  std::vector<double> ref_r;               // the state g0 and RuRv0 were taken at (3*nv)
   // Leaflet compositions: areas (A^2) per lipid type, [face*ntypes + x].
   int ntypes = 1;
   std::vector<Lipid> lipids;

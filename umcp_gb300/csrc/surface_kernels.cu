@@ -5,6 +5,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "kernels.cuh"
 #include "launch.h"
 #include "philox.h"
@@ -51,6 +53,7 @@ struct FaceSmem<float, NCP, NPT> {
   static_assert(THW % 32 == 16 && THW % 4 == 0, "half-warp stride");
   Q4<float> B[NPT][5][NC4];
   alignas(16) float Xt[HW][3][NCPP];
+  alignas(16) float Dt[HW][3][NCPP];  // the same control points' change from the reference state
   alignas(16) float Tc[HW][THW];
   float W[NPT];
   double red[HW][6];
@@ -146,6 +149,7 @@ template <typename T>
 struct FaceAhead {
   int img[3] = {0, 0, 0};
   float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};  // precision form
+  float dsp[3] = {0, 0, 0};                    // precision form: r - r0
   double X[3] = {0, 0, 0};                     // plain path (image position)
   T g0 = 1, rr0 = 0, P2 = 0, Hbar = 0, Pres = 0;
   int dest = 0;
@@ -170,7 +174,11 @@ __device__ __forceinline__ void load_ahead(const FaceSrc &S, const SurfaceParams
         a.X[c] = S.r[3 * (size_t)v + c] + a.img[0] * P.box[0][c] + a.img[1] * P.box[1][c] + a.img[2] * P.box[2][c];
     } else {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { a.hi[c] = S.rhi[3 * (size_t)v + c]; a.lo[c] = S.rlo[3 * (size_t)v + c]; }
+      for (int c = 0; c < 3; ++c) {
+        a.hi[c] = S.rhi[3 * (size_t)v + c];
+        a.lo[c] = S.rlo[3 * (size_t)v + c];
+        a.dsp[c] = S.dsp[3 * (size_t)v + c];
+      }
     }
     a.dest = __ldg(&S.dest[(size_t)f * NCP + lane]);
   }
@@ -193,7 +201,7 @@ __device__ __forceinline__ void stage_basis(FaceSmem<T, NCP, NPT> &sm, const dou
   for (int i = threadIdx.x; i < NPT; i += NT) sm.W[i] = (T)weight[i];
   // padding control points stay zero
   if constexpr (sizeof(T) == 4)
-    for (int i = threadIdx.x; i < HW * 3 * NCPP; i += NT) (&sm.Xt[0][0][0])[i] = 0.f;
+    for (int i = threadIdx.x; i < HW * 3 * NCPP; i += NT) (&sm.Xt[0][0][0])[i] = (&sm.Dt[0][0][0])[i] = 0.f;
   else
     for (int i = threadIdx.x; i < HW * NCPP; i += NT) sm.X[i / NCPP][i % NCPP] = Q4<T>{0, 0, 0, 0};
 }
@@ -211,16 +219,23 @@ __device__ __forceinline__ void point_pass_f32(FaceSmem<float, NCP, NPT> &sm, in
                                                bool reg_alpha, float *ea, float *ec, float *er, float dreg[3]) {
   using S = FaceSmem<float, NCP, NPT>;
   constexpr int NC4 = S::NC4, TROW = S::TROW;
-  float2 A[5][3];
+  float2 A[5][3], Ad[2][3];  // Ad: the u and v rows contracted with the displacements (Dt)
 #pragma unroll
   for (int k = 0; k < 5; ++k)
 #pragma unroll
     for (int c = 0; c < 3; ++c) A[k][c] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Ad[k][c] = make_float2(0.f, 0.f);
 #pragma unroll 1
   for (int c4 = 0; c4 < NC4; ++c4) {
-    float4 x[3];
+    float4 x[3], d[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = *reinterpret_cast<const float4 *>(&sm.Xt[hw][c][4 * c4]);
+    for (int c = 0; c < 3; ++c) {
+      x[c] = *reinterpret_cast<const float4 *>(&sm.Xt[hw][c][4 * c4]);
+      d[c] = *reinterpret_cast<const float4 *>(&sm.Dt[hw][c][4 * c4]);
+    }
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const Q4<float> b = sm.B[lane][k][c4];
@@ -229,15 +244,21 @@ __device__ __forceinline__ void point_pass_f32(FaceSmem<float, NCP, NPT> &sm, in
       for (int c = 0; c < 3; ++c) {
         A[k][c] = __ffma2_rn(b01, make_float2(x[c].x, x[c].y), A[k][c]);
         A[k][c] = __ffma2_rn(b23, make_float2(x[c].z, x[c].w), A[k][c]);
+        if (k < 2) {
+          Ad[k][c] = __ffma2_rn(b01, make_float2(d[c].x, d[c].y), Ad[k][c]);
+          Ad[k][c] = __ffma2_rn(b23, make_float2(d[c].z, d[c].w), Ad[k][c]);
+        }
       }
     }
   }
-  Vec3<float> K[5];
+  Vec3<float> K[5], dR[2];
 #pragma unroll
   for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) dR[k] = {Ad[k][0].x + Ad[k][0].y, Ad[k][1].x + Ad[k][1].y, Ad[k][2].x + Ad[k][2].y};
   Vec3<float> Kb[5], Kreg[2];
   point_adjoint<float>(K, sm.W[lane], cur.g0, cur.rr0, dudv, cur.P2, cur.Hbar, cur.Pres, mod.kc, mod.KA, mod.kg,
-                       mod.k_reg, ea, ec, er, Kb, Kreg);
+                       mod.k_reg, ea, ec, er, Kb, Kreg, dR);
   float2 Kd[5][3];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -291,12 +312,12 @@ __device__ __forceinline__ void point_pass_f32(FaceSmem<float, NCP, NPT> &sm, in
 template <typename T, int NCP, int NPT>
 __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, int lane, unsigned hmask,
                                              const FaceAhead<T> &cur, const SurfaceParams &P, const T alpha[3],
-                                             const T ialpha[3], const Moduli<T> &mod, T dudv, bool reg_alpha, T *__restrict__ partial,
-                                             T e3[3], T da[3]) {
+                                             const T ialpha[3], const T am1[3], const Moduli<T> &mod, T dudv,
+                                             bool reg_alpha, T *__restrict__ partial, T e3[3], T da[3]) {
   constexpr int NC4 = FaceSmem<T, NCP, NPT>::NC4;
   const T kc = mod.kc, KA = mod.KA, kg = mod.kg, k_reg = mod.k_reg;
   // ---- 1. control points, relative to the patch corner
-  T xl[3] = {0, 0, 0};
+  T xl[3] = {0, 0, 0}, dx[3] = {0, 0, 0};
   if constexpr (sizeof(T) == 8) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -320,7 +341,12 @@ __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, 
       float s1, e1, s2, e2;
       two_sum(cur.hi[c], sh, s1, e1);
       two_sum(s1, -ahi, s2, e2);
-      xl[c] = alpha[c] * (s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl))));
+      const float lc = s2 + ((e1 + e2) + ((cur.lo[c] - alo) + (she + shl)));
+      xl[c] = alpha[c] * lc;
+      // change from the reference state (box scales 1 there): alpha L - L0 = (alpha - 1) L + (L - L0),
+      // L - L0 = dsp - dsp of the corner (the lattice shifts cancel)
+      const float d0 = __shfl_sync(hmask, cur.dsp[c], 0, 16);
+      dx[c] = fmaf(am1[c], lc, cur.dsp[c] - d0);
     }
   }
   if constexpr (sizeof(T) == 4) {
@@ -328,6 +354,9 @@ __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, 
       sm.Xt[hw][0][lane] = xl[0];
       sm.Xt[hw][1][lane] = xl[1];
       sm.Xt[hw][2][lane] = xl[2];
+      sm.Dt[hw][0][lane] = dx[0];
+      sm.Dt[hw][1][lane] = dx[1];
+      sm.Dt[hw][2][lane] = dx[2];
     }
   } else {
     if (lane < NCP) sm.X[hw][lane] = Q4<T>{xl[0], xl[1], xl[2], T(0)};
@@ -437,8 +466,8 @@ __device__ __forceinline__ void face_compute(FaceSmem<T, NCP, NPT> &sm, int hw, 
 template <typename T, int NCP, int NPT>
 __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     face_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
-                const float *__restrict__ rhi, const float *__restrict__ rlo, T *__restrict__ partial,
-                double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
+                const float *__restrict__ rhi, const float *__restrict__ rlo, const float *__restrict__ dsp,
+                T *__restrict__ partial, double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
   using S = FaceSmem<T, NCP, NPT>;
   constexpr int HW = S::HW, NT = FaceCfg<T>::threads;
   __shared__ S sm;
@@ -449,10 +478,11 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
   const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
   const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
   const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
+  const T am1[3] = {(T)(r[3 * P.nv] - 1.0), (T)(r[3 * P.nv + 1] - 1.0), (T)(r[3 * P.nv + 2] - 1.0)};
   const T dudv = (T)L.dudv;
   const bool reg_alpha = L.irregular && P.k_reg != 0.0;
   const Moduli<T> mod(P);
-  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, dsp, L.nfaces};
   HalfWarpSums<T> acc;
 
   const int stride = gridDim.x * HW;
@@ -467,7 +497,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
     load_ahead<T, NCP, NPT>(src, P, f + stride, end, cp_next, lane, nxt);
     cp_next = cp_after;
     T e3[3], da[3];
-    face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, mod, dudv, reg_alpha, partial, e3, da);
+    face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, am1, mod, dudv, reg_alpha, partial, e3, da);
     acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
     acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
     if (lane == 0 && !isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
@@ -504,7 +534,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
 // ---------------------------------------------------------------- tensor-core face pass
 //
 // Regular faces in the precision form, with the two basis contractions on the
-// 5th-generation tensor cores (tcgen05, kind::tf32, 3xTF32 splits) and the
+// 5th-generation tensor cores (tcgen05, kind::f16 on fp16 hi/lo splits) and the
 // pointwise energy and adjoint on the FP32 pipes. A CTA owns a tile of 128
 // faces (the MMA's M; face = TMEM lane) and 256 threads: thread (face, half)
 // takes the half-th quadrature point of each 2-point chunk.
@@ -513,7 +543,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
 // patch frame Eu = X2 - X0, Ev = X1 - X0 (control points 2 and 1 sit at
 // lattice (1,0) and (0,1)) and X'_x = X_x - X0 - u_x Eu - v_x Ev:
 //   Ru = Eu + sum b_u X',  Rv = Ev + sum b_v X',  S.. = sum b_.. X'.
-// X' is of the size of the curvature, not of the patch, so the TF32 split
+// X' is of the size of the curvature, not of the patch, so the fp16 split
 // errors scale with the curvature terms themselves.
 //
 // Per chunk j (points 2j, 2j+1):
@@ -1011,7 +1041,7 @@ __global__ void __launch_bounds__(tc::kThreads, 2)
   const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
   const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
   const Moduli<float> mod(P);
-  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, nullptr, L.nfaces};
   HalfWarpSums<float> acc;
   uint32_t phase = 0;
   bool ok = true;
@@ -1038,16 +1068,29 @@ __global__ void __launch_bounds__(tc::kThreads, 2)
   }
 }
 
-// FP32 hi/lo pairs of the positions for the precision form: r = hi + lo to
-// about 2^-48 relative.
+// The precision form's FP32 copies of one position coordinate x = r[i]:
+// x = hi + lo to about 2^-48 relative, and dsp = x - r0[i] (the displacement
+// from the reference state, rounded once from FP64).
+__device__ __forceinline__ void store_f32_position(size_t i, double x, float *__restrict__ hi,
+                                                   float *__restrict__ lo, const double *__restrict__ r0,
+                                                   float *__restrict__ dsp) {
+  const float h = (float)x;
+  hi[i] = h;
+  lo[i] = (float)(x - (double)h);
+  dsp[i] = (float)(x - r0[i]);
+}
+
 __global__ void split_positions_kernel(int n, const double *__restrict__ r, float *__restrict__ hi,
-                                       float *__restrict__ lo) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double x = r[i];
-    const float h = (float)x;
-    hi[i] = h;
-    lo[i] = (float)(x - (double)h);
-  }
+                                       float *__restrict__ lo, const double *__restrict__ r0,
+                                       float *__restrict__ dsp) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    store_f32_position(i, r[i], hi, lo, r0, dsp);
+}
+
+// dst |= *src (one thread): a status word handed on to another.
+__global__ void status_merge_kernel(const int *__restrict__ src, int *__restrict__ dst) {
+  const int v = *src;
+  if (v) *dst |= v;
 }
 
 // Stand-alone form of the block-partial sum (used when the face launches do
@@ -1179,7 +1222,8 @@ __device__ __forceinline__ uint64_t current_step(const uint64_t *cnt) { return c
 template <typename T>
 __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const int *__restrict__ off, StepArgs a,
                                    const uint64_t *__restrict__ cnt, double *__restrict__ r, double *__restrict__ p,
-                                   float *__restrict__ rhi, float *__restrict__ rlo, const int *__restrict__ status) {
+                                   float *__restrict__ rhi, float *__restrict__ rlo, const double *__restrict__ r0,
+                                   float *__restrict__ dsp, const int *__restrict__ status) {
   if (*status) return;
   const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
@@ -1199,11 +1243,7 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       r[3 * (size_t)v + c] = rn[c];
-      if (rhi) {
-        const float h = (float)rn[c];
-        rhi[3 * (size_t)v + c] = h;
-        rlo[3 * (size_t)v + c] = (float)(rn[c] - (double)h);
-      }
+      if (rhi) store_f32_position(3 * (size_t)v + c, rn[c], rhi, rlo, r0, dsp);
     }
   }
 }
@@ -1224,17 +1264,13 @@ __global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ cnt
 
 __global__ void drift_kernel(int nv, StepArgs a, double *__restrict__ r, double *__restrict__ p,
                              const double *__restrict__ qdot, float *__restrict__ rhi, float *__restrict__ rlo,
-                             const int *__restrict__ status) {
+                             const double *__restrict__ r0, float *__restrict__ dsp, const int *__restrict__ status) {
   if (*status) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nv; i += gridDim.x * blockDim.x) {
     const double x = __dadd_rn(r[i], __dmul_rn(qdot[i], a.AK));
     r[i] = x;
     if (a.kind == 1) p[i] = 0.0;
-    if (rhi) {
-      const float h = (float)x;
-      rhi[i] = h;
-      rlo[i] = (float)(x - (double)h);
-    }
+    if (rhi) store_f32_position(i, x, rhi, rlo, r0, dsp);
   }
 }
 
@@ -1286,6 +1322,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
       const double *r = src.r;
       const T alpha[3] = {(T)r[3 * P.nv], (T)r[3 * P.nv + 1], (T)r[3 * P.nv + 2]};
       const T ialpha[3] = {T(1) / alpha[0], T(1) / alpha[1], T(1) / alpha[2]};
+      const T am1[3] = {(T)(r[3 * P.nv] - 1.0), (T)(r[3 * P.nv + 1] - 1.0), (T)(r[3 * P.nv + 2] - 1.0)};
       const bool reg_alpha = irregular && P.k_reg != 0.0;
       const Moduli<T> mod(P);
       const int end = tile.first + tile.count;
@@ -1298,8 +1335,8 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
         load_ahead<T, NCP, NPT>(src, P, f + HW, end, cp_next, lane, nxt);
         cp_next = cp_after;
         T e3[3], da[3];
-        face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, mod, dudv, reg_alpha, (T *)sj.partial,
-                                  e3, da);
+        face_compute<T, NCP, NPT>(sm, hw, lane, hmask, cur, P, alpha, ialpha, am1, mod, dudv, reg_alpha,
+                                  (T *)sj.partial, e3, da);
         acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
         cur = nxt;
         __syncwarp(hmask);
@@ -1343,6 +1380,7 @@ struct Smem {
   // is an odd number of 16-byte chunks, so the float4 reads of a warp do not
   // conflict
   float4 X[kThreads][9];
+  float4 D[kThreads][9];  // the same control points' change from the reference state, same layout
   float W[kNpt];
   double red[kWarps][6];
 };
@@ -1363,14 +1401,14 @@ __device__ __forceinline__ float4 ld4(const float4 *p) {
 }
 
 // One warp's 32 faces of face tables, copied into shared memory ahead of use
-// with coalesced 16-byte asynchronous copies (the per-point g0/rr0 rows are
-// 60 bytes apart per face, so direct per-thread loads touch a sector per
-// thread). Row r of face lane: cp[12 lane ..], g0/rr0[15 lane + p], comp[3 lane ..].
+// with coalesced 16-byte asynchronous copies (the per-point g0 rows are 60
+// bytes apart per face, so direct per-thread loads touch a sector per
+// thread). Row r of face lane: cp[12 lane ..], g0[15 lane + p]. The
+// composition (read once per face) and the reference angles (read only when
+// k_reg or kg is set) are read from global memory directly.
 struct Stage {
   uint4 cp[32 * kNcp / 4];
   float g0[32 * kNpt];
-  float rr0[32 * kNpt];
-  float comp[32 * 3];
 };
 constexpr size_t kStageBytes = sizeof(Stage) * 2 * kWarps;  // double-buffered per warp (dynamic shared memory)
 constexpr size_t kSumBytes = sizeof(float) * 12 * kThreads;    // per-thread Kahan totals (after the stages)
@@ -1400,9 +1438,8 @@ __device__ __forceinline__ void stage_rows(void *dst, const void *src, int bytes
 __device__ __forceinline__ void stage_issue(Stage &st, const FaceSrc &S, int f0, int n, int lane) {
   stage_rows(st.cp, S.cp + (size_t)f0 * kNcp, n * kNcp * 4, lane);
   stage_rows(st.g0, S.g0f + (size_t)f0 * kNpt, n * kNpt * 4, lane);
-  stage_rows(st.rr0, S.rr0f + (size_t)f0 * kNpt, n * kNpt * 4, lane);
-  stage_rows(st.comp, S.compf + (size_t)f0 * 3, n * 12, lane);
   if (lane < kNcp) prefetch_l2(S.dest + (size_t)f0 * kNcp + 32 * lane);  // read at the faces' end
+  if (lane < 3) prefetch_l2(S.compf + (size_t)f0 * 3 + 32 * lane);
 }
 }  // namespace tpf
 
@@ -1414,14 +1451,16 @@ __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, co
 
 // Face f's energy terms and dE/dalpha; writes its alpha-scaled gradient
 // partials to the face's slots. vec: cp and dest are 16-byte aligned.
-// STAGED: the face's tables come from cur (row lane) instead of global
-// memory; with next given, the next faces' control-point positions are
+// STAGED: the face's control points and g0 come from cur (row lane) instead of
+// global memory; with next given, the next faces' control-point positions are
 // prefetched into L1 half-way through (every lane of the warp is active then).
+// am1 = alpha - 1 (formed in FP64): the box scales' part of the change from
+// the reference state.
 template <bool STAGED, bool KG_REG>
 __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
-                                         const float alpha[3], const float ialpha[3], const Moduli<float> &mod,
-                                         float dudv, bool vec, float *__restrict__ partial, float e3[3],
-                                         float da[3], const tpf::Stage *cur = nullptr,
+                                         const float alpha[3], const float ialpha[3], const float am1[3],
+                                         const Moduli<float> &mod, float dudv, bool vec, float *__restrict__ partial,
+                                         float e3[3], float da[3], const tpf::Stage *cur = nullptr,
                                          const tpf::Stage *next = nullptr, int lane = 0) {
   using namespace tpf;
   uint32_t cp[kNcp];
@@ -1442,55 +1481,66 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
 #pragma unroll
     for (int j = 0; j < kNcp; ++j) cp[j] = __ldg(&S.cp[(size_t)f * kNcp + j]);
   }
+  const float P2 = __ldg(&S.compf[3 * (size_t)f]), Hbar = __ldg(&S.compf[3 * (size_t)f + 1]),
+              Pres = __ldg(&S.compf[3 * (size_t)f + 2]);
   // ---- control points relative to the patch corner (control point 0), in
   // their lattice images, times alpha; error-free sums on the hi/lo pairs as
-  // in face_compute, so the local coordinates carry full FP32 precision.
-  float X[kNcp][3];
-  float4 *xs = sm.X[threadIdx.x];
-  float ahi[3], alo[3];
+  // in face_compute, so the local coordinates carry full FP32 precision. Their
+  // change from the reference state: alpha L - L0 = (alpha - 1) L + (dsp -
+  // dsp of the corner). Formed and stored four control points at a time.
+  float4 *xs = sm.X[threadIdx.x], *ds = sm.D[threadIdx.x];
+  float ahi[3], alo[3], ad[3];
   {
     const int v0 = (int)(cp[0] & kVertexMask);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { ahi[c] = __ldg(&S.rhi[3 * (size_t)v0 + c]); alo[c] = __ldg(&S.rlo[3 * (size_t)v0 + c]); }
+    for (int c = 0; c < 3; ++c) {
+      ahi[c] = __ldg(&S.rhi[3 * (size_t)v0 + c]);
+      alo[c] = __ldg(&S.rlo[3 * (size_t)v0 + c]);
+      ad[c] = __ldg(&S.dsp[3 * (size_t)v0 + c]);
+    }
   }
 #pragma unroll
-  for (int j = 0; j < kNcp; ++j) {
-    const int v = (int)(cp[j] & kVertexMask), code = (int)(cp[j] >> kVertexBits);
-    float hi[3], lo[3], sh[3] = {0.f, 0.f, 0.f}, she[3] = {0.f, 0.f, 0.f}, shl[3] = {0.f, 0.f, 0.f};
+  for (int c4 = 0; c4 < kNc4; ++c4) {
+    float X[4][3], Dx[4][3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { hi[c] = __ldg(&S.rhi[3 * (size_t)v + c]); lo[c] = __ldg(&S.rlo[3 * (size_t)v + c]); }
-    if (code != 13) {  // a periodic image: the lattice shift as hi + lo (each term exact)
-      const int img[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = 4 * c4 + jj;
+      const int v = (int)(cp[j] & kVertexMask), code = (int)(cp[j] >> kVertexBits);
+      float hi[3], lo[3], dv[3], sh[3] = {0.f, 0.f, 0.f}, she[3] = {0.f, 0.f, 0.f}, shl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
+      for (int c = 0; c < 3; ++c) {
+        hi[c] = __ldg(&S.rhi[3 * (size_t)v + c]);
+        lo[c] = __ldg(&S.rlo[3 * (size_t)v + c]);
+        dv[c] = __ldg(&S.dsp[3 * (size_t)v + c]);
+      }
+      if (code != 13) {  // a periodic image: the lattice shift as hi + lo (each term exact)
+        const int img[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          float t, e;
-          two_sum(sh[c], (float)img[d] * P.box_hi[d][c], t, e);
-          sh[c] = t;
-          she[c] += e;
-          shl[c] += (float)img[d] * P.box_lo[d][c];
-        }
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            float t, e;
+            two_sum(sh[c], (float)img[d] * P.box_hi[d][c], t, e);
+            sh[c] = t;
+            she[c] += e;
+            shl[c] += (float)img[d] * P.box_lo[d][c];
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float s1, e1, s2, e2;
+        two_sum(hi[c], sh[c], s1, e1);
+        two_sum(s1, -ahi[c], s2, e2);
+        const float l = s2 + ((e1 + e2) + ((lo[c] - alo[c]) + (she[c] + shl[c])));
+        X[jj][c] = alpha[c] * l;
+        Dx[jj][c] = fmaf(am1[c], l, dv[c] - ad[c]);
+      }
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      float s1, e1, s2, e2;
-      two_sum(hi[c], sh[c], s1, e1);
-      two_sum(s1, -ahi[c], s2, e2);
-      X[j][c] = alpha[c] * (s2 + ((e1 + e2) + ((lo[c] - alo[c]) + (she[c] + shl[c]))));
+      st4(&xs[kNc4 * c + c4], make_float4(X[0][c], X[1][c], X[2][c], X[3][c]));
+      st4(&ds[kNc4 * c + c4], make_float4(Dx[0][c], Dx[1][c], Dx[2][c], Dx[3][c]));
     }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int c4 = 0; c4 < kNc4; ++c4)
-      st4(&xs[kNc4 * c + c4], make_float4(X[4 * c4][c], X[4 * c4 + 1][c], X[4 * c4 + 2][c], X[4 * c4 + 3][c]));
-  float P2, Hbar, Pres;
-  if constexpr (STAGED) {
-    P2 = cur->comp[3 * lane]; Hbar = cur->comp[3 * lane + 1]; Pres = cur->comp[3 * lane + 2];
-  } else {
-    P2 = __ldg(&S.compf[3 * (size_t)f]); Hbar = __ldg(&S.compf[3 * (size_t)f + 1]);
-    Pres = __ldg(&S.compf[3 * (size_t)f + 2]);
   }
   // ---- the quadrature points
   float2 G2[kNcp / 2][3];  // gradient sums of control points 2 i, 2 i + 1 per coordinate
@@ -1499,10 +1549,9 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
   float ea = 0.f, ec = 0.f, er = 0.f, dax = 0.f, day = 0.f, daz = 0.f;
 #pragma unroll 1
   for (int p = 0; p < kNpt; ++p) {
-    float g0, rr0;
+    float g0, rr0 = 0.f;
     if constexpr (STAGED) {
       g0 = cur->g0[kNpt * lane + p];
-      rr0 = cur->rr0[kNpt * lane + p];
       if (next && p == kPrefetchPoint) {
         cp_async_wait<0>();  // the next faces' tables (queued when these faces started) have landed
         __syncwarp();
@@ -1515,22 +1564,30 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
             const size_t o = 3 * (size_t)(w[e] & kVertexMask);
             prefetch_l1(S.rhi + o);
             prefetch_l1(S.rlo + o);
+            prefetch_l1(S.dsp + o);
           }
         }
       }
     } else {
       g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]);
-      rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
     }
-    // K[k]_c as two partial sums (even, odd control points) in one pair
-    float2 A[5][3];
+    if constexpr (KG_REG) rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
+    // K[k]_c as two partial sums (even, odd control points) in one pair; the
+    // u and v rows also over the displacements (dR, the tangents' change
+    // from the reference state)
+    float2 A[5][3], Ad[2][3];
 #pragma unroll
     for (int k = 0; k < 5; ++k) A[k][0] = A[k][1] = A[k][2] = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int c4 = 0; c4 < kNc4; ++c4) {
-      float4 x[3];  // coordinate c of control points 4 c4 .. 4 c4 + 3
+    for (int k = 0; k < 2; ++k) Ad[k][0] = Ad[k][1] = Ad[k][2] = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) x[c] = ld4(&xs[kNc4 * c + c4]);
+    for (int c4 = 0; c4 < kNc4; ++c4) {
+      float4 x[3], d[3];  // coordinate c of control points 4 c4 .. 4 c4 + 3
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        x[c] = ld4(&xs[kNc4 * c + c4]);
+        d[c] = ld4(&ds[kNc4 * c + c4]);
+      }
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const Q4<float> b = sm.B[p][k][c4];
@@ -1539,16 +1596,22 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
         for (int c = 0; c < 3; ++c) {
           A[k][c] = __ffma2_rn(b01, make_float2(x[c].x, x[c].y), A[k][c]);
           A[k][c] = __ffma2_rn(b23, make_float2(x[c].z, x[c].w), A[k][c]);
+          if (k < 2) {
+            Ad[k][c] = __ffma2_rn(b01, make_float2(d[c].x, d[c].y), Ad[k][c]);
+            Ad[k][c] = __ffma2_rn(b23, make_float2(d[c].z, d[c].w), Ad[k][c]);
+          }
         }
       }
     }
-    Vec3<float> K[5];
+    Vec3<float> K[5], dR[2];
 #pragma unroll
     for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) dR[k] = {Ad[k][0].x + Ad[k][0].y, Ad[k][1].x + Ad[k][1].y, Ad[k][2].x + Ad[k][2].y};
     Vec3<float> Kb[5], Kreg[2];
     float a, c, r;
     point_adjoint<float, KG_REG>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a,
-                                 &c, &r, Kb, Kreg);
+                                 &c, &r, Kb, Kreg, dR);
     ea += a;
     ec += c;
     er += r;
@@ -1603,8 +1666,7 @@ __device__ __forceinline__ bool tpf_vec(const FaceSrc &S) {
 // The face tables can be staged with 16-byte copies.
 __device__ __forceinline__ bool tpf_stage_ok(const FaceSrc &S) {
   return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest) |
-           reinterpret_cast<uintptr_t>(S.g0f) | reinterpret_cast<uintptr_t>(S.rr0f) |
-           reinterpret_cast<uintptr_t>(S.compf)) & 15) == 0;
+           reinterpret_cast<uintptr_t>(S.g0f)) & 15) == 0;
 }
 
 // Kahan-compensated FP32 totals of one thread, kept in shared memory (its
@@ -1640,8 +1702,9 @@ __device__ __forceinline__ double warp_sum(double q) {
 // to finish sums them (as face_kernel does).
 __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     face_tpf_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
-                    const float *__restrict__ rhi, const float *__restrict__ rlo, float *__restrict__ partial,
-                    double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
+                    const float *__restrict__ rhi, const float *__restrict__ rlo, const float *__restrict__ dsp,
+                    float *__restrict__ partial, double *__restrict__ blockpart, int *__restrict__ status,
+                    FinishArgs fin) {
   using namespace tpf;
   __shared__ Smem sm;
   extern __shared__ __align__(16) unsigned char tpf_dyn[];
@@ -1651,8 +1714,9 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
   const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+  const float am1[3] = {(float)(r[3 * P.nv] - 1.0), (float)(r[3 * P.nv + 1] - 1.0), (float)(r[3 * P.nv + 2] - 1.0)};
   const Moduli<float> mod(P);
-  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, L.nfaces};
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, dsp, L.nfaces};
   // the launch wrapper checks that the tables are 16-byte aligned (tpf_stage_ok)
   const float dudv = (float)L.dudv;
   const bool kg_reg = P.kg != 0.0 || P.k_reg != 0.0;  // else the pointwise step leaves those terms out
@@ -1677,10 +1741,10 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     if (f < n) {
       float e3[3], da[3];
       if (kg_reg)
-        tpf_face<true, true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+        tpf_face<true, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
                              nb < n ? &st[buf ^ 1] : nullptr, lane);
       else
-        tpf_face<true, false>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+        tpf_face<true, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
                               nb < n ? &st[buf ^ 1] : nullptr, lane);
       acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
       acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
@@ -1761,6 +1825,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
       const double *r = src.r;
       const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
       const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+      const float am1[3] = {(float)(r[3 * P.nv] - 1.0), (float)(r[3 * P.nv + 1] - 1.0),
+                            (float)(r[3 * P.nv + 2] - 1.0)};
       const Moduli<float> mod(P);
       const int end = tile.first + tile.count;
       float *partial = (float *)sj.partial;
@@ -1781,10 +1847,10 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
           if (f < end) {
             float e3[3], da[3];
             if (kg_reg)
-              tpf_face<true, true>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+              tpf_face<true, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
                                    nb < end ? &st[buf ^ 1] : nullptr, lane);
             else
-              tpf_face<true, false>(sm, src, P, f, alpha, ialpha, mod, dudv, true, partial, e3, da, &st[buf],
+              tpf_face<true, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
                                     nb < end ? &st[buf ^ 1] : nullptr, lane);
             acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
           }
@@ -1798,8 +1864,8 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
           const int f = fb + lane;
           if (f < end) {
             float e3[3], da[3];
-            if (kg_reg) tpf_face<false, true>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
-            else tpf_face<false, false>(sm, src, P, f, alpha, ialpha, mod, dudv, vec, partial, e3, da);
+            if (kg_reg) tpf_face<false, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+            else tpf_face<false, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
             acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
           }
         }
@@ -1894,11 +1960,7 @@ __global__ void batch_gather_step_kernel(const BatchJob *__restrict__ jobs, cons
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       r[3 * (size_t)v + c] = rn[c];
-      if (J.rhi) {
-        const float h = (float)rn[c];
-        J.rhi[3 * (size_t)v + c] = h;
-        J.rlo[3 * (size_t)v + c] = (float)(rn[c] - (double)h);
-      }
+      if (J.rhi) store_f32_position(3 * (size_t)v + c, rn[c], J.rhi, J.rlo, J.r0, J.dsp);
     }
   }
 }
@@ -1920,12 +1982,8 @@ __global__ void batch_start_kernel(const BatchJob *__restrict__ jobs, const Batc
     }
     if (J.rhi && (int)threadIdx.x < tile.count) {
       const int v = tile.first + threadIdx.x;
-      for (int c = 0; c < 3; ++c) {
-        const double x = J.r[3 * (size_t)v + c];
-        const float h = (float)x;
-        J.rhi[3 * (size_t)v + c] = h;
-        J.rlo[3 * (size_t)v + c] = (float)(x - (double)h);
-      }
+      for (int c = 0; c < 3; ++c)
+        store_f32_position(3 * (size_t)v + c, J.r[3 * (size_t)v + c], J.rhi, J.rlo, J.r0, J.dsp);
     }
   }
 }
@@ -2537,34 +2595,81 @@ static int grid_for(int n, int per_block) {
   return g < 1 ? 1 : g;
 }
 
+// A value fixed per device and computed once on it (thread-safe: meshes may
+// be made on several threads). cudaFuncSetAttribute applies to the current
+// device only, and the persistent grids follow each device's SM count, so
+// neither may be shared between the devices of one process.
+constexpr int kMaxDevices = 64;
+struct PerDevice {
+  std::once_flag once[kMaxDevices];
+  int value[kMaxDevices] = {};
+};
+template <class F>
+static int per_device(PerDevice &pd, F make) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices) return make();
+  std::call_once(pd.once[dev], [&] { pd.value[dev] = make(); });
+  return pd.value[dev];
+}
+// The dynamic shared memory limits above 48 KB that the staged kernels opt
+// into, once per device; returns the cudaError_t of the opt-in.
+static cudaError_t tpf_opt_in() {
+  static PerDevice pd;
+  return (cudaError_t)per_device(pd, [] {
+    return (int)cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
+  });
+}
+static cudaError_t batch_tpf_opt_in() {
+  static PerDevice pd;
+  return (cudaError_t)per_device(pd, [] {
+    return (int)cudaFuncSetAttribute(dev::batch_face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)dev::tpf::kStageBytes);
+  });
+}
+static cudaError_t tc_opt_in() {
+  static PerDevice pd;
+  return (cudaError_t)per_device(pd, [] {
+    return (int)cudaFuncSetAttribute(dev::face_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)dev::tc::kSmemBytes);
+  });
+}
+static int sm_count() {
+  static PerDevice pd;
+  return per_device(pd, [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  });
+}
+
 template <typename T, int NCP, int NPT>
 static int face_grid_size(int nfaces) {
   // Persistent grid: as many blocks as fit on the device at once (a fixed
-  // number, so the face-to-block assignment and the sums' order are fixed).
-  static const int cached = [] {  // thread-safe one-time initialisation
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // number per device, so the face-to-block assignment and the sums' order are fixed).
+  static PerDevice pd;
+  const int cached = per_device(pd, [] {
+    int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_kernel<T, NCP, NPT>,
                                                   dev::FaceCfg<T>::threads, 0);
-    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  }();
+    return sm_count() * (per_sm > 0 ? per_sm : 1);
+  });
   int need = grid_for(nfaces, dev::FaceCfg<T>::half_warps);
   return need < cached ? need : cached;
 }
 
 // The thread-per-face kernel's persistent grid (precision form, regular faces).
 static int face_grid_size_tpf(int nfaces) {
-  static const int cached = [] {  // thread-safe one-time initialisation (meshes may be made on several threads)
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
+  static PerDevice pd;
+  const int cached = per_device(pd, [] {
+    int per_sm = 0;
+    tpf_opt_in();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads,
                                                   dev::tpf::kStageBytes + dev::tpf::kSumBytes);
-    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  }();
+    return sm_count() * (per_sm > 0 ? per_sm : 1);
+  });
   int need = grid_for(nfaces, dev::tpf::kThreads);
   return need < cached ? need : cached;
 }
@@ -2583,48 +2688,53 @@ template int face_blocks<float>(int, int, int);
 
 template <typename T>
 cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int npt, const dev::SurfaceParams &P,
-                         const double *r, const float *rhi, const float *rlo, T *partial, double *blockpart,
-                         int *status, int grid, const FinishArgs &fin, cudaStream_t s) {
+                         const double *r, const F32Pos &f, T *partial, double *blockpart, int *status, int grid,
+                         const FinishArgs &fin, cudaStream_t s) {
   if (L.nfaces <= 0) return cudaSuccess;
   constexpr int NT = dev::FaceCfg<T>::threads;
+  const float *rhi = f.hi, *rlo = f.lo, *dsp = f.dsp;
   if constexpr (sizeof(T) == 4) {
+    if (!rhi || !rlo || !dsp) return cudaErrorInvalidValue;
     if (ncp == 12 && npt == 15) {
       const uintptr_t al = reinterpret_cast<uintptr_t>(L.cp) | reinterpret_cast<uintptr_t>(dest) |
-                           reinterpret_cast<uintptr_t>(L.g0f) | reinterpret_cast<uintptr_t>(L.rr0f) |
-                           reinterpret_cast<uintptr_t>(L.compf);
+                           reinterpret_cast<uintptr_t>(L.g0f);
       if (al & 15) return cudaErrorMisalignedAddress;  // the kernel stages the tables with 16-byte copies
-      static bool attr = false;
-      if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
-        if (e != cudaSuccess) return e;
-        attr = true;
-      }
+      const cudaError_t e = tpf_opt_in();
+      if (e != cudaSuccess) return e;
       dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes + dev::tpf::kSumBytes, s>>>(
-          L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
+          L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status, fin);
       return cudaGetLastError();
     }
   }
   if (ncp == 12 && npt == 15)
-    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
+    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status,
+                                                           fin);
   else if (ncp == 11 && npt == 16)
-    dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
+    dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status,
+                                                           fin);
   else if (ncp == 13 && npt == 16)
-    dev::face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart, status, fin);
+    dev::face_kernel<T, 13, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status,
+                                                           fin);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 template cudaError_t launch_faces<double>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
-                                          const double *, const float *, const float *, double *, double *, int *,
-                                          int, const FinishArgs &, cudaStream_t);
+                                          const double *, const F32Pos &, double *, double *, int *, int,
+                                          const FinishArgs &, cudaStream_t);
 template cudaError_t launch_faces<float>(const dev::FaceLaunch &, const int *, int, int, const dev::SurfaceParams &,
-                                         const double *, const float *, const float *, float *, double *, int *, int,
+                                         const double *, const F32Pos &, float *, double *, int *, int,
                                          const FinishArgs &, cudaStream_t);
 
-cudaError_t launch_split_positions(int n, const double *r, float *hi, float *lo, cudaStream_t s) {
+cudaError_t launch_split_positions(int n, const double *r, const F32Pos &f, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  dev::split_positions_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, r, hi, lo);
+  if (!f.hi || !f.lo || !f.r0 || !f.dsp) return cudaErrorInvalidValue;
+  dev::split_positions_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, r, f.hi, f.lo, f.r0, f.dsp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_status_merge(const int *src, int *dst, cudaStream_t s) {
+  dev::status_merge_kernel<<<1, 1, 0, s>>>(src, dst);
   return cudaGetLastError();
 }
 
@@ -2644,23 +2754,24 @@ template cudaError_t launch_gather<float>(int, const float *, const int *, doubl
 
 template <typename T>
 cudaError_t launch_gather_step(int nv, const T *partial, const int *off, const StepArgs &a, const uint64_t *cnt,
-                               double *r, double *p, float *rhi, float *rlo, const int *status, cudaStream_t s) {
-  dev::gather_step_kernel<T><<<grid_for(nv, 256), 256, 0, s>>>(nv, partial, off, a, cnt, r, p, rhi, rlo, status);
+                               double *r, double *p, const F32Pos &f, const int *status, cudaStream_t s) {
+  dev::gather_step_kernel<T><<<grid_for(nv, 256), 256, 0, s>>>(nv, partial, off, a, cnt, r, p, f.hi, f.lo, f.r0,
+                                                               f.dsp, status);
   return cudaGetLastError();
 }
 template cudaError_t launch_gather_step<double>(int, const double *, const int *, const StepArgs &, const uint64_t *,
-                                                double *, double *, float *, float *, const int *, cudaStream_t);
+                                                double *, double *, const F32Pos &, const int *, cudaStream_t);
 template cudaError_t launch_gather_step<float>(int, const float *, const int *, const StepArgs &, const uint64_t *,
-                                               double *, double *, float *, float *, const int *, cudaStream_t);
+                                               double *, double *, const F32Pos &, const int *, cudaStream_t);
 
 cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *cnt, double *p, const double *g, const int *status,
                         cudaStream_t s) {
   dev::kick_kernel<<<grid_for(nv, 256), 256, 0, s>>>(nv, a, cnt, p, g, status);
   return cudaGetLastError();
 }
-cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, float *rhi, float *rlo,
+cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, const F32Pos &f,
                          const int *status, cudaStream_t s) {
-  dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, rhi, rlo, status);
+  dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, f.hi, f.lo, f.r0, f.dsp, status);
   return cudaGetLastError();
 }
 cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
@@ -2712,15 +2823,10 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
   constexpr int NT = dev::FaceCfg<T>::threads;
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
-      static bool attr = false;
-      if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(dev::batch_face_tpf_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dev::tpf::kStageBytes);
-        if (e != cudaSuccess) return e;
-        attr = true;
-      }
+      cudaError_t e = batch_tpf_opt_in();
+      if (e != cudaSuccess) return e;
       if (!next_tile) return cudaErrorInvalidValue;
-      cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
+      e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
       if (e != cudaSuccess) return e;
       dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes, s>>>(
           jobs, group, tiles, counts, basis, weight, dudv, tile_sums, next_tile);
@@ -2796,27 +2902,16 @@ template cudaError_t launch_geo_grad<float>(const GeoArgs &, float *, cudaStream
 namespace umcp {
 
 int face_blocks_tc(int nfaces) {
-  static const int sms = [] {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 152;
-  }();
   const int tiles = (nfaces + dev::tc::kFaces - 1) / dev::tc::kFaces;
-  const int cap = 2 * sms;  // two CTAs per SM (shared memory and tensor memory)
+  const int cap = 2 * sm_count();  // two CTAs per SM (shared memory and tensor memory)
   return tiles < 1 ? 1 : (tiles < cap ? tiles : cap);
 }
 
 cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev::SurfaceParams &P, const double *r,
                             const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
                             int grid, const FinishArgs &fin, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(dev::face_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)dev::tc::kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  const cudaError_t e = tc_opt_in();
+  if (e != cudaSuccess) return e;
   dev::face_tc_kernel<<<grid, dev::tc::kThreads, dev::tc::kSmemBytes, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart,
                                                                            status, fin);
   return cudaGetLastError();
