@@ -35,6 +35,16 @@ all vesicles, a per-vesicle energy sum and one fused gather + update.
 --impl reference runs the oracle's C restatement of the reference path (the
 reference's own code cannot be built on the GPU host) with all host cores,
 one vesicle per process at a time, as independent reference runs would.
+
+Profiling modes (the commands behind the ncu summaries; no JSON line):
+  --mode facepass   queues the per-face pass `--repeat` times after one
+            energy+gradient call: on an --nx x --ny planar membrane (or an
+            --icosphere level), or, with --vesicles N, the batched face
+            launches over the first N vesicles of the benchmark workload after
+            three batched BD steps at --tile-faces.
+  --mode massapply  builds M^-1 on an icosahedral vesicle of --level (the
+            reference's settings: 66 mass points per face, truncation 1e-20)
+            and times --repeat applies with CUDA events after 3 untimed ones.
 """
 from __future__ import annotations
 
@@ -85,6 +95,17 @@ def parse_args():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "facepass", "massapply"])
+    ap.add_argument("--nx", type=int, default=512, help="facepass: planar membrane size")
+    ap.add_argument("--ny", type=int, default=512)
+    ap.add_argument("--icosphere", type=int, default=0, help="facepass: an icosahedral vesicle of this level instead")
+    ap.add_argument("--level", type=int, default=5, help="massapply: Loop subdivisions of the icosahedron")
+    ap.add_argument("--radius", type=float, default=1000.0, help="massapply: vesicle radius (A)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="facepass / massapply")
+    ap.add_argument("--repeat", type=int, default=3, help="facepass / massapply")
+    ap.add_argument("--tile-faces", type=int, default=128, help="facepass with --vesicles")
+    ap.add_argument("--face-kernel", default="simt", choices=["tc", "simt"],
+                    help="facepass: regular faces of the FP32 form on the tensor cores or the SIMT kernel")
     return ap.parse_args()
 
 
@@ -650,9 +671,105 @@ def reference_arm(args) -> None:
     print(json.dumps(out))
 
 
+# ------------------------------------------------------------------ profiling modes
+
+def facepass_mode(args) -> None:
+    """The per-face pass alone (the dominant kernels), for ncu captures."""
+    import umcp_gb300 as U
+    from umcp_gb300 import workloads as W
+
+    prec = U.FP32_CENTRED if args.precision == "fp32" else U.FP64
+    ctx = U.Context(0)
+    if args.vesicles:
+        with tempfile.TemporaryDirectory() as td:
+            pp = W.vesicle_plans(W.vesicle_specs(args.vesicles, WORKLOAD["seed"]), Path(td), prec)
+        meshes = [U.Mesh(ctx, plan, prm) for plan, prm in pp]
+        batch = U.Batch(ctx, prec, tile_faces=args.tile_faces)
+        for i, m in enumerate(meshes):
+            batch.add(m, W.bd_integrator(WORKLOAD["seed"], i), 0, 4)  # live after three steps: the passes do work
+        batch.run(3)
+        done, st = batch.poll()
+        for _ in range(args.repeat):
+            batch.face_pass()
+        ctx.synchronize()
+        info = batch.info()
+        print(f"vesicles={info.n_jobs} vertices={info.n_vertices} faces={info.n_faces} tiles={list(info.n_tiles)} "
+              f"steps={int(done.min())} status={int(st.max())}")
+        return
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=prec,
+                   face_kernel=U.TENSOR_CORES if args.face_kernel == "tc" else U.SIMT)
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "m.mesh"
+        if args.icosphere:
+            U.generate_icosphere(path, args.icosphere, 1000.0, 2.0, 7)
+        else:
+            U.generate_planar(path, args.nx, args.ny, 10.0, 20.0, 7)
+        plan = U.Plan(path, prm)
+    mesh = U.Mesh(ctx, plan, prm)
+    E, _ = mesh.energy_grad(plan.positions())
+    for _ in range(args.repeat):
+        mesh.face_pass()
+    ctx.synchronize()
+    info = mesh.info()
+    print(f"faces={info.n_faces} points={info.n_points} E={E:.10g}")
+
+
+def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool) -> int:
+    """Algorithmic bytes of one apply, out += M^-1 in on 3 components per row:
+    CSR 8 per nonzero (FP32 value and column; 12 in FP64) plus, per row, the
+    row pointer (4), the input gathered at least once (16 as the packed FP32
+    copy, 24 in FP64) and the output read and written (48); dense 4 (or 8) per
+    entry plus the same per row."""
+    per_entry = (4 if fp32 else 8) if dense else (8 if fp32 else 12)
+    entries = nrow * nrow if dense else nnz
+    per_row = (0 if dense else 4) + (16 if fp32 else 24) + 48
+    return per_entry * entries + per_row * nrow
+
+
+def massapply_mode(args) -> None:
+    """Times the effective-mass inverse apply (umcp_mass_apply_device)."""
+    import torch
+
+    import umcp_gb300 as U
+
+    fp32 = args.precision == "fp32"
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=U.FP32_CENTRED if fp32 else U.FP64)
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "vesicle.mesh"
+        U.generate_icosphere(path, args.level, args.radius, 2.0, 7)
+        plan = U.Plan(path, prm)
+    ctx = U.Context(0)
+    mesh = U.Mesh(ctx, plan, prm)
+    info = mesh.mass_build(plan)
+    nrow = mesh.nv
+    dev = torch.device("cuda:0")
+    x = torch.randn(3 * nrow, dtype=torch.float64, generator=torch.Generator().manual_seed(7)).to(dev)
+    y = torch.zeros(3 * nrow, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    for _ in range(3):
+        mesh.mass_apply_device(x.data_ptr(), y.data_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.repeat):
+        mesh.mass_apply_device(x.data_ptr(), y.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    us = e0.elapsed_time(e1) * 1e3 / max(args.repeat, 1)
+    nbytes = mass_apply_bytes(nrow, info.nnz_inverse, bool(info.dense), fp32)
+    fill = info.nnz_inverse / float(nrow * nrow)
+    print(f"rows={nrow} nnz={info.nnz_inverse} fill={fill:.3f} {'dense' if info.dense else 'csr'} {args.precision} "
+          f"apply {us:.1f} us bytes={nbytes} ({nbytes / (us * 1e-6) / 1e9:.0f} GB/s) "
+          f"finite={bool(torch.isfinite(y).all().item())}")
+
+
 def main() -> None:
     args = parse_args()
-    if args.impl == "reference":
+    if args.mode == "facepass":
+        facepass_mode(args)
+    elif args.mode == "massapply":
+        massapply_mode(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         engine_arm(args)

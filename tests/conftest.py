@@ -19,10 +19,11 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def built_libraries():
     """Builds the engine and the oracle if they are missing or stale."""
+    from oracle import build as OBLD
     from umcp_gb300 import build as B
 
     B.build_engine()
-    B.build_oracle()
+    OBLD.build_oracle()
     yield
 
 

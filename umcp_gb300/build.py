@@ -1,12 +1,10 @@
-"""Builds the engine's shared library (CUDA for sm_103a + host C++), the
-oracle's C restatement and, when the reference tree is present, the
-reference-built oracle binary. Objects are rebuilt only when a source is newer.
+"""Builds the engine's shared library (CUDA for sm_103a + host C++) and the
+hd-style driver. Objects are rebuilt only when a source is newer. (The
+checker, under oracle/, has its own recipe: oracle/build.py.)
 
 Outputs (all git-ignored):
   umcp_gb300/lib/libumcp_gb300.so   engine: kernels + C ABI (include/umcp_gpu.h)
   umcp_gb300/lib/hd_gb300           the hd-style dynamics driver on the engine
-  oracle/lib/libumcp_oracle.so      CPU restatement used by tests as the checker
-  oracle/_ref/ref_driver            reference sources + shims (only where they exist)
 """
 from __future__ import annotations
 
@@ -23,9 +21,6 @@ BUILD = ROOT / "umcp_gb300" / "_build"
 LIB_DIR = ROOT / "umcp_gb300" / "lib"
 ENGINE_LIB = LIB_DIR / "libumcp_gb300.so"
 HD_EXE = LIB_DIR / "hd_gb300"
-ORACLE_DIR = ROOT / "oracle"
-ORACLE_LIB = ORACLE_DIR / "lib" / "libumcp_oracle.so"
-REF_TREE = Path(os.environ.get("UMCP_REFERENCE_SRC", "/root/reference/src"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -88,31 +83,8 @@ def build_engine(verbose: bool = False) -> Path:
     return ENGINE_LIB
 
 
-def build_oracle(verbose: bool = False) -> Path:
-    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    src = ORACLE_DIR / "umcp_oracle.c"
-    if _stale(ORACLE_LIB, [src, ORACLE_DIR / "umcp_oracle.h"]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", str(ORACLE_LIB), str(src), "-lm"])
-    if verbose:
-        print(f"built {ORACLE_LIB}")
-    return ORACLE_LIB
-
-
-def build_reference_oracle(verbose: bool = False) -> Path | None:
-    """Compiles the reference's own sources (only where the tree exists)."""
-    if not (REF_TREE / "interpLib.C").exists():
-        return None
-    _run(["make", "-s", "-C", str(ORACLE_DIR / "ref"), f"REF_SRC={REF_TREE}", f"-j{os.cpu_count() or 2}"])
-    out = ORACLE_DIR / "_ref" / "ref_driver"
-    if verbose:
-        print(f"built {out}")
-    return out
-
-
 def build_all(verbose: bool = False) -> None:
     build_engine(verbose)
-    build_oracle(verbose)
-    build_reference_oracle(verbose)
 
 
 if __name__ == "__main__":
