@@ -673,6 +673,23 @@ def reference_arm(args) -> None:
 
 # ------------------------------------------------------------------ profiling modes
 
+def _time_passes(ctx, face_pass, repeat: int) -> float:
+    """Microseconds per face pass: `repeat` passes between two CUDA events on
+    the context's stream (the first pass of a capture is the profiled one)."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda:0"))
+    face_pass()  # untimed
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(repeat):
+        face_pass()
+    e1.record(stream)
+    e1.synchronize()
+    ctx.synchronize()
+    return e0.elapsed_time(e1) * 1e3 / max(repeat, 1)
+
+
 def facepass_mode(args) -> None:
     """The per-face pass alone (the dominant kernels), for ncu captures."""
     import umcp_gb300 as U
@@ -689,12 +706,10 @@ def facepass_mode(args) -> None:
             batch.add(m, W.bd_integrator(WORKLOAD["seed"], i), 0, 4)  # live after three steps: the passes do work
         batch.run(3)
         done, st = batch.poll()
-        for _ in range(args.repeat):
-            batch.face_pass()
-        ctx.synchronize()
+        us = _time_passes(ctx, batch.face_pass, args.repeat)
         info = batch.info()
         print(f"vesicles={info.n_jobs} vertices={info.n_vertices} faces={info.n_faces} tiles={list(info.n_tiles)} "
-              f"steps={int(done.min())} status={int(st.max())}")
+              f"steps={int(done.min())} status={int(st.max())} face_pass_us={us:.1f}")
         return
     prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=prec,
                    face_kernel=U.TENSOR_CORES if args.face_kernel == "tc" else U.SIMT)
@@ -707,11 +722,9 @@ def facepass_mode(args) -> None:
         plan = U.Plan(path, prm)
     mesh = U.Mesh(ctx, plan, prm)
     E, _ = mesh.energy_grad(plan.positions())
-    for _ in range(args.repeat):
-        mesh.face_pass()
-    ctx.synchronize()
+    us = _time_passes(ctx, mesh.face_pass, args.repeat)
     info = mesh.info()
-    print(f"faces={info.n_faces} points={info.n_points} E={E:.10g}")
+    print(f"faces={info.n_faces} points={info.n_points} E={E:.10g} face_pass_us={us:.1f}")
 
 
 def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool) -> int:
