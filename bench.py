@@ -14,10 +14,13 @@ all vesicles, a per-vesicle energy sum and one fused gather + update.
   value     device-resident throughput: K steps between CUDA events on the
             engine's stream (the step inputs, about 0.4 GB of face tables and
             state, exceed the 129 MB L2, so no flush is needed).
-  e2e       the same jobs through the public serving API (umcp_server_*):
-            mesh files on the host in, plans built, state uploaded, K steps,
-            final states copied back; wall clock from first submit to last
-            result.
+  e2e       the same batch driven from the host through the public C ABI
+            (umcp_batch_step_host), as the reference's loop holds its state
+            on the host: every step all jobs' states go in from pinned host
+            memory and the new states and energies come back; wall clock.
+  admission the same vesicles as mesh files through the serving API
+            (umcp_server_*): plans built, state uploaded, K steps, results
+            copied back; wall clock from first submit to last result.
   roofline  the batch's face launches (the dominant kernels) timed alone with
             CUDA events: algorithmic bytes per launch / duration against the
             measured HBM copy bandwidth, and FP32 flop rate against the
@@ -32,9 +35,11 @@ all vesicles, a per-vesicle energy sum and one fused gather + update.
             side), kc 10-40 kT, steps log-uniform in 1e3-1e5; p50/p99 job
             latency and aggregate vertex-steps/s.
 
---impl reference runs the oracle's C restatement of the reference path (the
-reference's own code cannot be built on the GPU host) with all host cores,
-one vesicle per process at a time, as independent reference runs would.
+--impl reference runs the oracle's C restatement of the reference path on its
+own plan of every vesicle (oracle/planner.py: no engine code is loaded), with
+all host cores, vesicles dealt round robin over one process per core, as
+independent reference runs would (the reference's own sources are not on the
+GPU host).
 
 Profiling modes (the commands behind the ncu summaries; no JSON line):
   --mode facepass   queues the per-face pass `--repeat` times after one
@@ -232,39 +237,82 @@ def time_batch(batch, ctx, stream, torch, K: int) -> float:
     return e0.elapsed_time(e1) / 1e3
 
 
-def cpu_port_sample(specs, tmpdir: Path, seconds: float) -> dict:
-    """Single-core oracle (restatement of the reference path): energy +
-    gradient + BD update per step on the first vesicles of the workload, in
-    turn, for about `seconds`."""
-    import umcp_gb300 as U
-    from oracle import bridge as OB
-    from umcp_gb300 import workloads as W
+def workload_config(specs) -> dict:
+    """The workload's description: the same dict in both arms' lines."""
+    nv = sum(10 * 4 ** s.level + 2 for s in specs)
+    nf = sum(20 * 4 ** s.level for s in specs)
+    return dict(WORKLOAD, n_vesicles=len(specs), vertices=nv, faces=nf)
 
-    D_dt = WORKLOAD["rms_step_A"] ** 2 / 2.0
-    chosen = [next(s for s in specs if s.level == lvl) for lvl in (2, 3, 4, 5) if any(s.level == lvl for s in specs)]
-    sys_ = []
-    for s in chosen:
-        plan, prm = W.vesicle_plans([s], tmpdir / "cpu", U.FP64, threads=1)[0]
-        sys_.append((plan, prm, OB.Oracle(plan, prm), plan.positions(), np.zeros(3 * plan.nv)))
+
+def engine_mapped() -> bool:
+    """Whether this process has the engine's shared library mapped (the CPU
+    legs must not: they run the oracle's restatement alone)."""
+    try:
+        return "libumcp_gb300" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return False
+
+
+class OracleVesicles:
+    """The workload's vesicles planned by the oracle (oracle/planner.py, no
+    engine code): the vesicle generator, the reference's plan construction
+    and setg0, the reference's basis rows; the topology is planned once per
+    subdivision level (the generator's connectivity depends on the level only,
+    and a vesicle's box of 3 R leaves every control point in its home image)."""
+
+    def __init__(self):
+        self.topology = {}
+
+    def surface(self, s):
+        from oracle import planner as OP
+        from umcp_gb300 import kc_from_kT
+        from umcp_gb300 import workloads as W
+
+        m = OP.icosphere(s.level, s.radius, s.sigma, s.seed)
+        return OP.Surface(m, kc_from_kT(s.kc_kT), 0.215, lipids=W.lipid_text(s.c0),
+                          topology=self.topology.setdefault(s.level, {}))
+
+
+def _oracle_bd_steps(systems, seconds: float, seed: int, rms: float):
+    """Overdamped BD steps (energy + gradient + update, the oracle's C
+    restatement) over the systems in turn for `seconds` (each at least once)."""
+    from oracle import bridge as OB
+
+    D_dt = rms * rms / 2.0
+    kT = 0.592186663194
     steps, vs, t0 = 0, 0, time.perf_counter()
     while True:
-        plan, prm, O, r, p = sys_[steps % len(sys_)]
-        g = O.grad(r)
-        O.energy(r)
-        xi = OB.noise(WORKLOAD["seed"], 0, steps, plan.nv)
+        S, r, p, idx = systems[steps % len(systems)]
+        S.energy(r)
+        g = S.grad(r)
+        xi = OB.noise(seed, idx, steps // len(systems), S.nv)
         rv = r[:-3].copy()
-        OB.step(0, 1.0, 0.0, U.KCAL_MOL_PER_KT_298, D_dt, rv, p, g[:-3], xi)
+        OB.step(0, 1.0, 0.0, kT, D_dt, rv, p, g[:-3], xi)
         r[:-3] = rv
         steps += 1
-        vs += plan.nv
+        vs += S.nv
         el = time.perf_counter() - t0
-        if el >= seconds and steps >= len(sys_):
-            break
+        if el >= seconds and steps >= len(systems):
+            return vs, el, steps
+
+
+def cpu_port_sample(specs, seconds: float) -> dict:
+    """Single-core oracle (restatement of the reference path, planned by the
+    oracle itself): energy + gradient + BD update per step over one vesicle
+    of each subdivision level of the workload, in turn, for about `seconds`."""
+    chosen = [next(s for s in specs if s.level == lvl) for lvl in (2, 3, 4, 5) if any(s.level == lvl for s in specs)]
+    ov = OracleVesicles()
+    systems = []
+    for s in chosen:
+        S = ov.surface(s)
+        systems.append((S, S.positions.copy(), np.zeros(3 * S.nv), s.index))
+    vs, el, steps = _oracle_bd_steps(systems, seconds, WORKLOAD["seed"], WORKLOAD["rms_step_A"])
     levels = "/".join(str(s.level) for s in chosen)
     return {"value": vs / el, "unit": "vertex-steps/s", "cores": 1, "kind": "port",
             "sample": f"{steps} BD steps (energy+gradient+update), one vesicle per step in turn over one vesicle of "
                       f"each subdivision level ({levels}) of the same workload, one core, {el:.1f} s; the oracle's "
-                      f"C restatement of the reference path (the reference cannot be built on this host)"}
+                      f"C restatement of the reference path on its own plan of each vesicle (the reference's "
+                      f"sources are not on this host)"}
 
 
 def serving_run(ctx, U, W, seconds: float, rate: float, seed: int, tmpdir: Path) -> dict:
@@ -355,6 +403,57 @@ def planar_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int) -> dict:
 
 
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
+
+
+def config1_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_gbs: float) -> dict:
+    """The plain FP64 method on one closed vesicle: an icosahedron subdivided
+    3x (642 vertices, 1280 faces), R 100 A, radial noise N(0, 1 A) (seed
+    1001), kc 20 kT, c0 0, T 298 K; one energy+gradient, then K overdamped BD
+    steps with sqrt(2 D dt) = 0.05 A, timed with CUDA events on the engine's
+    stream. Beside it the same vesicle on one host core through the oracle's
+    C restatement (its own plan), 20 steps."""
+    tmpdir.mkdir(parents=True, exist_ok=True)
+    path = tmpdir / "config1.mesh"
+    U.generate_icosphere(path, 3, 100.0, 1.0, 1001)
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=U.FP64)
+    plan = U.Plan(path, prm)
+    mesh = U.Mesh(ctx, plan, prm)
+    E0, g0 = mesh.energy_grad(plan.positions())
+    it = W.bd_integrator(1001, 0, 0.05)
+    mesh.run(it, 0, 32, energies=False)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    mesh.run_async(it, 32, K)
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    r1, _ = mesh.state_get()
+    byts, flops, _ = face_pass_work([plan], 8)
+    # the same vesicle on one host core, the oracle's own plan
+    from oracle import planner as OP
+
+    S = OP.Surface(OP.icosphere(3, 100.0, 1.0, 1001), U.kc_from_kT(20.0), 0.215)
+    Ecpu = S.energy(plan.positions())
+    systems = [(S, S.positions.copy(), np.zeros(3 * S.nv), 0)]
+    vs, el, nsteps = _oracle_bd_steps(systems, 0.0, 1001, 0.05)
+    t0 = time.perf_counter()
+    for _ in range(20):
+        _oracle_bd_steps(systems, 0.0, 1001, 0.05)
+    cpu_s = (time.perf_counter() - t0) / 20
+    return {"workload": "plain FP64 path, one icosahedral vesicle subdivided 3x (642 vertices, 1280 faces), R 100 A, "
+                        "radial noise N(0, 1 A), kc 20 kT, c0 0; one energy+gradient, then BD steps with "
+                        "sqrt(2 D dt) = 0.05 A",
+            "steps": K, "vertex_steps_per_s": plan.nv * K / sec, "ms_per_step": sec * 1e3 / K,
+            "first_energy": E0, "first_energy_rel_err_vs_oracle": abs(E0 - Ecpu) / abs(Ecpu),
+            "states_finite": bool(np.all(np.isfinite(r1))),
+            "fp64_tflops": flops * K / sec / 1e12, "fp64_frac_of_nominal": flops * K / sec / 1e12 / FP64_NOMINAL_TFLOPS,
+            "face_pass_bytes_per_step": byts, "hbm_gbs": byts * K / sec / 1e9, "hbm_frac": byts * K / sec / 1e9 / peak_gbs,
+            "note": "the whole mesh's data (about 0.6 MB) stays in L2; one step is two face launches and a fused "
+                    "gather-update, captured as CUDA graphs of 32 steps, so the step is launch- and latency-bound "
+                    "rather than bound by FP64 issue or HBM",
+            "cpu_oracle_1core": {"vertex_steps_per_s": plan.nv / cpu_s, "ms_per_step": cpu_s * 1e3, "cores": 1,
+                                 "kind": "port", "sample": "20 BD steps after one untimed step"}}
 
 
 def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_gbs: float) -> dict:
@@ -488,9 +587,9 @@ def engine_arm(args) -> None:
         "metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": K, "warmup": Wu,
         "ms_per_step": total_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded vesicles generated on the host)",
-        "config": dict(WORKLOAD, n_vesicles=len(specs), vertices=nv_total, faces=nfaces,
-                       parallelism=f"replicas x{world}" if world > 1 else "one GPU",
-                       tile_faces=info.tile_faces, face_grid=list(info.face_grid)),
+        "config": workload_config(specs),
+        "engine": {"parallelism": f"replicas x{world}" if world > 1 else "one GPU", "tile_faces": info.tile_faces,
+                   "face_grid": list(info.face_grid)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"],
                      "traffic": (BATCH_FACE_DRAM_BYTES_PER_FACE * nfaces) if BATCH_FACE_DRAM_BYTES_PER_FACE else None,
@@ -506,26 +605,56 @@ def engine_arm(args) -> None:
         "wall_s_timed": t_wall,
     }
     if world > 1:
-        out["config"]["vertices_all_ranks"] = nv_job  # each rank its own replica set; config is rank 0's
+        out["engine"]["vertices_all_ranks"] = nv_job  # each rank its own replica set; config is rank 0's
     e32_first = np.array([m.energies(1)[0] for m in meshes32])
     del batch
 
+    # ---- e2e: the same batch driven from the host (umcp_batch_step_host):
+    # every step, all jobs' states go in from pinned host memory and the new
+    # states and each job's energy come back; wall clock around K calls
+    be = U.Batch(ctx, U.FP32_CENTRED, tile_faces=info.tile_faces)
+    for i, m in enumerate(meshes32):
+        be.add(m, W.bd_integrator(WORKLOAD["seed"] + 7, i, WORKLOAD["rms_step_A"]), 0, Wu + K)
+    npack = sum(3 * m.nv + 3 for m in meshes32)
+    pack_t = torch.empty(npack, dtype=torch.float64, pin_memory=True)
+    E_t = torch.empty(len(meshes32), dtype=torch.float64, pin_memory=True)
+    pack = pack_t.numpy()
+    pack[:] = np.concatenate([m.state_get()[0] for m in meshes32])
+    for _ in range(Wu):
+        be.step_host(pack_t.data_ptr(), pack_t.data_ptr(), E_t.data_ptr(), 1)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        be.step_host(pack_t.data_ptr(), pack_t.data_ptr(), E_t.data_ptr(), 1)
+    e2e_wall = time.perf_counter() - t0
+    if world > 1:
+        e2e_wall = over_ranks(e2e_wall, "max", f"cuda:{local}")
+    done_e, st_e = be.poll()
+    assert np.all(st_e == 0) and np.all(done_e == Wu + K) and np.all(np.isfinite(E_t.numpy())), "a job failed"
+    out["e2e"] = {"value": nv_job * K / e2e_wall, "unit": "vertex-steps/s",
+                  "h2d_bytes_per_step": 8.0 * npack, "d2h_bytes_per_step": 8.0 * (npack + len(meshes32)),
+                  "path": "umcp_batch_step_host once per step: every job's state (positions and box scales, "
+                          "packed) copied in from pinned host memory, one batched step, the new states and each "
+                          "job's energy copied back; wall clock",
+                  "wall_s": e2e_wall}
+    del be
+
     if rank == 0 and world == 1:
-        # ---- e2e: the same vesicles through the serving API, host files in and results out
+        # ---- admission: the same vesicles submitted to the serving API as mesh files
         srv = U.Server(ctx, U.FP32_CENTRED, chunk_ms=50.0)
         t0 = time.perf_counter()
         ids = [srv.submit(tmp / "fp32" / f"vesicle_{s.index}.mesh", pp32[s.index][1],
                           W.bd_integrator(WORKLOAD["seed"], s.index, WORKLOAD["rms_step_A"]), 0, K) for s in specs]
         srv.wait_all()
-        e2e_wall = time.perf_counter() - t0
+        sub_wall = time.perf_counter() - t0
         jinfo = [srv.job(j) for j in ids]
         assert all(j.status == 0 and j.steps_done == K for j in jinfo), "a served vesicle failed"
-        out["e2e"] = {"value": nv_total * K / e2e_wall, "unit": "vertex-steps/s",
-                      "h2d_bytes_per_step": sum(j.h2d_bytes for j in jinfo) / K,
-                      "d2h_bytes_per_step": sum(j.d2h_bytes for j in jinfo) / K,
-                      "path": "umcp_server_submit of the 256 mesh files (plans built on host threads, state "
-                              "uploaded), K steps batched, final states copied to the host; wall clock",
-                      "wall_s": e2e_wall}
+        out["admission"] = {"vertex_steps_per_s": nv_total * K / sub_wall, "wall_s": sub_wall, "steps": K,
+                            "last_admit_s": max(j.t_admit - j.t_submit for j in jinfo),
+                            "path": "umcp_server_submit of the 256 mesh files (plans built on host threads, state "
+                                    "uploaded), K steps batched, final states copied to the host; wall clock from "
+                                    "the first submit to the last result"}
         srv.close()
 
         if not args.no_variants:
@@ -585,6 +714,8 @@ def engine_arm(args) -> None:
             var["batched_fp32_over_plain_fp64"] = value / var["plain_fp64_one_by_one"]["vertex_steps_per_s"]
             del meshes64
             var["planar128_fp32"] = planar_variant(ctx, U, W, torch, stream, tmp / "planar", 300)
+            var["config1_plain_fp64_642"] = config1_variant(ctx, U, W, torch, stream, tmp / "config1", 1000,
+                                                            peaks["hbm_gbs"])
             var["langevin_mass_40962"] = langevin_mass_variant(ctx, U, W, torch, stream, tmp / "large", 2000,
                                                                peaks["hbm_gbs"])
             out["variants"] = var
@@ -593,7 +724,7 @@ def engine_arm(args) -> None:
             if "variants" in out:
                 out["serving"]["over_plain_fp64_one_by_one"] = (
                     out["serving"]["vertex_steps_per_s"] / out["variants"]["plain_fp64_one_by_one"]["vertex_steps_per_s"])
-        out["cpu_baseline"] = cpu_port_sample(specs, tmp, args.cpu_seconds)
+        out["cpu_baseline"] = cpu_port_sample(specs, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -604,34 +735,26 @@ def engine_arm(args) -> None:
 # ------------------------------------------------------------------ reference arm
 
 def _ref_worker(job):
-    """One host process: BD steps of its vesicles in turn for `seconds`."""
-    specs, tmpdir, seconds, seed, rms = job
-    import umcp_gb300 as U
-    from oracle import bridge as OB
-    from umcp_gb300 import workloads as W
-
-    D_dt = rms * rms / 2.0
-    sys_ = []
+    """One host process of the reference arm: plans its vesicles with the
+    oracle (no engine code), steps each once untimed, then steps them in turn
+    for `seconds`. Returns (vertex-steps, seconds, steps, engine library mapped)."""
+    specs, seconds, seed, rms = job
+    ov = OracleVesicles()
+    systems = []
     for s in specs:
-        plan, prm = W.vesicle_plans([s], Path(tmpdir), U.FP64, threads=1)[0]
-        sys_.append((plan.nv, OB.Oracle(plan, prm), plan.positions(), np.zeros(3 * plan.nv), s.index))
-    steps, vs, t0 = 0, 0, time.perf_counter()
-    while True:
-        nv, O, r, p, idx = sys_[steps % len(sys_)]
-        O.energy(r)
-        g = O.grad(r)
-        xi = OB.noise(seed, idx, steps // len(sys_), nv)
-        rv = r[:-3].copy()
-        OB.step(0, 1.0, 0.0, U.KCAL_MOL_PER_KT_298, D_dt, rv, p, g[:-3], xi)
-        r[:-3] = rv
-        steps += 1
-        vs += nv
-        if time.perf_counter() - t0 >= seconds and steps >= len(sys_):
-            break
-    return vs, time.perf_counter() - t0, steps
+        S = ov.surface(s)
+        systems.append((S, S.positions.copy(), np.zeros(3 * S.nv), s.index))
+    _oracle_bd_steps(systems, 0.0, seed, rms)
+    vs, el, steps = _oracle_bd_steps(systems, seconds, seed, rms)
+    return vs, el, steps, engine_mapped()
 
 
 def reference_arm(args) -> None:
+    """The reference path on the host cores: the oracle's C restatement of
+    surface::energy / surface::grad and the BD update, on the oracle's own
+    plan of every vesicle of the workload (one process per core, vesicles
+    dealt round robin), for --ref-seconds. The reference's own build cannot
+    run here: its sources are not on this host."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -640,32 +763,34 @@ def reference_arm(args) -> None:
     from umcp_gb300 import workloads as W
 
     specs = W.vesicle_specs(args.vesicles, WORKLOAD["seed"])
-    P = os.cpu_count() or 1
-    tmp = Path(tempfile.mkdtemp(prefix="umcp_ref_"))
-    # each process takes vesicles round robin, at most 4 (their plans are built inside the sample's time)
-    per = [specs[i::P][:4] for i in range(P)]
-    per = [p for p in per if p]
+    P = min(os.cpu_count() or 1, len(specs))
+    per = [specs[i::P] for i in range(P)]
     seconds = max(5.0, args.ref_seconds)
-    jobs = [(p, str(tmp / f"w{i}"), seconds, WORKLOAD["seed"], WORKLOAD["rms_step_A"]) for i, p in enumerate(per)]
+    jobs = [(p, seconds, WORKLOAD["seed"], WORKLOAD["rms_step_A"]) for p in per]
     t0 = time.perf_counter()
-    with mp.get_context("spawn").Pool(len(per)) as pool:
+    with mp.get_context("spawn").Pool(P) as pool:
         res = pool.map(_ref_worker, jobs)
     wall = time.perf_counter() - t0
     vs = sum(r[0] for r in res)
     el = max(r[1] for r in res)
     steps = sum(r[2] for r in res)
+    mapped = engine_mapped() or any(r[3] for r in res)
     value = vs / el
+    cfg = workload_config(specs)
     out = {
         "metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 1), "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "warmup": max(args.warmup, 1), "ms_per_step": cfg["vertices"] / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
         "data": "synthetic (seeded vesicles generated on the host)",
-        "config": dict(WORKLOAD, n_vesicles=len(specs), parallelism=f"{len(per)} host processes"),
-        "cpu_baseline": {"value": value, "unit": "vertex-steps/s", "cores": len(per), "kind": "port",
-                         "sample": f"{len(per)} processes, each stepping up to 4 of the workload's vesicles in turn "
-                                   f"(energy + gradient + BD update per step) for {seconds:.0f} s: {steps} steps in "
-                                   f"all, {wall:.0f} s wall. The oracle's C restatement of the reference path (the "
-                                   f"reference's own build needs its source tree, absent on this host)."},
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": "vertex-steps/s", "cores": P, "kind": "port",
+                         "sample": f"{P} processes, {len(specs)} vesicles dealt round robin ({len(per[0])} or fewer "
+                                   f"each), every one planned by the oracle and stepped once untimed, then BD steps "
+                                   f"(energy + gradient + update) of each process's vesicles in turn for "
+                                   f"{seconds:.0f} s: {steps} steps in all, {wall:.0f} s wall. ms_per_step is one "
+                                   f"step of the whole workload at that rate. The oracle's C restatement of the "
+                                   f"reference path (the reference's sources are not on this host)."},
+        "engine_library_mapped": bool(mapped),
         "e2e": {"value": value, "unit": "vertex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))

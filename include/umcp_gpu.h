@@ -374,6 +374,18 @@ umcp_status umcp_batch_run(umcp_batch *batch, int n_steps);
 umcp_status umcp_batch_poll(umcp_batch *batch, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_job(umcp_batch *batch, const umcp_mesh *mesh, int64_t *steps_done, int *job_status);
 umcp_status umcp_batch_info_get(const umcp_batch *batch, umcp_batch_info *info);
+/* The host-driven form of a batch run, for callers that keep the states on
+ * the host as the reference's dynamics loop does (src/hd.C:1102-1720, one
+ * surface per process there): r_in holds every job's state (3*nv+3 doubles:
+ * positions, then the box scales) packed in job order (the order of
+ * umcp_batch_add; umcp_batch_poll reports the same order). They are copied
+ * in (one copy; pinned host memory makes it a direct DMA), n_steps steps are
+ * run as umcp_batch_run runs them, and the new states and each job's latest
+ * energy are copied out to r_out (packed the same way; may equal r_in) and
+ * E (one double per job). Either output may be NULL, and r_in may be NULL
+ * to step the resident states. Momenta stay on the device. Waits for the
+ * copies; per-job status as umcp_batch_poll reports it. */
+umcp_status umcp_batch_step_host(umcp_batch *batch, const double *r_in, double *r_out, double *E, int n_steps);
 /* Queues only the face launches of one step over the batch's current jobs
  * (tables as of the latest run): the unit a roofline measurement times. The
  * jobs' states and counters do not change; jobs that have done their step

@@ -148,3 +148,46 @@ def test_a_diverging_job_stops_alone(ctx):
     assert np.array_equal(bad.state_get()[0], alone.state_get()[0])
     k = int(done[1])
     assert np.max(np.abs(bad.energies(k) - alone.energies(k)) / np.abs(alone.energies(k))) <= E_TOL[U.FP64]
+
+
+@pytest.mark.parametrize("precision", [U.FP64, U.FP32_CENTRED])
+def test_host_driven_steps_follow_the_resident_run(ctx, precision):
+    """umcp_batch_step_host: the jobs' states go in from one packed host
+    array and come out after each call; the trajectory is the device-resident
+    batch run's, bit for bit, and E holds each job's latest step energy. A
+    state the caller changes between calls is the one the next step starts
+    from."""
+    its = _integrators()[:2]
+    names = ["ico2_plain", "ico3_deformed"]
+    runs = []
+    for host in (False, True):
+        batch = U.Batch(ctx, precision)
+        meshes = [_mesh(ctx, n, precision) for n in names]
+        for k, m in enumerate(meshes):
+            batch.add(m, its[k], 10 * k, 40)
+        if host:
+            pack = np.concatenate([m.state_get()[0] for m in meshes])
+            E = np.zeros(len(meshes))
+            for _ in range(20):
+                batch.step_host(pack, pack, E, 2)
+            states = np.split(pack, np.cumsum([3 * m.nv + 3 for m in meshes])[:-1])
+            assert all(np.array_equal(s, m.state_get()[0]) for s, m in zip(states, meshes))
+            assert np.array_equal(E, [m.energies(40)[-1] for m in meshes])
+        else:
+            batch.run(40)
+            states = [m.state_get()[0] for m in meshes]
+        runs.append(states)
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+    # a changed state is picked up by the next call
+    batch = U.Batch(ctx, precision)
+    m = _mesh(ctx, "ico2_plain", precision)
+    batch.add(m, its[0], 0, 5)
+    r = m.state_get()[0]
+    r[:-3] *= 1.001
+    out = np.zeros_like(r)
+    batch.step_host(r, out, None, 1)
+    alone = _mesh(ctx, "ico2_plain", precision)
+    alone.state_set(r)
+    alone.run(its[0], 0, 1)
+    assert np.array_equal(out, alone.state_get()[0])

@@ -213,6 +213,7 @@ _SIGNATURES = {
     "umcp_batch_job": [_VP, _VP, _I64, _I],
     "umcp_batch_info_get": [_VP, C.POINTER(BatchInfo)],
     "umcp_batch_face_pass": [_VP],
+    "umcp_batch_step_host": [_VP, _VP, _VP, _VP, C.c_int],
     "umcp_ctx_mem_info": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
     "umcp_plan_device_bytes": [_VP, _VP, C.c_int, C.c_int64, C.POINTER(C.c_size_t)],
     "umcp_server_create": [_VP, C.POINTER(ServerOpts), C.POINTER(_VP)],
@@ -612,6 +613,18 @@ class Batch:
 
     def run(self, n_steps: int) -> None:
         _check(library().umcp_batch_run(self._h, n_steps))
+
+    def step_host(self, r_in, r_out, E, n_steps: int = 1) -> None:
+        """Host-driven steps (umcp_batch_step_host): r_in / r_out / E are host
+        arrays (float64, the jobs' 3*nv+3 states packed in add order / one
+        energy per job) or raw host addresses (int, e.g. of pinned memory), or
+        None."""
+        def ptr(a):
+            if a is None or isinstance(a, int):
+                return C.c_void_p(a)
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+            return C.c_void_p(a.ctypes.data)
+        _check(library().umcp_batch_step_host(self._h, ptr(r_in), ptr(r_out), ptr(E), n_steps))
 
     def poll(self) -> tuple[np.ndarray, np.ndarray]:
         """(steps done, status) of every job, in add order."""

@@ -57,6 +57,10 @@ struct umcp_batch {
   // device tables
   DevBuf d_jobs, d_tiles, d_vtiles, d_tile_off, d_tile_idx, d_counts, d_live, d_prog, d_start, d_step0, d_tile_sums;
   DevBuf d_next_tile;  // tile counter of the regular face launch
+  // host-driven steps (umcp_batch_step_host): the jobs' states packed in job
+  // order, each job's offset into the pack, and the jobs' latest energies
+  DevBuf d_pack, d_pack_off, d_pack_E;
+  size_t pack_doubles = 0;
   size_t cap_jobs = 0, cap_tiles = 0, cap_vtiles = 0;
   // host copies of the counts and the latest progress (pinned)
   int counts[kCountWords] = {};
@@ -188,6 +192,9 @@ static umcp_status rebuild(umcp_batch *b) {
       vtiles.push_back(BatchTile{(int)j, first, std::min(kVertexTile, b->jobs[j].m->nv - first)});
   b->counts[kCountJobs] = (int)b->jobs.size();
   b->counts[kCountVertexTiles] = (int)vtiles.size();
+  std::vector<long long> pack_off(1, 0);
+  for (const Job &J : b->jobs) pack_off.push_back(pack_off.back() + 3 * (long long)J.m->nv + 3);
+  b->pack_doubles = (size_t)pack_off.back();
 
   const size_t nj = jt.size(), nt = tiles.size(), nvt = vtiles.size();
   if (nj > b->cap_jobs || nt > b->cap_tiles || nvt > b->cap_vtiles || !b->d_counts.p) {
@@ -212,6 +219,12 @@ static umcp_status rebuild(umcp_batch *b) {
     if (b->h_prog) cudaFreeHost(b->h_prog);
     b->h_prog = nullptr;
     UMCP_CUDA(cudaMallocHost((void **)&b->h_prog, 2 * b->cap_jobs * sizeof(unsigned long long)));
+    UMCP_CUDA(b->d_pack_off.alloc((b->cap_jobs + 1) * sizeof(long long)));
+    UMCP_CUDA(b->d_pack_E.alloc(b->cap_jobs * sizeof(double)));
+  }
+  if (b->pack_doubles * sizeof(double) > b->d_pack.bytes) {
+    UMCP_CUDA(cudaStreamSynchronize(s));
+    UMCP_CUDA(b->d_pack.alloc(std::max(b->pack_doubles * sizeof(double), 2 * b->d_pack.bytes)));
   }
   // Pageable sources: each copy has read its source when the call returns,
   // and the stream orders it after the steps already queued.
@@ -228,6 +241,8 @@ static umcp_status rebuild(umcp_batch *b) {
   if (!vtiles.empty())
     UMCP_CUDA(cudaMemcpyAsync(b->d_vtiles.p, vtiles.data(), vtiles.size() * sizeof(BatchTile),
                               cudaMemcpyHostToDevice, s));
+  UMCP_CUDA(cudaMemcpyAsync(b->d_pack_off.p, pack_off.data(), pack_off.size() * sizeof(long long),
+                            cudaMemcpyHostToDevice, s));
   UMCP_CUDA(cudaMemcpyAsync(b->d_counts.p, b->counts, sizeof(b->counts), cudaMemcpyHostToDevice, s));
   UMCP_CUDA(cudaStreamSynchronize(s));  // b->counts is rewritten by the next rebuild
   b->dirty = false;
@@ -542,6 +557,34 @@ extern "C" umcp_status umcp_batch_info_get(const umcp_batch *b, umcp_batch_info 
   info->tile_faces = b->tile_faces;
   info->tuned_face_ms = b->tuned_ms;
   return UMCP_OK;
+}
+
+extern "C" umcp_status umcp_batch_step_host(umcp_batch *b, const double *r_in, double *r_out, double *E,
+                                            int n_steps) {
+  if (!b || n_steps < 0) return fail(UMCP_ERR_INVALID, "bad argument");
+  if (b->jobs.empty()) return UMCP_OK;
+  UMCP_CUDA(cudaSetDevice(b->ctx->device));
+  cudaStream_t s = b->ctx->stream;
+  umcp_status st;
+  if ((st = harvest(b)) != UMCP_OK) return st;
+  if (b->dirty && (st = rebuild(b)) != UMCP_OK) return st;
+  if ((st = start_jobs(b)) != UMCP_OK) return st;
+  const size_t bytes = b->pack_doubles * sizeof(double);
+  if (r_in) {
+    UMCP_CUDA(cudaMemcpyAsync(b->d_pack.p, r_in, bytes, cudaMemcpyHostToDevice, s));
+    UMCP_CUDA(launch_batch_unpack(b->d_jobs.as<BatchJob>(), b->d_vtiles.as<BatchTile>(), b->d_counts.as<int>(),
+                                  b->d_pack_off.as<long long>(), b->d_pack.as<double>(), b->vgrid, s));
+  }
+  if ((st = umcp_batch_run(b, n_steps)) != UMCP_OK) return st;
+  if (r_out || E) {
+    UMCP_CUDA(launch_batch_pack(b->d_jobs.as<BatchJob>(), b->d_vtiles.as<BatchTile>(), b->d_counts.as<int>(),
+                                b->d_pack_off.as<long long>(), b->d_pack.as<double>(), b->d_pack_E.as<double>(),
+                                b->vgrid, s));
+    if (r_out) UMCP_CUDA(cudaMemcpyAsync(r_out, b->d_pack.p, bytes, cudaMemcpyDeviceToHost, s));
+    if (E) UMCP_CUDA(cudaMemcpyAsync(E, b->d_pack_E.p, b->jobs.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  UMCP_CUDA(cudaStreamSynchronize(s));
+  return harvest(b);
 }
 
 extern "C" umcp_status umcp_batch_face_pass(umcp_batch *b) {

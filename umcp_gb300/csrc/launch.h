@@ -200,6 +200,13 @@ cudaError_t launch_batch_gather_step(const BatchJob *jobs, const BatchTile *vtil
 // Run start of the jobs with start[j] != 0: counters {step0[j], 0}, status 0, hi/lo split.
 cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const int *start,
                                const unsigned long long *step0, int grid, cudaStream_t s);
+// Host-driven steps: jobs' states packed in job order at pack + off[j] (3 nv + 3
+// doubles each). unpack: into the jobs' resident states (and FP32 copies);
+// pack: back out, with each job's latest energy in E[j].
+cudaError_t launch_batch_unpack(const BatchJob *jobs, const BatchTile *vtiles, const int *counts,
+                                const long long *off, const double *pack, int grid, cudaStream_t s);
+cudaError_t launch_batch_pack(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const long long *off,
+                              double *pack, double *E, int grid, cudaStream_t s);
 // Device-filling grid of a batch face launch for a patch type.
 template <typename T>
 int batch_face_blocks(int ncp, int npt);

@@ -1988,6 +1988,53 @@ __global__ void batch_start_kernel(const BatchJob *__restrict__ jobs, const Batc
   }
 }
 
+// Host-driven batch steps: every job's state (3 nv + 3 doubles: positions,
+// then the box scales) packed in job order at pack[off[j] ..]. In: into each
+// job's resident state and the precision form's FP32 copies. Out: back into
+// the pack, and each job's latest energy into E[j].
+__global__ void batch_unpack_kernel(const BatchJob *__restrict__ jobs, const BatchTile *__restrict__ vtiles,
+                                    const int *__restrict__ counts, const long long *__restrict__ off,
+                                    const double *__restrict__ pack) {
+  const int nvtiles = counts[7];
+  for (int t = blockIdx.x; t < nvtiles; t += gridDim.x) {
+    const BatchTile tile = vtiles[t];
+    const BatchJob &J = jobs[tile.job];
+    const double *src = pack + off[tile.job];
+    if ((int)threadIdx.x < tile.count) {
+      const size_t v = (size_t)(tile.first + threadIdx.x);
+      for (int c = 0; c < 3; ++c) {
+        const double x = src[3 * v + c];
+        J.r[3 * v + c] = x;
+        if (J.rhi) store_f32_position(3 * v + c, x, J.rhi, J.rlo, J.r0, J.dsp);
+      }
+    }
+    if (tile.first == 0 && threadIdx.x < 3) {
+      const size_t a = 3 * (size_t)J.f.P.nv + threadIdx.x;
+      J.r[a] = src[a];
+    }
+  }
+}
+
+__global__ void batch_pack_kernel(const BatchJob *__restrict__ jobs, const BatchTile *__restrict__ vtiles,
+                                  const int *__restrict__ counts, const long long *__restrict__ off,
+                                  double *__restrict__ pack, double *__restrict__ E) {
+  const int nvtiles = counts[7];
+  for (int t = blockIdx.x; t < nvtiles; t += gridDim.x) {
+    const BatchTile tile = vtiles[t];
+    const BatchJob &J = jobs[tile.job];
+    double *dst = pack + off[tile.job];
+    if ((int)threadIdx.x < tile.count) {
+      const size_t v = (size_t)(tile.first + threadIdx.x);
+      for (int c = 0; c < 3; ++c) dst[3 * v + c] = J.r[3 * v + c];
+    }
+    if (tile.first == 0 && threadIdx.x < 3) {
+      const size_t a = 3 * (size_t)J.f.P.nv + threadIdx.x;
+      dst[a] = J.r[a];
+    }
+    if (tile.first == 0 && threadIdx.x == 3) E[tile.job] = *J.E;
+  }
+}
+
 // ---------------------------------------------------------------- area, volume
 //
 // One half-warp per face, as in the face pass: lanes are control points while
@@ -2875,6 +2922,18 @@ template cudaError_t launch_batch_gather_step<float>(const BatchJob *, const Bat
 cudaError_t launch_batch_start(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const int *start,
                                const unsigned long long *step0, int grid, cudaStream_t s) {
   dev::batch_start_kernel<<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, start, step0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_unpack(const BatchJob *jobs, const BatchTile *vtiles, const int *counts,
+                                const long long *off, const double *pack, int grid, cudaStream_t s) {
+  dev::batch_unpack_kernel<<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, off, pack);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_pack(const BatchJob *jobs, const BatchTile *vtiles, const int *counts, const long long *off,
+                              double *pack, double *E, int grid, cudaStream_t s) {
+  dev::batch_pack_kernel<<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, off, pack, E);
   return cudaGetLastError();
 }
 
