@@ -357,7 +357,7 @@ def serving_run(ctx, U, W, seconds: float, rate: float, seed: int, tmpdir: Path)
         if d > 0:
             time.sleep(d)
         prm = U.params(kc=U.kc_from_kT(kc), KA=0.215, precision=U.FP32_CENTRED)
-        ids.append(srv.submit(path, prm, W.bd_integrator(seed, len(ids)), 0, steps))
+        ids.append(srv.submit(path, prm, W.bd_integrator(seed, len(ids), WORKLOAD["rms_step_A"]), 0, steps))
     srv.wait_all()
     wall = time.perf_counter() - t0
     st = srv.stats()
@@ -828,7 +828,7 @@ def facepass_mode(args) -> None:
         meshes = [U.Mesh(ctx, plan, prm) for plan, prm in pp]
         batch = U.Batch(ctx, prec, tile_faces=args.tile_faces)
         for i, m in enumerate(meshes):
-            batch.add(m, W.bd_integrator(WORKLOAD["seed"], i), 0, 4)  # live after three steps: the passes do work
+            batch.add(m, W.bd_integrator(WORKLOAD["seed"], i, WORKLOAD["rms_step_A"]), 0, 4)  # live after three steps
         batch.run(3)
         done, st = batch.poll()
         us = _time_passes(ctx, batch.face_pass, args.repeat)

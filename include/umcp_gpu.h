@@ -119,6 +119,16 @@ umcp_status umcp_plan_point_coeffs(const umcp_plan *plan, int face, double u, do
  * positions. Host only. */
 umcp_status umcp_plan_evaluate(const umcp_plan *plan, const double *r, int n, const int *faces, const double *uv,
                                double *R, double *N);
+/* The same evaluation on the device, from a mesh's resident state, at every
+ * face's lattice points (u, v) = (i/plim, j/plim), i + j <= plim (i outer):
+ * R and N (host, 3 doubles per point, N may be NULL) hold the points of face
+ * 0 first, then face 1, ... in the plan's face order. */
+umcp_status umcp_limit_points(umcp_mesh *mesh, int plim, double *R, double *N);
+/* surface::writeLimitingSurface (src/write_structures.C:660-715) of the
+ * resident state: the xyz text the reference writes (a count line, a title
+ * line, "C x y z" per point at %lf) with each face's three corners
+ * (plim = 1), evaluated by umcp_limit_points. */
+umcp_status umcp_write_limiting_surface(umcp_mesh *mesh, const char *path);
 void umcp_plan_destroy(umcp_plan *plan);
 
 /* ---- device context and meshes --------------------------------------- */

@@ -79,3 +79,23 @@ def test_driver_runs_saves_and_resumes(tmp_path):
                          capture_output=True, text=True, timeout=600)
     assert res.returncode == 0 and "Loaded" in res.stdout, res.stderr
     assert (tmp_path / "job2.save").exists()
+
+
+def test_driver_minimizes_first_and_restarts_the_temperature_average(tmp_path):
+    """nmin runs the reference's L-BFGS before the dynamics; nequil restarts
+    AV_TEMP at that outer iteration; kv and planar_topology (inert on the
+    membrane path) are accepted."""
+    inp = tmp_path / "run.inp"
+    params = (GOLDEN / "ico2_plain.params").read_text()
+    inp.write_text(f"mesh {GOLDEN / 'ico2_plain.mesh'}\njobname {tmp_path / 'job'}\n{params}do_ld yes\n"
+                   "time_step 1e-15\ngamma_langevin 10\nnsteps 4\no_lim 3\nseed 9\nnmin 1\nnequil 2\nkv 0.01\n"
+                   "planar_topology no\n")
+    res = subprocess.run([str(UB.HD_EXE), str(inp)], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    assert "minimization 0:" in res.stdout
+    tl = [x.split() for x in res.stdout.splitlines() if x.startswith("t: ")]
+    temp = [float(x[x.index("TEMP:") + 1]) for x in tl]
+    av = [float(x[x.index("AV_TEMP") + 1]) for x in tl]
+    assert len(tl) == 4
+    assert abs(av[1] - (temp[0] + temp[1]) / 2) <= 1e-6 * abs(av[1])
+    assert abs(av[3] - (temp[2] + temp[3]) / 2) <= 1e-6 * abs(av[3])

@@ -204,6 +204,8 @@ _SIGNATURES = {
     "umcp_restraints_get": [_VP, _D, _D, _D],
     "umcp_plan_point_coeffs": [_VP, C.c_int, C.c_double, C.c_double, _I, _D, _I],
     "umcp_plan_evaluate": [_VP, _D, C.c_int, _I, _D, _D, _D],
+    "umcp_limit_points": [_VP, C.c_int, _D, _D],
+    "umcp_write_limiting_surface": [_VP, C.c_char_p],
     "umcp_batch_create": [_VP, C.c_int, C.POINTER(BatchOpts), C.POINTER(_VP)],
     "umcp_batch_destroy": [_VP],
     "umcp_batch_add": [_VP, _VP, C.POINTER(Integrator), C.c_uint64, C.c_int64],
@@ -483,6 +485,21 @@ class Mesh:
         """As energy_grad_device, with all scratch in the library's static device
         array instead of the mesh's own buffers (no allocation at call time)."""
         _check(library().umcp_energy_grad_static(self._h, C.c_void_p(d_r), C.c_void_p(d_E), C.c_void_p(d_g)))
+
+    def limit_points(self, plim: int, normals: bool = True) -> tuple[np.ndarray, np.ndarray | None]:
+        """Limit points (and unit normals) of the resident state at every face's
+        lattice (i/plim, j/plim), i + j <= plim: arrays [faces, points, 3]."""
+        info = self.info()
+        npts = (plim + 1) * (plim + 2) // 2
+        R = np.zeros((info.n_faces, npts, 3))
+        N = np.zeros((info.n_faces, npts, 3)) if normals else None
+        _check(library().umcp_limit_points(self._h, plim, R.ctypes.data_as(_D),
+                                           None if N is None else N.ctypes.data_as(_D)))
+        return R, N
+
+    def write_limiting_surface(self, path) -> None:
+        """The reference's limiting-surface xyz file of the resident state."""
+        _check(library().umcp_write_limiting_surface(self._h, str(path).encode()))
 
     def check_status(self) -> None:
         """Waits for the mesh's queued work; raises UmcpError if a kernel recorded

@@ -445,7 +445,9 @@ extern "C" umcp_status umcp_mesh_create(umcp_ctx *ctx, const umcp_plan *plan, co
     G->nfaces = (int)s.idx.size();
     G->slot_base = slot_base;
     G->irregular = s.irr;
+    G->valence = B.valence;
     G->dudv = s.irr ? 1.0 : 0.5;
+    for (int f : s.idx) G->face_index.push_back(s.irr ? (int)PL.reg_faces.size() + f : f);
     std::vector<uint32_t> cp((size_t)G->nfaces * G->ncp);
     std::vector<double> g0((size_t)G->nfaces * G->npt), rr0((size_t)G->nfaces * G->npt), comp((size_t)G->nfaces * 3);
     for (int q = 0; q < G->nfaces; ++q) {

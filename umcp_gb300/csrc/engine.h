@@ -45,6 +45,8 @@ struct DevBuf {
 
 struct Group {
   int ncp = 0, npt = 0, nfaces = 0, slot_base = 0, irregular = 0;
+  int valence = 6;                  // of the patch type's lowest corner
+  std::vector<int> face_index;      // each face's index in the plan (regular faces, then irregular)
   bool tc = false;                  // regular faces of the precision form on the tensor cores
   int nblocks = 0, block_base = 0;  // persistent face-pass grid and its block-partial rows
   double dudv = 0.5;

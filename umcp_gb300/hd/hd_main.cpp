@@ -8,17 +8,38 @@
 //   mesh FILE          the .mesh file                      (required)
 //   jobname NAME       output prefix (NAME.save)           (default "job")
 //   load FILE          restart file to start from          (src/restart.C format)
-//   nsteps|nouter N    outer iterations, one t: line each  (default 1)
-//   o_lim|ninner N     steps per outer iteration           (default 1)
-//   time_step S        seconds                             (default 1e-13)
-//   gamma_langevin G   friction, per AKMA time unit        (default 10)
+//   nsteps|nouter N    outer iterations, one t: line each  (default 10000)
+//   o_lim|ninner N     steps per outer iteration           (default 10000)
+//   time_step S        seconds (default 1e-3 (2 sqrt(65/pi))^2 / (4 diffc))
+//   diffc D            A^2/s, sets only that default       (default 1e10)
+//   gamma_langevin G   friction, per AKMA time unit        (default 0.001)
 //   do_ld yes|no, do_bd_membrane yes|no                    (Langevin, mass-weighted BD)
-//   seed N, T K, kc, KA, kg, k_reg, lipid ... lines        (as the reference)
+//   seed N             (default: the clock's microseconds)
+//   T K, kc, KA, kg, k_reg, lipid ... lines                (as the reference)
+//   nequil N           the temperature average (AV_TEMP) restarts at outer
+//                      iteration N (src/hd.C:2142-2147; default nsteps / 10)
+// (the defaults are the reference's, src/input.C:16-310)
+//   nmin N             N energy minimizations before the dynamics (the
+//                      reference's L-BFGS, src/hd.C:805-840, src/minimize.C:489)
+//   kv, restrain_volume_inside|outside
+//                      the minimizer's leaflet-volume restraint
+//                      (src/minimize.C:90-112): accepted while it is off;
+//                      with nmin > 0, kv > 0 and restrain_volume_inside or
+//                      _outside on, the run stops with an error (that term
+//                      is not built)
+//   planar_topology    accepted; the reference reads it only for the SRD
+//                      solvent (src/hd.C:123, 625), which is not built
 // Additions of this engine (no reference keyword):
 //   do_bd_overdamped D overdamped BD with diffusion coefficient D (A^2/s)
 //   precision fp64|fp32, mass yes|no (M^-1 from the limit surface for
 //   do_ld/do_bd_membrane, default yes, as hd.C always builds it),
 //   K_area, K_volume   global area/volume restraints (targets: the start state)
+//   ignore_unsupported yes   warn about unsupported keywords instead of stopping
+// Any other keyword of the reference (particles, collisions, output and
+// analysis options, ...) stops the run with an error naming it: the driver
+// runs the membrane path only and does not drop input it cannot honour. So
+// does a run with neither do_ld nor do_bd_membrane (the reference's plain
+// Hamiltonian dynamics with its nequil friction switch, not built here).
 //
 // Output per outer iteration, as the reference prints it (src/hd.C:1896-1899):
 //   t: <ns> ns o: <o> T: <kinetic> V: <potential> T+V: ... TEMP: ... MEM_TEMP: ...
@@ -53,7 +74,14 @@ std::string lower(std::string s) {
   return s;
 }
 
-bool yes(const std::string &v) { return lower(v) == "yes" || v == "1" || lower(v) == "true"; }
+bool yes(const std::string &v) { return lower(v) == "yes" || v == "1" || lower(v) == "true" || lower(v) == "on"; }
+
+// Keywords this driver honours (lower case); "lipid" lines go to the lipid parser.
+const char *const kHandled[] = {"mesh", "jobname", "load", "nsteps", "nouter", "o_lim", "ninner", "time_step",
+                                "gamma_langevin", "do_ld", "do_bd_membrane", "do_bd_overdamped", "seed", "t", "kc",
+                                "ka", "kg", "k_reg", "lipid", "precision", "mass", "k_area", "k_volume", "nequil",
+                                "nmin", "kv", "restrain_volume_inside", "restrain_volume_outside", "planar_topology",
+                                "diffc", "ignore_unsupported"};
 
 int die(const char *what) {
   fprintf(stderr, "hd_gb300: %s: %s\n", what, umcp_last_error());
@@ -99,11 +127,38 @@ int main(int argc, char **argv) {
     fprintf(stderr, "hd_gb300: no mesh keyword\n");
     return 1;
   }
+  {
+    std::string unsupported;
+    for (const auto &e : kv) {
+      bool ok = false;
+      for (const char *h : kHandled) ok = ok || e.first == h;
+      if (!ok) unsupported += (unsupported.empty() ? "" : ", ") + e.first;
+    }
+    if (!unsupported.empty()) {
+      fprintf(stderr, "hd_gb300: keywords outside the membrane path, not built here: %s\n", unsupported.c_str());
+      if (!yes(get("ignore_unsupported", "no"))) return 2;
+    }
+  }
+  if (!yes(get("do_ld", "no")) && !yes(get("do_bd_membrane", "no")) && !kv.count("do_bd_overdamped")) {
+    fprintf(stderr, "hd_gb300: set do_ld yes, do_bd_membrane yes or do_bd_overdamped D: the reference's plain "
+                    "Hamiltonian dynamics (friction only after nequil, no noise) is not built\n");
+    return 2;
+  }
+  const int nmin = atoi(get("nmin", "0").c_str());
+  if (nmin > 0 && atof(get("kv", "0").c_str()) > 0 &&
+      (yes(get("restrain_volume_inside", "no")) || yes(get("restrain_volume_outside", "no")))) {
+    fprintf(stderr, "hd_gb300: the minimizer's leaflet-volume restraint (kv with restrain_volume_inside/outside, "
+                    "src/minimize.C:90-112) is not built\n");
+    return 2;
+  }
   const std::string mesh_path = kv["mesh"], job = get("jobname", "job");
-  const int nouter = atoi(getn({"nsteps", "nouter"}, "1").c_str());
-  const int ninner = atoi(getn({"o_lim", "ninner"}, "1").c_str());
-  const double time_step = atof(get("time_step", "1e-13").c_str());
-  int seed = atoi(get("seed", "1").c_str());
+  const int nouter = atoi(getn({"nsteps", "nouter"}, "10000").c_str());
+  const int ninner = atoi(getn({"o_lim", "ninner"}, "10000").c_str());
+  const int nequil = kv.count("nequil") ? atoi(kv["nequil"].c_str()) : (int)(nouter * 0.1);
+  const double diffc = atof(get("diffc", "1e10").c_str());
+  const double lipid_d = 2.0 * std::sqrt(65.0 / M_PI);
+  const double time_step = kv.count("time_step") ? atof(kv["time_step"].c_str()) : 1e-3 * lipid_d * lipid_d / (4.0 * diffc);
+  int seed = kv.count("seed") ? atoi(kv["seed"].c_str()) : (int)(std::fmod(now_s(), 1.0) * 1e6);
 
   umcp_params prm;
   umcp_params_default(&prm);
@@ -115,7 +170,7 @@ int main(int argc, char **argv) {
   umcp_integrator it{};
   it.time_step = time_step;
   it.seed = (uint64_t)seed;
-  it.gamma = atof(get("gamma_langevin", "10").c_str());
+  it.gamma = atof(get("gamma_langevin", "0.001").c_str());
   it.divergence_threshold = 1e5;
   if (kv.count("do_bd_overdamped")) {
     it.kind = UMCP_OVERDAMPED_BD;
@@ -162,8 +217,16 @@ int main(int argc, char **argv) {
     if (umcp_restraints_set(mesh, &rs) != UMCP_OK) return die("restraints");
   }
 
+  for (int k = 0; k < nmin; ++k) {
+    umcp_minimize_info mi;
+    if (umcp_minimize(mesh, nullptr, nullptr, &mi) != UMCP_OK) return die("minimize");
+    printf("minimization %d: %d iterations, energy %.10le -> %.10le\n", k, mi.iterations, mi.energy_initial,
+           mi.energy_final);
+  }
+
   std::vector<double> r(3 * (size_t)nv + 3), p(3 * (size_t)nv), q(3 * (size_t)nv), e((size_t)std::max(ninner, 1));
   double av_temp = 0, rate = 0;
+  int n_temp = 0;
   const std::string crash = job + "_crash0.save";
   for (int o = 0; o < nouter; ++o) {
     // the line's state: energy terms, kinetic energy p.M^-1 p / 2
@@ -179,9 +242,11 @@ int main(int argc, char **argv) {
       for (size_t i = 0; i < p.size(); ++i) T += 0.5 * p[i] * p[i];
     }
     const double temp = 2 * T / (3.0 * nv - 3.0) / (5.92186663194e-01 / 298.0);
+    if (o == nequil) av_temp = 0, n_temp = 0;  // the average restarts after equilibration
     av_temp += temp;
+    ++n_temp;
     printf("t: %le ns o: %d T: %.8le V: %.12le T+V: %.14le TEMP: %le MEM_TEMP: %le AV_TEMP %le VR: %.3le VMEM: %le VP: %le",
-           o * (double)ninner * time_step * 1e9, o, T, V, T + V, temp, temp, av_temp / (o + 1), terms[2], V, 0.0);
+           o * (double)ninner * time_step * 1e9, o, T, V, T + V, temp, temp, av_temp / n_temp, terms[2], V, 0.0);
     if (rate > 0) printf(" steps/s: %le", rate);
     printf("\n");
     fflush(stdout);

@@ -73,9 +73,36 @@ def vesicle_plans(specs: list[VesicleSpec], tmpdir: Path, precision: int, temper
         return list(ex.map(lambda s: _build_vesicle(s, tmpdir, precision, temperature), specs))
 
 
-def bd_integrator(seed: int, stream: int, rms_step: float = RMS_STEP_A):
+def bd_integrator(seed: int, stream: int, rms_step: float):
     """Overdamped BD with sqrt(2 D dt) = rms_step (time_step 1, D = rms^2/2)."""
     return U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=rms_step * rms_step / 2.0, seed=seed, stream=stream)
+
+
+def hessian_lambda_max(mesh, r: np.ndarray, iters: int = 30, eps: float = 1e-4) -> float:
+    """Largest eigenvalue of the energy's Hessian in the vertex coordinates at
+    state r (kcal/mol/A^2), by power iteration on central differences of the
+    engine's gradient: H v ~ (g(r + eps v) - g(r - eps v)) / (2 eps)."""
+    n = 3 * mesh.nv
+    v = np.random.default_rng(1).normal(size=n)
+    v /= np.linalg.norm(v)
+    lam = 0.0
+    for _ in range(iters):
+        rp, rm = r.copy(), r.copy()
+        rp[:n] += eps * v
+        rm[:n] -= eps * v
+        hv = (mesh.energy_grad(rp)[1][:n] - mesh.energy_grad(rm)[1][:n]) / (2.0 * eps)
+        lam = float(v @ hv)
+        v = hv / np.linalg.norm(hv)
+    return lam
+
+
+def stable_rms_step(lambda_max: float, temperature: float = 298.0) -> float:
+    """The overdamped BD update r += -(D dt/kT) g + sqrt(2 D dt) xi is stable
+    while (D dt/kT) lambda_max < 2 (the stiffest mode's drift overshoots
+    beyond that); this returns the sqrt(2 D dt) that puts it at 1, half the
+    limit: sqrt(2 kT / lambda_max)."""
+    kT = U.KCAL_MOL_PER_KT_298 / 298.0 * temperature
+    return math.sqrt(2.0 * kT / lambda_max)
 
 
 def planar_plan(tmpdir: Path, nx: int, ny: int, seed: int, precision: int, kc_kT: float = 20.0,
