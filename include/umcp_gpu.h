@@ -347,11 +347,22 @@ umcp_status umcp_mesh_energies(umcp_mesh *mesh, double *energies, int64_t n);
  * one face kernel per patch type over all jobs, one per-job energy sum and
  * one fused gather + update. */
 typedef struct umcp_batch umcp_batch;
+/* The face launches' layout: the regular faces' tile size (one block's unit of
+ * work), the irregular faces' tile size and the regular launch's blocks per
+ * SM. With tile_faces 0 the three are chosen by timing the face launches at
+ * the first run (again when the batch has grown fourfold): tile_faces over
+ * multiples of the face kernel's faces per block pass, irregular tiles of 1 to
+ * 8 faces per half-warp, and the occupancy limit or one block fewer. The
+ * choice is keyed by (device, precision, patch types present, log2 of the
+ * face count) and, with tune_cache set, read from and written to that JSON
+ * file, so a later batch of the same kind takes it without timing. The
+ * choice changes how the energy sums are grouped (their last bits), never the
+ * per-vertex gradient sums, so trajectories do not depend on it. */
 typedef struct {
-  int tile_faces;     /* faces per tile of regular faces (one block's unit of work); 0: chosen by timing at the
-                         first run. Irregular faces use tiles of at most 4 faces per half-warp (32 in the FP32
-                         form, 16 in FP64). */
-  int blocks_per_sm;  /* cap on the persistent face grid; 0: the occupancy limit */
+  int tile_faces;     /* faces per regular tile; 0: tuned as above */
+  int blocks_per_sm;  /* cap on the persistent face grids; 0: the occupancy limit (or the tuned value) */
+  int irr_tile_faces; /* faces per irregular tile; 0: 4 per half-warp of the kernel's block (or the tuned value) */
+  const char *tune_cache; /* JSON file of tuned choices, or NULL */
 } umcp_batch_opts;
 typedef struct {
   int n_jobs;
@@ -361,7 +372,9 @@ typedef struct {
   int n_vertex_tiles;
   int tile_faces;
   int kernels_per_step;
-  double tuned_face_ms;            /* the tile timing's best face-pass time (ms), 0 when not tuned */
+  double tuned_face_ms;            /* the best face-pass time of the tuning (ms), 0 when not tuned */
+  int irr_tile_faces;
+  int tune_source;                 /* 0 given by the options, 1 timed, 2 read from the tune cache */
 } umcp_batch_info;
 /* precision: umcp_precision of every job's mesh. opts may be NULL. */
 umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umcp_batch_opts *opts, umcp_batch **out);

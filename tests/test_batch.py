@@ -191,3 +191,36 @@ def test_host_driven_steps_follow_the_resident_run(ctx, precision):
     alone.state_set(r)
     alone.run(its[0], 0, 1)
     assert np.array_equal(out, alone.state_get()[0])
+
+
+def test_tuned_layout_is_cached_and_leaves_trajectories_unchanged(ctx, tmp_path):
+    """The face launches' layout (regular and irregular tile sizes, blocks per
+    SM) is timed at a batch's first run and written to the tune cache; a second
+    batch of the same kind reads it instead of timing. A different layout
+    groups the energy sums differently but the per-vertex gradient sums not at
+    all, so positions are the same bit for bit."""
+    import json
+
+    cache = tmp_path / "tune.json"
+    its = _integrators()
+    runs = []
+    for opts in ({"tune_cache": cache}, {"tune_cache": cache},
+                 {"tile_faces": 128, "irr_tile_faces": 8, "blocks_per_sm": 2}):
+        batch = U.Batch(ctx, U.FP32_CENTRED, **opts)
+        meshes = [_mesh(ctx, n, U.FP32_CENTRED) for n in CASES]
+        for k, m in enumerate(meshes):
+            batch.add(m, its[k], 100 * k, 20)
+        batch.run(20)
+        runs.append((batch.info(), [m.state_get()[0] for m in meshes], [m.energies(20) for m in meshes]))
+    (i1, r1, e1), (i2, r2, e2), (i3, r3, e3) = runs
+    assert i1.tune_source == 1 and i2.tune_source == 2 and i3.tune_source == 0
+    entries = json.loads(cache.read_text())
+    assert len(entries) == 1
+    (key, choice), = entries.items()
+    assert "fp32" in key and choice["tile_faces"] == i1.tile_faces == i2.tile_faces
+    assert choice["irr_tile_faces"] == i1.irr_tile_faces == i2.irr_tile_faces
+    assert (i3.tile_faces, i3.irr_tile_faces, i3.face_grid[0]) == (128, 8, min(i1.face_grid[0], 2 * 152))
+    for a, b, c in zip(r1, r2, r3):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+    for a, c in zip(e1, e3):
+        assert np.max(np.abs(a - c) / np.abs(a)) <= E_TOL[U.FP32_CENTRED]

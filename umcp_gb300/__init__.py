@@ -77,7 +77,8 @@ class Integrator(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("tile_faces", C.c_int), ("blocks_per_sm", C.c_int)]
+    _fields_ = [("tile_faces", C.c_int), ("blocks_per_sm", C.c_int), ("irr_tile_faces", C.c_int),
+                ("tune_cache", C.c_char_p)]
 
 
 class BatchInfo(C.Structure):
@@ -85,6 +86,7 @@ class BatchInfo(C.Structure):
         ("n_jobs", C.c_int), ("n_vertices", C.c_longlong), ("n_faces", C.c_longlong),
         ("n_tiles", C.c_int * 3), ("face_grid", C.c_int * 3), ("n_vertex_tiles", C.c_int),
         ("tile_faces", C.c_int), ("kernels_per_step", C.c_int), ("tuned_face_ms", C.c_double),
+        ("irr_tile_faces", C.c_int), ("tune_source", C.c_int),
     ]
 
 
@@ -607,10 +609,12 @@ class Batch:
     """Many meshes of one context advanced together (umcp_batch_*). Each job
     behaves as Mesh.run(it, step0, n_steps) on its own mesh."""
 
-    def __init__(self, ctx: Context, precision: int = FP64, tile_faces: int = 0, blocks_per_sm: int = 0):
+    def __init__(self, ctx: Context, precision: int = FP64, tile_faces: int = 0, blocks_per_sm: int = 0,
+                 irr_tile_faces: int = 0, tune_cache: str | os.PathLike | None = None):
         self.ctx = ctx  # keep the context alive; a job's mesh leaves the batch when it is destroyed
         self._h = C.c_void_p()
-        opts = BatchOpts(tile_faces, blocks_per_sm)
+        self._cache = str(tune_cache).encode() if tune_cache else None  # keep alive
+        opts = BatchOpts(tile_faces, blocks_per_sm, irr_tile_faces, self._cache)
         _check(library().umcp_batch_create(ctx.handle, precision, C.byref(opts), C.byref(self._h)))
 
     def __del__(self):

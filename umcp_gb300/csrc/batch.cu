@@ -8,9 +8,13 @@
 // vertex tiles, each job's tile list, and a count array that every kernel
 // reads at run time. Membership changes rewrite the tables between runs; the
 // captured steps stay valid until a table outgrows its capacity.
+#include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
 #include <vector>
 
 #include "engine.h"
@@ -40,8 +44,12 @@ struct Job {
 struct umcp_batch {
   umcp_ctx *ctx = nullptr;
   int precision = UMCP_FP64;
-  int opt_tile_faces = 0, opt_blocks_per_sm = 0;
-  int tile_faces = 0;  // chosen at the first run when opt_tile_faces is 0
+  int opt_tile_faces = 0, opt_blocks_per_sm = 0, opt_irr_tile = 0;
+  std::string tune_cache;  // JSON file of tuned choices ("" = none)
+  int tile_faces = 0;      // chosen at the first run when opt_tile_faces is 0
+  int irr_tile = 0;        // faces per irregular tile (0: 4 per half-warp)
+  int max_grid[3] = {0, 0, 0};  // the occupancy-limited persistent grids
+  int tune_source = 0;     // 0 options, 1 timed, 2 tune cache
   double tuned_ms = 0;
   long long tuned_faces = 0;  // faces in the batch when the tile size was last timed
   std::vector<Job> jobs;
@@ -172,7 +180,7 @@ static umcp_status rebuild(umcp_batch *b) {
   const int hw = b->precision == UMCP_FP64 ? dev::FaceCfg<double>::half_warps : dev::FaceCfg<float>::half_warps;
   for (int t = 0; t < kTypes; ++t) {
     b->counts[kCountTileBase + t] = (int)tiles.size();
-    const int tft = t == 0 ? tf : std::min(tf, 4 * hw);
+    const int tft = t == 0 ? tf : (b->irr_tile > 0 ? b->irr_tile : std::min(tf, 4 * hw));
     for (size_t j = 0; j < b->jobs.size(); ++j) {
       const int nf = jt[j].f.src[t].nfaces;
       for (int first = 0; first < nf; first += tft) {
@@ -336,45 +344,158 @@ static umcp_status capture(umcp_batch *b, int steps, cudaGraphExec_t *out) {
   return UMCP_OK;
 }
 
-// Times the face launches (the only tile-size dependent part of a step) for
-// candidate tile sizes and keeps the fastest. Runs on the batch's current
-// jobs after their run start; the face launches change nothing but the
-// gradient-partial slots and tile sums, which every step rewrites.
-static umcp_status autotune(umcp_batch *b) {
+// ---- the face launches' layout, tuned by timing and cached
+
+namespace {
+
+struct Layout {
+  int tile_faces = 0, irr_tile = 0, blocks_per_sm = 0;
+  double face_ms = 0;
+};
+
+// Key of a batch's kind: device, precision, patch types present, log2 of faces.
+std::string layout_key(const umcp_batch *b, long long faces) {
+  cudaDeviceProp prop;
+  std::string dev = cudaGetDeviceProperties(&prop, b->ctx->device) == cudaSuccess ? prop.name : "device";
+  std::string types;
+  for (int t = 0; t < kTypes; ++t)
+    if (b->have_type[t]) types += (types.empty() ? "" : "+") + std::to_string(t == 0 ? 6 : t == 1 ? 5 : 7);
+  const int bucket = faces > 0 ? (int)std::floor(std::log2((double)faces)) : 0;
+  return dev + "|" + (b->precision == UMCP_FP64 ? "fp64" : "fp32") + "|" + types + "|" + std::to_string(bucket);
+}
+
+// The cache file holds one JSON object, {"<key>": {"tile_faces": n,
+// "irr_tile_faces": n, "blocks_per_sm": n, "face_ms": x}, ...}, written by
+// this code only (the reader takes that layout, not general JSON).
+std::map<std::string, Layout> read_layouts(const std::string &path) {
+  std::map<std::string, Layout> out;
+  FILE *f = fopen(path.c_str(), "r");
+  if (!f) return out;
+  std::string text;
+  char buf[4096];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+  fclose(f);
+  size_t p = 0;
+  while ((p = text.find('"', p)) != std::string::npos) {
+    const size_t e = text.find('"', p + 1);
+    if (e == std::string::npos) break;
+    const std::string key = text.substr(p + 1, e - p - 1);
+    const size_t open = text.find('{', e), close = text.find('}', e);
+    if (open == std::string::npos || close == std::string::npos || open > close) break;
+    const std::string body = text.substr(open, close - open);
+    Layout L;
+    auto num = [&](const char *name) {
+      const size_t q = body.find(std::string("\"") + name + "\"");
+      return q == std::string::npos ? 0.0 : atof(body.c_str() + body.find(':', q) + 1);
+    };
+    L.tile_faces = (int)num("tile_faces");
+    L.irr_tile = (int)num("irr_tile_faces");
+    L.blocks_per_sm = (int)num("blocks_per_sm");
+    L.face_ms = num("face_ms");
+    if (L.tile_faces > 0) out[key] = L;
+    p = close + 1;
+  }
+  return out;
+}
+
+void write_layouts(const std::string &path, const std::map<std::string, Layout> &all) {
+  const std::string tmp = path + ".tmp";
+  FILE *f = fopen(tmp.c_str(), "w");
+  if (!f) return;
+  fprintf(f, "{\n");
+  size_t k = 0;
+  for (const auto &e : all)
+    fprintf(f, "  \"%s\": {\"tile_faces\": %d, \"irr_tile_faces\": %d, \"blocks_per_sm\": %d, \"face_ms\": %.6f}%s\n",
+            e.first.c_str(), e.second.tile_faces, e.second.irr_tile, e.second.blocks_per_sm, e.second.face_ms,
+            ++k < all.size() ? "," : "");
+  fprintf(f, "}\n");
+  fclose(f);
+  rename(tmp.c_str(), path.c_str());  // replaces the file whole
+}
+
+}  // namespace
+
+// Puts a layout in place: tiles and grids (the captured steps are re-made).
+static umcp_status apply_layout(umcp_batch *b, const Layout &L) {
+  int sms = 0;
+  UMCP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->ctx->device));
+  b->tile_faces = L.tile_faces;
+  b->irr_tile = L.irr_tile;
+  for (int t = 0; t < kTypes; ++t) {
+    const int cap = t == 0 && L.blocks_per_sm > 0 ? L.blocks_per_sm * sms : b->max_grid[t];
+    b->face_grid[t] = std::max(1, std::min(b->max_grid[t], cap));
+  }
+  b->drop_graphs();
+  return rebuild(b);
+}
+
+static float time_face_launches(umcp_batch *b, cudaEvent_t e0, cudaEvent_t e1, umcp_status *st) {
   cudaStream_t s = b->ctx->stream;
-  // FP64: multiples of the half-warp kernel's faces per pass (8 per block of
-  // 64 threads); FP32: multiples of the thread-per-face kernel's 128, up to
-  // 2048, where the per-warp copy pipeline covers more of each tile.
+  float ms = 0;
+  if (queue_faces(b) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess) { *st = UMCP_ERR_CUDA; return 0; }
+  for (int k = 0; k < 3; ++k)
+    if (queue_faces(b) != cudaSuccess) { *st = UMCP_ERR_CUDA; return 0; }
+  if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+      cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { *st = UMCP_ERR_CUDA; return 0; }
+  return ms / 3;
+}
+
+// Chooses the face launches' layout for the batch's current jobs (after
+// their run start): from the tune cache, else by timing the face launches,
+// which change nothing but the gradient-partial slots and tile sums that
+// every step rewrites. First the regular tile size (multiples of the face
+// kernel's faces per block pass: 8 per FP64 block, 128 per thread-per-face
+// block, up to 2048), then the irregular tile size (1 to 8 faces per
+// half-warp), then the regular launch's blocks per SM (the occupancy limit or
+// one fewer), each with the others held.
+static umcp_status autotune(umcp_batch *b, long long faces) {
+  const std::string key = layout_key(b, faces);
+  std::map<std::string, Layout> cached;
+  if (!b->tune_cache.empty()) {
+    cached = read_layouts(b->tune_cache);
+    auto it = cached.find(key);
+    if (it != cached.end()) {
+      b->tune_source = 2;
+      b->tuned_ms = it->second.face_ms;
+      return apply_layout(b, it->second);
+    }
+  }
   const bool f64 = b->precision == UMCP_FP64;
-  const int hw = f64 ? dev::FaceCfg<double>::half_warps : 32;
+  const int hw = f64 ? dev::FaceCfg<double>::half_warps : dev::FaceCfg<float>::half_warps;
+  int sms = 0;
+  UMCP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->ctx->device));
+  const int max_bps = std::max(1, b->max_grid[0] / std::max(sms, 1));
   cudaEvent_t e0, e1;
   UMCP_CUDA(cudaEventCreate(&e0));
   UMCP_CUDA(cudaEventCreate(&e1));
-  int best = 0;
-  float best_ms = 0;
+  umcp_status st = UMCP_OK;
+  Layout best;
+  auto trial = [&](Layout L) {
+    if (st != UMCP_OK) return;
+    if ((st = apply_layout(b, L)) != UMCP_OK) return;
+    L.face_ms = time_face_launches(b, e0, e1, &st);
+    if (st == UMCP_OK && (best.tile_faces == 0 || L.face_ms < best.face_ms)) best = L;
+  };
+  const int unit = f64 ? dev::FaceCfg<double>::half_warps : 32;
   for (int mult : {1, 2, 4, 8, 16, 32, 64}) {
     if ((f64 && mult > 32) || (!f64 && mult < 4)) continue;
-    b->tile_faces = hw * mult;
-    umcp_status st = rebuild(b);
-    if (st != UMCP_OK) return st;
-    UMCP_CUDA(queue_faces(b));  // warm-up
-    UMCP_CUDA(cudaEventRecord(e0, s));
-    for (int k = 0; k < 3; ++k) UMCP_CUDA(queue_faces(b));
-    UMCP_CUDA(cudaEventRecord(e1, s));
-    UMCP_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    UMCP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    ms /= 3;
-    if (best == 0 || ms < best_ms) {
-      best = b->tile_faces;
-      best_ms = ms;
-    }
+    trial(Layout{unit * mult, 4 * hw, max_bps, 0});
   }
+  if (b->have_type[1] || b->have_type[2])
+    for (int per : {1, 2, 8}) trial(Layout{best.tile_faces, per * hw, best.blocks_per_sm, 0});
+  if (max_bps > 1) trial(Layout{best.tile_faces, best.irr_tile, max_bps - 1, 0});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  b->tile_faces = best;
-  b->tuned_ms = best_ms;
-  return rebuild(b);
+  if (st != UMCP_OK) return st;
+  b->tune_source = 1;
+  b->tuned_ms = best.face_ms;
+  if (!b->tune_cache.empty()) {
+    cached = read_layouts(b->tune_cache);  // as of now: another batch may have written meanwhile
+    cached[key] = best;
+    write_layouts(b->tune_cache, cached);
+  }
+  return apply_layout(b, best);
 }
 
 extern "C" umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umcp_batch_opts *opts,
@@ -391,17 +512,22 @@ extern "C" umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umc
   b->ctx = ctx;
   b->precision = precision;
   if (opts) {
-    if (opts->tile_faces < 0 || opts->blocks_per_sm < 0) return fail(UMCP_ERR_INVALID, "negative batch option");
+    if (opts->tile_faces < 0 || opts->blocks_per_sm < 0 || opts->irr_tile_faces < 0)
+      return fail(UMCP_ERR_INVALID, "negative batch option");
     b->opt_tile_faces = opts->tile_faces;
     b->opt_blocks_per_sm = opts->blocks_per_sm;
+    b->opt_irr_tile = opts->irr_tile_faces;
+    if (opts->tune_cache) b->tune_cache = opts->tune_cache;
   }
   b->tile_faces = b->opt_tile_faces;
+  b->irr_tile = b->opt_irr_tile;
   int sms = 0;
   UMCP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   for (int t = 0; t < kTypes; ++t) {
     const int npt = t == 0 ? 15 : 16;
     int g = precision == UMCP_FP64 ? batch_face_blocks<double>(kTypeNcp[t], npt)
                                    : batch_face_blocks<float>(kTypeNcp[t], npt);
+    b->max_grid[t] = std::max(g, 1);
     if (b->opt_blocks_per_sm > 0) g = std::min(g, b->opt_blocks_per_sm * sms);
     b->face_grid[t] = std::max(g, 1);
   }
@@ -484,12 +610,13 @@ extern "C" umcp_status umcp_batch_run(umcp_batch *b, int n_steps) {
   if ((st = harvest(b)) != UMCP_OK) return st;
   if (b->dirty && (st = rebuild(b)) != UMCP_OK) return st;
   if ((st = start_jobs(b)) != UMCP_OK) return st;
-  // Tile size by timing, at the first run and again whenever the batch has
-  // grown fourfold in faces since (a few times at most over a batch's life).
+  // The face launches' layout (tune cache or timing), at the first run and
+  // again whenever the batch has grown fourfold in faces since (a few times
+  // at most over a batch's life).
   long long faces = 0;
   for (const Job &J : b->jobs) faces += J.m->nfaces;
   if (b->opt_tile_faces == 0 && (b->tile_faces == 0 || faces >= 4 * b->tuned_faces)) {
-    if ((st = autotune(b)) != UMCP_OK) return st;
+    if ((st = autotune(b, faces)) != UMCP_OK) return st;
     b->tuned_faces = faces;
   }
   const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
@@ -556,6 +683,8 @@ extern "C" umcp_status umcp_batch_info_get(const umcp_batch *b, umcp_batch_info 
   info->n_vertex_tiles = b->dirty ? 0 : b->counts[kCountVertexTiles];
   info->tile_faces = b->tile_faces;
   info->tuned_face_ms = b->tuned_ms;
+  info->irr_tile_faces = b->irr_tile;
+  info->tune_source = b->tune_source;
   return UMCP_OK;
 }
 

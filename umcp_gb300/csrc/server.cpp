@@ -314,7 +314,7 @@ extern "C" umcp_status umcp_server_create(umcp_ctx *ctx, const umcp_server_opts 
     if (st != UMCP_OK) return st;
     s->budget = 0.8 * (double)f;
   }
-  umcp_batch_opts bo{s->o.tile_faces, 0};
+  umcp_batch_opts bo{s->o.tile_faces, 0, 0, nullptr};
   umcp_status st = umcp_batch_create(ctx, s->o.precision, &bo, &s->batch);
   if (st != UMCP_OK) return st;
   s->t0 = Clock::now();
