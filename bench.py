@@ -518,7 +518,10 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
             "energy_first_last": [float(e_warm[0]), float(energies[-1])],
             "rms_displacement_A": float(np.sqrt(np.mean((r1[:-3] - r0[:-3]) ** 2))),
             "time_step_akma": dt, "thermal_0p05A_time_step_akma": dt_thermal, "volume_mode_omega_per_akma": omega,
-            "plan_s": t1 - t0, "mass_build_s": t2 - t1, "minv_dense": bool(mi.dense), "minv_nnz": int(mi.nnz_inverse),
+            "plan_s": t1 - t0, "mass_build_s": t2 - t1,
+            "mass_build_split_s": {"assembly": mi.assembly_s, "cholesky_inverse": mi.inverse_s,
+                                   "truncation_and_storage": mi.truncation_s},
+            "minv_dense": bool(mi.dense), "minv_nnz": int(mi.nnz_inverse),
             "minv_fill": mi.nnz_inverse / plan.nv ** 2,
             "minv_apply": {"ms": ms_apply, "bytes": apply_bytes, "gbs": gbs, "hbm_frac": gbs / peak_gbs,
                            "storage": "FP32 values, int32 columns (CSR)" if not mi.dense else "FP32 dense"}}

@@ -246,6 +246,9 @@ typedef struct {
   double mass_per_point;
   long long points, nnz_mass, nnz_inverse;
   int dense;            /* 1: M^-1 kept dense (fill >= 30%), 0: CSR */
+  double assembly_s;    /* wall time of the build: M assembled on the device, */
+  double inverse_s;     /* its Cholesky inverse (potrf + potri), */
+  double truncation_s;  /* symmetrising, truncation and the stored form */
 } umcp_mass_info;
 umcp_status umcp_mass_build(umcp_mesh *mesh, const umcp_plan *plan, const umcp_mass_opts *opts, umcp_mass_info *info);
 /* The installed M^-1 as a dense nv x nv row-major array. Meshes of the

@@ -78,6 +78,12 @@ def test_device_mass_build_matches_reference(name):
     minv = mesh.mass_get()
     assert np.max(np.abs(minv - g["minv"])) <= 1e-10 * np.max(np.abs(g["minv"]))
     assert np.array_equal(minv, minv.T)
+    # M is assembled on the device: its sparsity is the oracle's, the build is
+    # deterministic, and the three phases are timed
+    assert info.nnz_mass == np.count_nonzero(OM.effective_mass(plan))
+    assert min(info.assembly_s, info.inverse_s, info.truncation_s) > 0
+    info2 = mesh.mass_build(plan)
+    assert info2.nnz_mass == info.nnz_mass and np.array_equal(mesh.mass_get(), minv)
 
 
 @pytest.mark.gpu

@@ -111,6 +111,7 @@ class MassInfo(C.Structure):
     _fields_ = [
         ("area0", C.c_double), ("mass_per_point", C.c_double), ("points", C.c_longlong),
         ("nnz_mass", C.c_longlong), ("nnz_inverse", C.c_longlong), ("dense", C.c_int),
+        ("assembly_s", C.c_double), ("inverse_s", C.c_double), ("truncation_s", C.c_double),
     ]
 
 

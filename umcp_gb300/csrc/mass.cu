@@ -1,9 +1,14 @@
 // The limit-surface effective mass and its inverse on the device
 // (getSparseEffectiveMass, src/modes.C:1719-1990), and the M^-1 apply.
 //
-// M is assembled on the host from the mass points (plan.cpp
-// build_effective_mass), expanded to a dense FP64 matrix on the device,
-// factorised and inverted there (Cholesky: potrf + potri, as the reference
+// M is assembled on the device, directly as a dense FP64 matrix: every mass
+// point of a face is a combination of the face's control points with weights
+// that depend on the patch type only, so the 66 points of a face give one
+// block per patch type (plan.cpp face_mass_block), which each face adds at
+// its control points. Each row's thread adds the blocks of its vertex's
+// (face, control point) incidences in their fixed order, so M is
+// deterministic and no float atomics are used. It is then factorised and
+// inverted there (Cholesky: potrf + potri, as the reference
 // does with LAPACK), symmetrised and truncated at the reference's relative
 // tolerance (|M^-1_ij| / sqrt(|M^-1_ii M^-1_jj|) > rel_tol, src/modes.C:1893).
 // The reference's tolerance of 1e-20 keeps every entry, so M^-1 stays dense
@@ -17,6 +22,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -67,10 +73,49 @@ const Solver &solver() {
   return s;
 }
 
-__global__ void csr_to_dense_kernel(int n, const int *__restrict__ row_ptr, const int *__restrict__ col,
-                                    const double *__restrict__ val, double *__restrict__ A) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) A[(size_t)i * n + col[k]] = val[k];
+// The face groups of a mesh for the assembly: control points and the group's
+// face block (ncp x ncp, row-major).
+struct MassGroups {
+  const uint32_t *cp[3];
+  const double *block[3];
+  int ncp[3];
+};
+
+// owner[slot] = group << 30 | face << 4 | control point, for every
+// gradient-partial slot of the group (slots are one per (face, control point)).
+__global__ void slot_owner_kernel(int nfaces, int ncp, int group, const int *__restrict__ dest,
+                                  unsigned *__restrict__ owner) {
+  const int total = nfaces * ncp;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    owner[dest[t]] = ((unsigned)group << 30) | ((unsigned)(t / ncp) << 4) | (unsigned)(t % ncp);
+}
+
+// Row r of M: the rows of the face blocks of r's incidences, in slot order
+// (ascending (face, control point)), added into A[r][.]: each row is one
+// thread's, so the sums have a fixed order and nothing races.
+__global__ void mass_assemble_kernel(int n, const int *__restrict__ off, const unsigned *__restrict__ owner,
+                                     MassGroups G, double *__restrict__ A) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const int base = off[2 * r], cnt = off[2 * r + 1];
+    double *row = A + (size_t)r * n;
+    for (int k = 0; k < cnt; ++k) {
+      const unsigned o = owner[base + 32 * k];
+      const int g = (int)(o >> 30), f = (int)((o >> 4) & ((1u << 26) - 1)), a = (int)(o & 15u);
+      const int N = G.ncp[g];
+      const uint32_t *cp = G.cp[g] + (size_t)f * N;
+      const double *B = G.block[g] + (size_t)a * N;
+      for (int b = 0; b < N; ++b) row[cp[b] & dev::kVertexMask] += B[b];
+    }
+  }
+}
+
+// Nonzero entries of the dense n x n matrix.
+__global__ void count_nonzero_kernel(size_t total, const double *__restrict__ A, unsigned long long *__restrict__ cnt) {
+  unsigned long long c = 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    c += A[e] != 0.0;
+  for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
 }
 
 // potri with the lower triangle (column-major) leaves the inverse in the
@@ -295,22 +340,42 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
   const Solver &S = solver();
   if (!S.ok()) return fail(UMCP_ERR_UNSUPPORTED, "cuSOLVER (dense Cholesky) is not available on this host");
 
-  EffectiveMass EM;
-  build_effective_mass(P, n, o.mass_scale, o.points_per_edge, &EM);
+  if (m->groups.size() > 3 || m->nfaces >= (1 << 26)) return fail(UMCP_ERR_UNSUPPORTED, "mesh too large for the mass assembly");
+  const auto t_start = std::chrono::steady_clock::now();
+  const MassPoints MP = mass_points(P, o.mass_scale, o.points_per_edge);
 
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
   cudaStream_t s = m->ctx->stream;
   UMCP_CUDA(cudaStreamSynchronize(s));  // queued steps may still read the previous M^-1
   m->drop_graphs();
-  DevBuf A, drow, dcol, dval, work, dinfo, dkept;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
+  DevBuf A, owner, blocks[3], work, dinfo, dkept, dnnz;
   UMCP_CUDA(A.alloc((size_t)n * n * sizeof(double)));
   UMCP_CUDA(cudaMemsetAsync(A.p, 0, A.bytes, s));
-  UMCP_CUDA(upload(drow, EM.row_ptr));
-  UMCP_CUDA(upload(dcol, EM.col));
-  UMCP_CUDA(upload(dval, EM.val));
-  csr_to_dense_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, drow.as<int>(), dcol.as<int>(), dval.as<double>(),
-                                                      A.as<double>());
+  UMCP_CUDA(owner.alloc((size_t)std::max(m->nslot_cap, 1) * sizeof(unsigned)));
+  MassGroups MG{};
+  for (size_t g = 0; g < m->groups.size(); ++g) {
+    const Group &G = *m->groups[g];
+    std::vector<double> B((size_t)G.ncp * G.ncp);
+    face_mass_block(G.valence, G.ncp, o.points_per_edge, MP.mass_per_point, B.data());
+    UMCP_CUDA(upload(blocks[g], B));
+    MG.cp[g] = G.cp.as<uint32_t>();
+    MG.block[g] = blocks[g].as<double>();
+    MG.ncp[g] = G.ncp;
+    if (G.nfaces)
+      slot_owner_kernel<<<sms * 4, 256, 0, s>>>(G.nfaces, G.ncp, (int)g, G.dest.as<int>(), owner.as<unsigned>());
+  }
+  mass_assemble_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, m->off.as<int>(), owner.as<unsigned>(), MG, A.as<double>());
   UMCP_CUDA(cudaGetLastError());
+  UMCP_CUDA(dnnz.alloc(sizeof(unsigned long long)));
+  UMCP_CUDA(cudaMemsetAsync(dnnz.p, 0, sizeof(unsigned long long), s));
+  count_nonzero_kernel<<<sms * 8, 256, 0, s>>>((size_t)n * n, A.as<double>(), dnnz.as<unsigned long long>());
+  UMCP_CUDA(cudaGetLastError());
+  unsigned long long nnz_mass = 0;
+  UMCP_CUDA(cudaMemcpyAsync(&nnz_mass, dnnz.p, sizeof nnz_mass, cudaMemcpyDeviceToHost, s));
+  UMCP_CUDA(cudaStreamSynchronize(s));
+  const auto t_assembled = std::chrono::steady_clock::now();
 
   void *h = nullptr;
   if (S.create(&h) != 0) return fail(UMCP_ERR_CUDA, "cusolverDnCreate failed");
@@ -337,8 +402,7 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
   UMCP_CUDA(cudaMemcpyAsync(&hinfo, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   UMCP_CUDA(cudaStreamSynchronize(s));
   if (hinfo != 0) return fail(UMCP_ERR_INVALID, "effective mass matrix could not be inverted");
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->ctx->device);
+  const auto t_inverted = std::chrono::steady_clock::now();
   symmetrize_kernel<<<sms * 8, 256, 0, s>>>(n, A.as<double>());
   UMCP_CUDA(cudaGetLastError());
   UMCP_CUDA(dkept.alloc(sizeof(unsigned long long)));
@@ -397,13 +461,20 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
   UMCP_CUDA(m->min32.alloc(f32 ? (size_t)n * sizeof(float4) : 0));
   m->mrows = n;
   if (info) {
+    const auto t_end = std::chrono::steady_clock::now();
+    auto sec = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::chrono::duration<double>(b - a).count();
+    };
     memset(info, 0, sizeof(*info));
-    info->area0 = EM.area0;
-    info->mass_per_point = EM.mass_per_point;
-    info->points = EM.points;
-    info->nnz_mass = (long long)EM.val.size();
+    info->area0 = MP.area0;
+    info->mass_per_point = MP.mass_per_point;
+    info->points = MP.points;
+    info->nnz_mass = (long long)nnz_mass;
     info->nnz_inverse = (long long)kept;
     info->dense = m->mass_dense ? 1 : 0;
+    info->assembly_s = sec(t_start, t_assembled);
+    info->inverse_s = sec(t_assembled, t_inverted);
+    info->truncation_s = sec(t_inverted, t_end);
   }
   return UMCP_OK;
 }

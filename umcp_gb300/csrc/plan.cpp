@@ -522,7 +522,7 @@ int limit_point_rows(const Face &f, double u, double v, IrregularMap *maps[8], d
   return N;
 }
 
-void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, EffectiveMass *out) {
+MassPoints mass_points(const Plan &p, double mass_scale, int plim) {
   // Mass per point (src/hd.C:442-452): a lipid mass of 760.09 g/mol (POPC)
   // times mass_scale, spread over area0 at 65.35 A^2 per lipid and two
   // leaflets. area0 is surface::area's: 0.5 g0 w over the regular faces'
@@ -537,47 +537,27 @@ void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, Ef
   const double amu_per_kg = 1.0 / 1.661e-27;
   const double mass_per_lipid = mass_scale * 1000 * 760.09 / 6.022e23 / 1000;
   const size_t nfaces = p.reg_faces.size() + p.irr_faces.size();
-  const double m = amu_per_kg * 2 * area0 / (double)nfaces / ppf * mass_per_lipid / 65.35;
-  out->area0 = area0;
-  out->mass_per_point = m;
-  out->points = (long long)ppf * (long long)nfaces;
+  MassPoints out;
+  out.area0 = area0;
+  out.mass_per_point = amu_per_kg * 2 * area0 / (double)nfaces / ppf * mass_per_lipid / 65.35;
+  out.points = (long long)ppf * (long long)nfaces;
+  return out;
+}
 
+void face_mass_block(int valence, int ncp, int plim, double m, double *B) {
   IrregularMap map5(5), map7(7);
   IrregularMap *maps[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, &map5, nullptr, &map7};
-  // Per face: B = m sum_points c c^T over its control points (every point of
-  // a face is a combination of the face's own control points), then scattered.
-  struct Entry { int r, c; double v; };
-  std::vector<Entry> ent;
-  ent.reserve(nfaces * 144);
-  auto face_block = [&](const Face &f) {
-    const int N = f.ncp;
-    double B[kMaxCp][kMaxCp] = {};
-    double c[kMaxCp];
-    for (int fi = 0; fi <= plim; ++fi)
-      for (int fj = 0; fj <= plim - fi; ++fj) {
-        limit_point_coeffs(f, fi / (double)plim, fj / (double)plim, maps, c);
-        for (int a = 0; a < N; ++a)
-          for (int b = 0; b < N; ++b) B[a][b] += c[a] * c[b] * m;
-      }
-    for (int a = 0; a < N; ++a)
-      for (int b = 0; b < N; ++b) ent.push_back({f.cp[a], f.cp[b], B[a][b]});
-  };
-  for (const Face &f : p.reg_faces) face_block(f);
-  for (const Face &f : p.irr_faces) face_block(f);
-  std::sort(ent.begin(), ent.end(), [](const Entry &x, const Entry &y) { return x.r != y.r ? x.r < y.r : x.c < y.c; });
-  out->row_ptr.assign((size_t)nv + 1, 0);
-  out->col.clear();
-  out->val.clear();
-  for (size_t i = 0; i < ent.size();) {
-    size_t j = i;
-    double s = 0.0;
-    while (j < ent.size() && ent[j].r == ent[i].r && ent[j].c == ent[i].c) s += ent[j++].v;
-    out->col.push_back(ent[i].c);
-    out->val.push_back(s);
-    out->row_ptr[(size_t)ent[i].r + 1]++;
-    i = j;
-  }
-  for (int r = 0; r < nv; ++r) out->row_ptr[(size_t)r + 1] += out->row_ptr[r];
+  Face f{};
+  f.valence = valence;
+  f.ncp = ncp;
+  for (int a = 0; a < ncp * ncp; ++a) B[a] = 0.0;
+  double c[kMaxCp];
+  for (int fi = 0; fi <= plim; ++fi)
+    for (int fj = 0; fj <= plim - fi; ++fj) {
+      limit_point_coeffs(f, fi / (double)plim, fj / (double)plim, maps, c);
+      for (int a = 0; a < ncp; ++a)
+        for (int b = 0; b < ncp; ++b) B[a * ncp + b] += c[a] * c[b] * m;
+    }
 }
 
 // ------------------------------------------------------------ lipids

@@ -93,13 +93,17 @@ int limit_point_rows(const Face &f, double u, double v, IrregularMap *maps[8], d
 // Effective mass of the limit surface (getSparseEffectiveMass,
 // src/modes.C:1735-1740): M = sum over mass points k of m c_k c_k^T, with the
 // (plim+1)(plim+2)/2 points per face and the mass per point of src/hd.C:417-452.
-struct EffectiveMass {
+// Every mass point of a face is a combination of the face's own control
+// points with weights that depend on the patch type only, so M is the sum
+// over faces of one block per patch type placed at the face's control points.
+struct MassPoints {
   double area0 = 0, mass_per_point = 0;
   long long points = 0;
-  std::vector<int> row_ptr, col;  // CSR of M over vertices, columns ascending
-  std::vector<double> val;
 };
-void build_effective_mass(const Plan &p, int nv, double mass_scale, int plim, EffectiveMass *out);
+MassPoints mass_points(const Plan &p, double mass_scale, int plim);
+// B[a*ncp + b] = m sum over a face's points of c_a c_b, for the patch type of
+// a corner of this valence (6: regular, ncp 12).
+void face_mass_block(int valence, int ncp, int plim, double m, double *B);
 
 // Parses the lipid directives of an input file ("lipid library NAME APL c0",
 // "lipid outer NAME parts", "lipid inner NAME parts"; src/lipid_composition.C:47-300).
