@@ -82,10 +82,10 @@ L2_BYTES = 129 * 1024 * 1024
 SM_COUNT, FP32_LANES_PER_SM = 152, 128
 # DRAM bytes per face of the batched face launches, from the ncu capture of
 # the first 64 vesicles of the workload at 512-face tiles (dram__bytes_read.sum
-# + dram__bytes_write.sum of the regular and valence-5 launches: 108.47 +
-# 28.08 + 2.18 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
+# + dram__bytes_write.sum of the regular and valence-5 launches: 87.30 +
+# 25.41 + 2.79 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
 # from it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 138.74e6 / 392960
+BATCH_FACE_DRAM_BYTES_PER_FACE = 115.51e6 / 392960
 
 
 def parse_args():
@@ -205,19 +205,23 @@ def face_pass_work(plans, esize: int) -> tuple[float, float, int]:
     control points and their slot destinations (2 x 4c), its gradient
     partials (3c x esize), g0 and the reference angle per point (2q x esize)
     and its composition (3 x esize); per vertex its position once (hi/lo
-    pairs, 24 B in the FP32 form; 24 B of FP64 in the plain path).
+    pairs, 24 B in the FP32 form; 24 B of FP64 in the plain path) and, in the
+    FP32 form, its displacement from the reference state (12 B).
     Flops per quadrature point: the five basis contractions over the c control
     points (5 x 3c FMA), the same contracted back onto them, and about 190
-    for the pointwise energy and adjoint.
+    for the pointwise energy and adjoint; in the FP32 form also the u and v
+    rows contracted with the displacements (2 x 3c FMA) and about 30 for the
+    area strain formed from them.
     """
+    strain = esize == 4
     byts = flops = 0.0
     faces = 0
     for pi in plans:
         for nf, c, q in ((pi.n_regular, 12, 15), (pi.n_irregular, 11, 16)):
             byts += nf * (8 * c + 3 * c * esize + 2 * q * esize + 3 * esize)
-            flops += nf * q * (2 * 2 * 5 * 3 * c + 190)
+            flops += nf * q * (2 * 2 * 5 * 3 * c + 190 + (2 * 2 * 3 * c + 30 if strain else 0))
             faces += nf
-        byts += 24.0 * pi.nv
+        byts += (36.0 if strain else 24.0) * pi.nv
     return byts, flops, faces
 
 
@@ -593,7 +597,8 @@ def engine_arm(args) -> None:
         "config": workload_config(specs),
         "engine": {"parallelism": f"replicas x{world}" if world > 1 else "one GPU", "tile_faces": info.tile_faces,
                    "face_grid": list(info.face_grid)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "roofline": {"bound": "hbm", "limiter": "FP32 instruction issue (see compute): the HBM fraction is "
+                     "small by design, the face work is ~40 flop per byte", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"],
                      "traffic": (BATCH_FACE_DRAM_BYTES_PER_FACE * nfaces) if BATCH_FACE_DRAM_BYTES_PER_FACE else None,
                      "kernel": "batch_face_tpf_kernel (regular faces) and batch_face_kernel (valence-5 and "
