@@ -122,10 +122,15 @@ __device__ __forceinline__ float qdiv(float a, float, float ib) { return a * ib;
 // leave every tangent's rounding in the strain: at and near the reference
 // state that rounding is the whole area force, on coarse patches up to 1e-5
 // of the gradient.
+// lkn, mo (optional): the scalars lb, kb, nb and the normal m with
+// Kb[2] = lb m, Kb[3] = kb m, Kb[4] = nb m, for a caller that contracts the
+// three second-derivative rows as one scalar per control point times m
+// (inlined: the Kb[2..4] it does not read are never formed).
 template <typename T, bool KG_REG = true>
 __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T rr0, T dudv, T P2, T Hbar, T Pres,
                                               T kc, T KA, T kg, T k_reg, T *ea, T *ec, T *er, Vec3<T> Kb[5],
-                                              Vec3<T> Kreg[2], const Vec3<T> *dR = nullptr) {
+                                              Vec3<T> Kreg[2], const Vec3<T> *dR = nullptr, T *lkn = nullptr,
+                                              Vec3<T> *mo = nullptr) {
   const Vec3<T> &Ru = K[0], &Rv = K[1], &Suu = K[2], &Suv = K[3], &Svv = K[4];
   Vec3<T> m = cross(Ru, Rv);
   T W = dot(m, m);
@@ -202,6 +207,12 @@ __device__ __forceinline__ void point_adjoint(const Vec3<T> K[5], T w, T g0, T r
     E12b = T(-2) * Tb * k + rE12;
     E22b = Tb * l + rE22;
   }
+  if (lkn) {
+    lkn[0] = lb;
+    lkn[1] = kb;
+    lkn[2] = nb;
+  }
+  if (mo) *mo = m;
   Kb[2] = {lb * m.x, lb * m.y, lb * m.z};
   Kb[3] = {kb * m.x, kb * m.y, kb * m.z};
   Kb[4] = {nb * m.x, nb * m.y, nb * m.z};

@@ -1359,17 +1359,18 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
 //
 // Regular faces of the precision form (12 control points, 15 quadrature
 // points), one face per thread. The thread keeps its face's centred control
-// points X[12][3] and gradient sums G[12][3] in registers and walks the 15
-// points; every thread of a warp reads the same basis row at the same time,
-// so the basis comes out of shared memory as broadcasts (one wavefront per
-// float4) and both contractions are plain multiply-adds on registers:
+// points X[12][3] (and their displacements from the reference state) in its
+// own columns of shared memory, its gradient sums G[12][3] in registers, and
+// walks the 15 points; every thread of a warp reads the same basis row at the
+// same time, so the basis comes out of shared memory as broadcasts (one
+// wavefront per float4) and both contractions are plain multiply-adds:
 //   K[k]_c = sum_j B[p][k][j] X[j]_c          (Ru, Rv, Suu, Suv, Svv)
-//   G[j]_c += sum_k B[p][k][j] Kb[k]_c        (Kb = dE/dK from point_adjoint)
-// Nothing goes through shared memory per face and nothing is shuffled, which
-// removes the transposes and shared-memory traffic of the half-warp form;
-// the FP32 multiply-add pipe is the remaining bound. Energy terms and
-// dE/dalpha are Kahan-summed per thread over its faces and reduced once at
-// the end, in a fixed order.
+//   G[j]_c += B[p][u][j] Kb[u]_c + B[p][v][j] Kb[v]_c + s[j] m_c,
+//   s[j] = B[p][uu][j] lb + B[p][uv][j] kb + B[p][vv][j] nb
+// (the adjoints of Suu, Suv, Svv are lb m, kb m, nb m: one scalar per control
+// point times the normal instead of three vector rows). Nothing is shuffled
+// or transposed per face. Energy terms and dE/dalpha are Kahan-summed per
+// thread over its faces and reduced once at the end, in a fixed order.
 namespace tpf {
 constexpr int kNcp = 12, kNpt = 15, kNc4 = 3;
 constexpr int kThreads = 128, kWarps = kThreads / 32, kMinBlocks = 3;
@@ -1384,6 +1385,7 @@ struct Smem {
   float W[kNpt];
   double red[kWarps][6];
 };
+constexpr size_t kSumBytes = sizeof(float) * 12 * kThreads;  // per-thread Kahan totals (dynamic shared memory)
 // Thread-private float4 in shared memory, stored and loaded through volatile
 // asm so the compiler re-reads it instead of keeping the stored registers
 // alive across the point loop (which is the register pressure this layout
@@ -1399,48 +1401,7 @@ __device__ __forceinline__ float4 ld4(const float4 *p) {
                : "r"((uint32_t)__cvta_generic_to_shared(p)));
   return v;
 }
-
-// One warp's 32 faces of face tables, copied into shared memory ahead of use
-// with coalesced 16-byte asynchronous copies (the per-point g0 rows are 60
-// bytes apart per face, so direct per-thread loads touch a sector per
-// thread). Row r of face lane: cp[12 lane ..], g0[15 lane + p]. The
-// composition (read once per face) and the reference angles (read only when
-// k_reg or kg is set) are read from global memory directly.
-struct Stage {
-  uint4 cp[32 * kNcp / 4];
-  float g0[32 * kNpt];
-};
-constexpr size_t kStageBytes = sizeof(Stage) * 2 * kWarps;  // double-buffered per warp (dynamic shared memory)
-constexpr size_t kSumBytes = sizeof(float) * 12 * kThreads;    // per-thread Kahan totals (after the stages)
-constexpr int kPrefetchPoint = 7;  // point after which the next faces' positions are prefetched
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src, int bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-               "l"(__cvta_generic_to_global(src)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.L1 [%0];" ::"l"(p)); }
-__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
-
-// bytes from src to dst, 16 per lane per round; a short last chunk reads only
-// its own bytes (the rest of the 16 is zero-filled).
-__device__ __forceinline__ void stage_rows(void *dst, const void *src, int bytes, int lane) {
-  for (int o = 16 * lane; o < bytes; o += 512)
-    cp_async16(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, min(16, bytes - o));
-}
-// Queue the copies of faces f0 .. f0 + n - 1 (n <= 32). Needs f0 % 4 == 0 and
-// 16-byte aligned tables (stage_ok).
-__device__ __forceinline__ void stage_issue(Stage &st, const FaceSrc &S, int f0, int n, int lane) {
-  stage_rows(st.cp, S.cp + (size_t)f0 * kNcp, n * kNcp * 4, lane);
-  stage_rows(st.g0, S.g0f + (size_t)f0 * kNpt, n * kNpt * 4, lane);
-  if (lane < kNcp) prefetch_l2(S.dest + (size_t)f0 * kNcp + 32 * lane);  // read at the faces' end
-  if (lane < 3) prefetch_l2(S.compf + (size_t)f0 * 3 + 32 * lane);
-}
+__device__ __forceinline__ float2 dup(float x) { return make_float2(x, x); }
 }  // namespace tpf
 
 __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, const double *weight) {
@@ -1451,26 +1412,16 @@ __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, co
 
 // Face f's energy terms and dE/dalpha; writes its alpha-scaled gradient
 // partials to the face's slots. vec: cp and dest are 16-byte aligned.
-// STAGED: the face's control points and g0 come from cur (row lane) instead of
-// global memory; with next given, the next faces' control-point positions are
-// prefetched into L1 half-way through (every lane of the warp is active then).
 // am1 = alpha - 1 (formed in FP64): the box scales' part of the change from
 // the reference state.
-template <bool STAGED, bool KG_REG>
+template <bool KG_REG>
 __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
                                          const float alpha[3], const float ialpha[3], const float am1[3],
                                          const Moduli<float> &mod, float dudv, bool vec, float *__restrict__ partial,
-                                         float e3[3], float da[3], const tpf::Stage *cur = nullptr,
-                                         const tpf::Stage *next = nullptr, int lane = 0) {
+                                         float e3[3], float da[3]) {
   using namespace tpf;
   uint32_t cp[kNcp];
-  if constexpr (STAGED) {
-#pragma unroll
-    for (int i = 0; i < kNc4; ++i) {
-      const uint4 v = cur->cp[kNc4 * lane + i];
-      cp[4 * i] = v.x; cp[4 * i + 1] = v.y; cp[4 * i + 2] = v.z; cp[4 * i + 3] = v.w;
-    }
-  } else if (vec) {
+  if (vec) {
     const uint4 *q = reinterpret_cast<const uint4 *>(S.cp + (size_t)f * kNcp);
 #pragma unroll
     for (int i = 0; i < kNc4; ++i) {
@@ -1506,15 +1457,23 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     for (int jj = 0; jj < 4; ++jj) {
       const int j = 4 * c4 + jj;
       const int v = (int)(cp[j] & kVertexMask), code = (int)(cp[j] >> kVertexBits);
-      float hi[3], lo[3], dv[3], sh[3] = {0.f, 0.f, 0.f}, she[3] = {0.f, 0.f, 0.f}, shl[3] = {0.f, 0.f, 0.f};
+      float hi[3], lo[3], dv[3], l[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         hi[c] = __ldg(&S.rhi[3 * (size_t)v + c]);
         lo[c] = __ldg(&S.rlo[3 * (size_t)v + c]);
         dv[c] = __ldg(&S.dsp[3 * (size_t)v + c]);
       }
-      if (code != 13) {  // a periodic image: the lattice shift as hi + lo (each term exact)
+      if (code == 13) {  // the home image (every control point of a closed vesicle)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float s2, e2;
+          two_sum(hi[c], -ahi[c], s2, e2);
+          l[c] = s2 + (e2 + (lo[c] - alo[c]));
+        }
+      } else {  // a periodic image: the lattice shift as hi + lo (each term exact)
         const int img[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+        float sh[3] = {0.f, 0.f, 0.f}, she[3] = {0.f, 0.f, 0.f}, shl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -1525,15 +1484,18 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
             she[c] += e;
             shl[c] += (float)img[d] * P.box_lo[d][c];
           }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float s1, e1, s2, e2;
+          two_sum(hi[c], sh[c], s1, e1);
+          two_sum(s1, -ahi[c], s2, e2);
+          l[c] = s2 + ((e1 + e2) + ((lo[c] - alo[c]) + (she[c] + shl[c])));
+        }
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float s1, e1, s2, e2;
-        two_sum(hi[c], sh[c], s1, e1);
-        two_sum(s1, -ahi[c], s2, e2);
-        const float l = s2 + ((e1 + e2) + ((lo[c] - alo[c]) + (she[c] + shl[c])));
-        X[jj][c] = alpha[c] * l;
-        Dx[jj][c] = fmaf(am1[c], l, dv[c] - ad[c]);
+        X[jj][c] = alpha[c] * l[c];
+        Dx[jj][c] = fmaf(am1[c], l[c], dv[c] - ad[c]);
       }
     }
 #pragma unroll
@@ -1549,28 +1511,8 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
   float ea = 0.f, ec = 0.f, er = 0.f, dax = 0.f, day = 0.f, daz = 0.f;
 #pragma unroll 1
   for (int p = 0; p < kNpt; ++p) {
-    float g0, rr0 = 0.f;
-    if constexpr (STAGED) {
-      g0 = cur->g0[kNpt * lane + p];
-      if (next && p == kPrefetchPoint) {
-        cp_async_wait<0>();  // the next faces' tables (queued when these faces started) have landed
-        __syncwarp();
-#pragma unroll
-        for (int i = 0; i < kNc4; ++i) {
-          const uint4 v = next->cp[kNc4 * lane + i];
-          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const size_t o = 3 * (size_t)(w[e] & kVertexMask);
-            prefetch_l1(S.rhi + o);
-            prefetch_l1(S.rlo + o);
-            prefetch_l1(S.dsp + o);
-          }
-        }
-      }
-    } else {
-      g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]);
-    }
+    const float g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]);
+    float rr0 = 0.f;
     if constexpr (KG_REG) rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
     // K[k]_c as two partial sums (even, odd control points) in one pair; the
     // u and v rows also over the displacements (dR, the tangents' change
@@ -1608,30 +1550,46 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     for (int k = 0; k < 5; ++k) K[k] = {A[k][0].x + A[k][0].y, A[k][1].x + A[k][1].y, A[k][2].x + A[k][2].y};
 #pragma unroll
     for (int k = 0; k < 2; ++k) dR[k] = {Ad[k][0].x + Ad[k][0].y, Ad[k][1].x + Ad[k][1].y, Ad[k][2].x + Ad[k][2].y};
-    Vec3<float> Kb[5], Kreg[2];
-    float a, c, r;
+    Vec3<float> Kb[5], Kreg[2], m;
+    float a, c, r, lkn[3];
     point_adjoint<float, KG_REG>(K, sm.W[p], g0, rr0, dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg, &a,
-                                 &c, &r, Kb, Kreg, dR);
+                                 &c, &r, Kb, Kreg, dR, lkn, &m);
     ea += a;
     ec += c;
     er += r;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      dax = fmaf(Kb[k].x, K[k].x, dax); day = fmaf(Kb[k].y, K[k].y, day); daz = fmaf(Kb[k].z, K[k].z, daz);
+    // alpha_c dE/dalpha_c over this point: sum_k Kb[k]_c K[k]_c, with Kb[2..4] = (lb, kb, nb) m
+    {
+      const float t[3] = {lkn[0] * K[2].x + lkn[1] * K[3].x + lkn[2] * K[4].x,
+                          lkn[0] * K[2].y + lkn[1] * K[3].y + lkn[2] * K[4].y,
+                          lkn[0] * K[2].z + lkn[1] * K[3].z + lkn[2] * K[4].z};
+      dax = fmaf(Kb[0].x, K[0].x, fmaf(Kb[1].x, K[1].x, fmaf(m.x, t[0], dax)));
+      day = fmaf(Kb[0].y, K[0].y, fmaf(Kb[1].y, K[1].y, fmaf(m.y, t[1], day)));
+      daz = fmaf(Kb[0].z, K[0].z, fmaf(Kb[1].z, K[1].z, fmaf(m.z, t[2], daz)));
     }
-    // G[j]_c += sum_k B[p][k][j] Kb[k]_c, control points j, j + 1 in one pair
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      const float2 kd[3] = {make_float2(Kb[k].x, Kb[k].x), make_float2(Kb[k].y, Kb[k].y),
-                            make_float2(Kb[k].z, Kb[k].z)};
+    // G[j]_c += B[u][j] Kb[u]_c + B[v][j] Kb[v]_c + s[j] m_c, control points j, j + 1 in one pair
+    {
+      const float2 ku[3] = {dup(Kb[0].x), dup(Kb[0].y), dup(Kb[0].z)};
+      const float2 kv[3] = {dup(Kb[1].x), dup(Kb[1].y), dup(Kb[1].z)};
+      const float2 md[3] = {dup(m.x), dup(m.y), dup(m.z)};
+      const float2 lb = dup(lkn[0]), kb = dup(lkn[1]), nb = dup(lkn[2]);
 #pragma unroll
       for (int c4 = 0; c4 < kNc4; ++c4) {
-        const Q4<float> b = sm.B[p][k][c4];
-        const float2 b01 = make_float2(b.x, b.y), b23 = make_float2(b.z, b.w);
+        const Q4<float> bu = sm.B[p][0][c4], bv = sm.B[p][1][c4], buu = sm.B[p][2][c4], buv = sm.B[p][3][c4],
+                        bvv = sm.B[p][4][c4];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          G2[2 * c4][c] = __ffma2_rn(b01, kd[c], G2[2 * c4][c]);
-          G2[2 * c4 + 1][c] = __ffma2_rn(b23, kd[c], G2[2 * c4 + 1][c]);
+        for (int h = 0; h < 2; ++h) {
+          const float2 u = h ? make_float2(bu.z, bu.w) : make_float2(bu.x, bu.y);
+          const float2 v = h ? make_float2(bv.z, bv.w) : make_float2(bv.x, bv.y);
+          float2 sj = __fmul2_rn(h ? make_float2(buu.z, buu.w) : make_float2(buu.x, buu.y), lb);
+          sj = __ffma2_rn(h ? make_float2(buv.z, buv.w) : make_float2(buv.x, buv.y), kb, sj);
+          sj = __ffma2_rn(h ? make_float2(bvv.z, bvv.w) : make_float2(bvv.x, bvv.y), nb, sj);
+          float2 *g = G2[2 * c4 + h];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) {
+            g[cc] = __ffma2_rn(u, ku[cc], g[cc]);
+            g[cc] = __ffma2_rn(v, kv[cc], g[cc]);
+            g[cc] = __ffma2_rn(sj, md[cc], g[cc]);
+          }
         }
       }
     }
@@ -1662,11 +1620,6 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
 
 __device__ __forceinline__ bool tpf_vec(const FaceSrc &S) {
   return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest)) & 15) == 0;
-}
-// The face tables can be staged with 16-byte copies.
-__device__ __forceinline__ bool tpf_stage_ok(const FaceSrc &S) {
-  return ((reinterpret_cast<uintptr_t>(S.cp) | reinterpret_cast<uintptr_t>(S.dest) |
-           reinterpret_cast<uintptr_t>(S.g0f)) & 15) == 0;
 }
 
 // Kahan-compensated FP32 totals of one thread, kept in shared memory (its
@@ -1708,7 +1661,6 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   using namespace tpf;
   __shared__ Smem sm;
   extern __shared__ __align__(16) unsigned char tpf_dyn[];
-  Stage *stages = reinterpret_cast<Stage *>(tpf_dyn);  // [warp][2]
   tpf_stage(sm, L.basis, L.weight);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1717,50 +1669,29 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   const float am1[3] = {(float)(r[3 * P.nv] - 1.0), (float)(r[3 * P.nv + 1] - 1.0), (float)(r[3 * P.nv + 2] - 1.0)};
   const Moduli<float> mod(P);
   const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, dsp, L.nfaces};
-  // the launch wrapper checks that the tables are 16-byte aligned (tpf_stage_ok)
+  const bool vec = tpf_vec(src);
   const float dudv = (float)L.dudv;
   const bool kg_reg = P.kg != 0.0 || P.k_reg != 0.0;  // else the pointwise step leaves those terms out
   const int n = L.nfaces, stride = gridDim.x * kThreads;
-  Stage *st = stages + 2 * warp;
-  SharedSums acc{reinterpret_cast<float *>(tpf_dyn + kStageBytes) + threadIdx.x};
+  SharedSums acc{reinterpret_cast<float *>(tpf_dyn) + threadIdx.x};
   acc.zero();
-  // Faces fb .. fb + 31 compute from st[buf] while the next 32 (fb + stride)
-  // are copied into st[buf ^ 1]. Only the last 32 of the mesh can be
-  // partial, and they have no successor, so every lane is active whenever a
-  // next stage exists.
-  int fb = (blockIdx.x * kWarps + warp) * 32, buf = 0;
-  if (fb < n) stage_issue(st[0], src, fb, min(32, n - fb), lane);
-  cp_async_commit();
-  for (; fb < n; fb += stride) {
-    const int nb = fb + stride;
-    if (nb < n) stage_issue(st[buf ^ 1], src, nb, min(32, n - nb), lane);
-    cp_async_commit();
-    cp_async_wait<1>();
-    __syncwarp();
+  for (int fb = (blockIdx.x * kWarps + warp) * 32; fb < n; fb += stride) {
     const int f = fb + lane;
     if (f < n) {
       float e3[3], da[3];
-      if (kg_reg)
-        tpf_face<true, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
-                             nb < n ? &st[buf ^ 1] : nullptr, lane);
-      else
-        tpf_face<true, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
-                              nb < n ? &st[buf ^ 1] : nullptr, lane);
+      if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+      else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
       acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
       acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
       if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
     }
-    __syncwarp();  // st[buf] is rewritten by the next round's copies
-    buf ^= 1;
   }
-  cp_async_wait<0>();
-  __syncthreads();  // the stage buffers double as the finish scratch below
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
     const double s = warp_sum(acc.get(q));
     if (lane == 0) sm.red[warp][q] = s;
   }
-  __syncthreads();
+  __syncthreads();  // every thread has read its sums: the finish may reuse their space
   if (threadIdx.x < 6) {
     double s = 0;
 #pragma unroll
@@ -1775,7 +1706,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     __syncthreads();
     if (last) {
       __threadfence();
-      static_assert(kStageBytes >= sizeof(double) * 6 * kThreads, "finish scratch must fit in the stage buffers");
+      static_assert(kSumBytes >= sizeof(double) * 6 * kThreads, "finish scratch must fit in the sums' space");
       finish_sums<kThreads>(fin, blockpart, reinterpret_cast<double(*)[kThreads]>(tpf_dyn));
       if (threadIdx.x == 0) *fin.done = 0u;
     }
@@ -1793,8 +1724,6 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   __shared__ Smem sm;
   __shared__ BatchFaceJob sj;
   __shared__ int s_active, s_tile;
-  extern __shared__ __align__(16) unsigned char tpf_dyn[];
-  Stage *st = reinterpret_cast<Stage *>(tpf_dyn) + 2 * (threadIdx.x >> 5);  // this warp's two stages
   const int ntiles = counts[group], tile_base = counts[3 + group];
   if ((int)blockIdx.x >= ntiles) return;
   tpf_stage(sm, basis, weight);
@@ -1831,43 +1760,14 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
       const int end = tile.first + tile.count;
       float *partial = (float *)sj.partial;
       const bool kg_reg = P.kg != 0.0 || P.k_reg != 0.0;  // else the pointwise step leaves those terms out
-      if (tpf_stage_ok(src) && tile.first % 4 == 0) {
-        // the single-mesh pipeline within the tile: this warp's next 32 faces
-        // are copied while the current 32 compute
-        int fb = tile.first + warp * 32, buf = 0;
-        if (fb < end) stage_issue(st[0], src, fb, min(32, end - fb), lane);
-        cp_async_commit();
-        for (; fb < end; fb += kThreads) {
-          const int nb = fb + kThreads;
-          if (nb < end) stage_issue(st[buf ^ 1], src, nb, min(32, end - nb), lane);
-          cp_async_commit();
-          cp_async_wait<1>();
-          __syncwarp();
-          const int f = fb + lane;
-          if (f < end) {
-            float e3[3], da[3];
-            if (kg_reg)
-              tpf_face<true, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
-                                   nb < end ? &st[buf ^ 1] : nullptr, lane);
-            else
-              tpf_face<true, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, true, partial, e3, da, &st[buf],
-                                    nb < end ? &st[buf ^ 1] : nullptr, lane);
-            acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
-          }
-          __syncwarp();
-          buf ^= 1;
-        }
-        cp_async_wait<0>();
-      } else {
-        const bool vec = tpf_vec(src);
-        for (int fb = tile.first + warp * 32; fb < end; fb += kThreads) {
-          const int f = fb + lane;
-          if (f < end) {
-            float e3[3], da[3];
-            if (kg_reg) tpf_face<false, true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
-            else tpf_face<false, false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
-            acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
-          }
+      const bool vec = tpf_vec(src);
+      for (int fb = tile.first + warp * 32; fb < end; fb += kThreads) {
+        const int f = fb + lane;
+        if (f < end) {
+          float e3[3], da[3];
+          if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+          else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+          acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
         }
       }
     }
@@ -2659,22 +2559,8 @@ static int per_device(PerDevice &pd, F make) {
   std::call_once(pd.once[dev], [&] { pd.value[dev] = make(); });
   return pd.value[dev];
 }
-// The dynamic shared memory limits above 48 KB that the staged kernels opt
-// into, once per device; returns the cudaError_t of the opt-in.
-static cudaError_t tpf_opt_in() {
-  static PerDevice pd;
-  return (cudaError_t)per_device(pd, [] {
-    return (int)cudaFuncSetAttribute(dev::face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(dev::tpf::kStageBytes + dev::tpf::kSumBytes));
-  });
-}
-static cudaError_t batch_tpf_opt_in() {
-  static PerDevice pd;
-  return (cudaError_t)per_device(pd, [] {
-    return (int)cudaFuncSetAttribute(dev::batch_face_tpf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)dev::tpf::kStageBytes);
-  });
-}
+// The dynamic shared memory limit above 48 KB that the tensor-core kernel
+// opts into, once per device; returns the cudaError_t of the opt-in.
 static cudaError_t tc_opt_in() {
   static PerDevice pd;
   return (cudaError_t)per_device(pd, [] {
@@ -2712,9 +2598,8 @@ static int face_grid_size_tpf(int nfaces) {
   static PerDevice pd;
   const int cached = per_device(pd, [] {
     int per_sm = 0;
-    tpf_opt_in();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::face_tpf_kernel, dev::tpf::kThreads,
-                                                  dev::tpf::kStageBytes + dev::tpf::kSumBytes);
+                                                  dev::tpf::kSumBytes);
     return sm_count() * (per_sm > 0 ? per_sm : 1);
   });
   int need = grid_for(nfaces, dev::tpf::kThreads);
@@ -2743,13 +2628,8 @@ cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int
   if constexpr (sizeof(T) == 4) {
     if (!rhi || !rlo || !dsp) return cudaErrorInvalidValue;
     if (ncp == 12 && npt == 15) {
-      const uintptr_t al = reinterpret_cast<uintptr_t>(L.cp) | reinterpret_cast<uintptr_t>(dest) |
-                           reinterpret_cast<uintptr_t>(L.g0f);
-      if (al & 15) return cudaErrorMisalignedAddress;  // the kernel stages the tables with 16-byte copies
-      const cudaError_t e = tpf_opt_in();
-      if (e != cudaSuccess) return e;
-      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes + dev::tpf::kSumBytes, s>>>(
-          L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status, fin);
+      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kSumBytes, s>>>(L, dest, P, r, rhi, rlo, dsp,
+                                                                              partial, blockpart, status, fin);
       return cudaGetLastError();
     }
   }
@@ -2858,6 +2738,14 @@ namespace umcp {
 
 template <typename T>
 int batch_face_blocks(int ncp, int npt) {
+  if (sizeof(T) == 4 && ncp == 12 && npt == 15) {  // the batched thread-per-face kernel's own occupancy
+    static PerDevice pd;
+    return per_device(pd, [] {
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::batch_face_tpf_kernel, dev::tpf::kThreads, 0);
+      return sm_count() * (per_sm > 0 ? per_sm : 1);
+    });
+  }
   return face_blocks<T>(1 << 30, ncp, npt);  // device-filling persistent grid
 }
 template int batch_face_blocks<double>(int, int);
@@ -2870,12 +2758,10 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
   constexpr int NT = dev::FaceCfg<T>::threads;
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
-      cudaError_t e = batch_tpf_opt_in();
-      if (e != cudaSuccess) return e;
       if (!next_tile) return cudaErrorInvalidValue;
-      e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
+      const cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
       if (e != cudaSuccess) return e;
-      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kStageBytes, s>>>(
+      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(
           jobs, group, tiles, counts, basis, weight, dudv, tile_sums, next_tile);
       return cudaGetLastError();
     }
