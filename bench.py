@@ -82,10 +82,10 @@ L2_BYTES = 129 * 1024 * 1024
 SM_COUNT, FP32_LANES_PER_SM = 152, 128
 # DRAM bytes per face of the batched face launches, from the ncu capture of
 # the first 64 vesicles of the workload at 512-face tiles (dram__bytes_read.sum
-# + dram__bytes_write.sum of the regular and valence-5 launches: 87.30 +
-# 25.41 + 2.79 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
+# + dram__bytes_write.sum of the regular and valence-5 launches: 86.26 +
+# 25.68 + 2.79 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
 # from it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 115.51e6 / 392960
+BATCH_FACE_DRAM_BYTES_PER_FACE = 114.74e6 / 392960
 
 
 def parse_args():
