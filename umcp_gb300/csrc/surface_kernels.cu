@@ -1402,6 +1402,12 @@ __device__ __forceinline__ float4 ld4(const float4 *p) {
   return v;
 }
 __device__ __forceinline__ float2 dup(float x) { return make_float2(x, x); }
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+// Point of the face loop at which the thread prefetches its next face's table
+// rows (control points, g0, composition, slot destinations) into L1. Those
+// rows are otherwise first touched when the next face starts (control points,
+// composition) or point by point (g0), each a round trip to L2.
+constexpr int kPrefetchPoint = 10;
 }  // namespace tpf
 
 __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, const double *weight) {
@@ -1413,12 +1419,13 @@ __device__ __forceinline__ void tpf_stage(tpf::Smem &sm, const double *basis, co
 // Face f's energy terms and dE/dalpha; writes its alpha-scaled gradient
 // partials to the face's slots. vec: cp and dest are 16-byte aligned.
 // am1 = alpha - 1 (formed in FP64): the box scales' part of the change from
-// the reference state.
+// the reference state. fn: the face this thread takes next (its rows are
+// prefetched), or -1.
 template <bool KG_REG>
 __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const SurfaceParams &P, int f,
                                          const float alpha[3], const float ialpha[3], const float am1[3],
                                          const Moduli<float> &mod, float dudv, bool vec, float *__restrict__ partial,
-                                         float e3[3], float da[3]) {
+                                         float e3[3], float da[3], int fn) {
   using namespace tpf;
   uint32_t cp[kNcp];
   if (vec) {
@@ -1511,6 +1518,15 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
   float ea = 0.f, ec = 0.f, er = 0.f, dax = 0.f, day = 0.f, daz = 0.f;
 #pragma unroll 1
   for (int p = 0; p < kNpt; ++p) {
+    if (p == kPrefetchPoint && fn >= 0) {
+      prefetch_l1(S.cp + (size_t)fn * kNcp);
+      prefetch_l1(S.cp + (size_t)fn * kNcp + kNcp - 1);
+      prefetch_l1(S.g0f + (size_t)fn * kNpt);
+      prefetch_l1(S.g0f + (size_t)fn * kNpt + kNpt - 1);
+      prefetch_l1(S.compf + (size_t)fn * 3);
+      prefetch_l1(S.dest + (size_t)fn * kNcp);
+      prefetch_l1(S.dest + (size_t)fn * kNcp + kNcp - 1);
+    }
     const float g0 = __ldg(&S.g0f[(size_t)f * kNpt + p]);
     float rr0 = 0.f;
     if constexpr (KG_REG) rr0 = __ldg(&S.rr0f[(size_t)f * kNpt + p]);
@@ -1679,8 +1695,10 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     const int f = fb + lane;
     if (f < n) {
       float e3[3], da[3];
-      if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
-      else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+      // no prefetch: a thread's next face is a grid stride away, and on the
+      // 512 x 512 planar pass the prefetch cost 1% instead of gaining
+      if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da, -1);
+      else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da, -1);
       acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
       acc.add(3, da[0]); acc.add(4, da[1]); acc.add(5, da[2]);
       if (!isfinite(e3[0] + e3[1] + e3[2])) atomicOr(status, kStatusNonFinite);
@@ -1765,8 +1783,9 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
         const int f = fb + lane;
         if (f < end) {
           float e3[3], da[3];
-          if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
-          else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da);
+          const int fn = f + kThreads < end ? f + kThreads : -1;
+          if (kg_reg) tpf_face<true>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da, fn);
+          else tpf_face<false>(sm, src, P, f, alpha, ialpha, am1, mod, dudv, vec, partial, e3, da, fn);
           acc.add(0, e3[0]); acc.add(1, e3[1]); acc.add(2, e3[2]);
         }
       }
