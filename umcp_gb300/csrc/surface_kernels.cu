@@ -1401,7 +1401,6 @@ __device__ __forceinline__ float4 ld4(const float4 *p) {
                : "r"((uint32_t)__cvta_generic_to_shared(p)));
   return v;
 }
-__device__ __forceinline__ float2 dup(float x) { return make_float2(x, x); }
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 // Point of the face loop at which the thread prefetches its next face's table
 // rows (control points, g0, composition, slot destinations) into L1. Those
@@ -1512,9 +1511,9 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
     }
   }
   // ---- the quadrature points
-  float2 G2[kNcp / 2][3];  // gradient sums of control points 2 i, 2 i + 1 per coordinate
+  float G[kNcp][3];  // gradient sums
 #pragma unroll
-  for (int i = 0; i < kNcp / 2; ++i) G2[i][0] = G2[i][1] = G2[i][2] = make_float2(0.f, 0.f);
+  for (int j = 0; j < kNcp; ++j) G[j][0] = G[j][1] = G[j][2] = 0.f;
   float ea = 0.f, ec = 0.f, er = 0.f, dax = 0.f, day = 0.f, daz = 0.f;
 #pragma unroll 1
   for (int p = 0; p < kNpt; ++p) {
@@ -1582,30 +1581,24 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
       day = fmaf(Kb[0].y, K[0].y, fmaf(Kb[1].y, K[1].y, fmaf(m.y, t[1], day)));
       daz = fmaf(Kb[0].z, K[0].z, fmaf(Kb[1].z, K[1].z, fmaf(m.z, t[2], daz)));
     }
-    // G[j]_c += B[u][j] Kb[u]_c + B[v][j] Kb[v]_c + s[j] m_c, control points j, j + 1 in one pair
+    // G[j]_c += B[u][j] Kb[u]_c + B[v][j] Kb[v]_c + s[j] m_c in scalar multiply-adds: with the
+    // forward contraction in paired ones, the mix keeps both FP32 multiply-add pipes busy
+    // (all paired: 763 us, this mix: 747 us, all scalar: 776 us on the 256-vesicle pass)
     {
-      const float2 ku[3] = {dup(Kb[0].x), dup(Kb[0].y), dup(Kb[0].z)};
-      const float2 kv[3] = {dup(Kb[1].x), dup(Kb[1].y), dup(Kb[1].z)};
-      const float2 md[3] = {dup(m.x), dup(m.y), dup(m.z)};
-      const float2 lb = dup(lkn[0]), kb = dup(lkn[1]), nb = dup(lkn[2]);
+      const float ku[3] = {Kb[0].x, Kb[0].y, Kb[0].z}, kv[3] = {Kb[1].x, Kb[1].y, Kb[1].z}, md[3] = {m.x, m.y, m.z};
 #pragma unroll
       for (int c4 = 0; c4 < kNc4; ++c4) {
         const Q4<float> bu = sm.B[p][0][c4], bv = sm.B[p][1][c4], buu = sm.B[p][2][c4], buv = sm.B[p][3][c4],
                         bvv = sm.B[p][4][c4];
+        const float u[4] = {bu.x, bu.y, bu.z, bu.w}, v[4] = {bv.x, bv.y, bv.z, bv.w};
+        const float uu[4] = {buu.x, buu.y, buu.z, buu.w}, uv[4] = {buv.x, buv.y, buv.z, buv.w},
+                    vv[4] = {bvv.x, bvv.y, bvv.z, bvv.w};
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const float2 u = h ? make_float2(bu.z, bu.w) : make_float2(bu.x, bu.y);
-          const float2 v = h ? make_float2(bv.z, bv.w) : make_float2(bv.x, bv.y);
-          float2 sj = __fmul2_rn(h ? make_float2(buu.z, buu.w) : make_float2(buu.x, buu.y), lb);
-          sj = __ffma2_rn(h ? make_float2(buv.z, buv.w) : make_float2(buv.x, buv.y), kb, sj);
-          sj = __ffma2_rn(h ? make_float2(bvv.z, bvv.w) : make_float2(bvv.x, bvv.y), nb, sj);
-          float2 *g = G2[2 * c4 + h];
+        for (int jj = 0; jj < 4; ++jj) {
+          const float sj = fmaf(vv[jj], lkn[2], fmaf(uv[jj], lkn[1], uu[jj] * lkn[0]));
+          float *g = G[4 * c4 + jj];
 #pragma unroll
-          for (int cc = 0; cc < 3; ++cc) {
-            g[cc] = __ffma2_rn(u, ku[cc], g[cc]);
-            g[cc] = __ffma2_rn(v, kv[cc], g[cc]);
-            g[cc] = __ffma2_rn(sj, md[cc], g[cc]);
-          }
+          for (int cc = 0; cc < 3; ++cc) g[cc] = fmaf(sj, md[cc], fmaf(v[jj], kv[cc], fmaf(u[jj], ku[cc], g[cc])));
         }
       }
     }
@@ -1629,7 +1622,7 @@ __device__ __forceinline__ void tpf_face(tpf::Smem &sm, const FaceSrc &S, const 
   for (int j = 0; j < kNcp; ++j) {
     float *o = partial + 3 * (size_t)d[j];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) o[c] = alpha[c] * ((j & 1) ? G2[j / 2][c].y : G2[j / 2][c].x);
+    for (int c = 0; c < 3; ++c) o[c] = alpha[c] * G[j][c];
   }
   e3[0] = ea; e3[1] = ec; e3[2] = er;
 }
