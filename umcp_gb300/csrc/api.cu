@@ -1087,6 +1087,8 @@ umcp_status umcp::make_step_args(const umcp_mesh *m, const umcp_integrator *it, 
   if (it->kind == 0) {
     a->mob_dt = it->D * it->time_step / m->kT;
     a->sigma = std::sqrt(2.0 * it->D * it->time_step);
+    a->mob_dt_f = (float)a->mob_dt;
+    a->sigma_f = (float)a->sigma;
   } else {
     a->sigma = std::sqrt(2.0 * it->gamma * m->kT * a->AK);
   }

@@ -64,7 +64,7 @@ struct umcp_batch {
   int vgrid = 0;
   // device tables
   DevBuf d_jobs, d_tiles, d_vtiles, d_tile_off, d_tile_idx, d_counts, d_live, d_prog, d_start, d_step0, d_tile_sums;
-  DevBuf d_next_tile;  // tile counter of the regular face launch
+  DevBuf d_next_tile;  // {tiles handed out, blocks done} of the regular face launch (it resets them)
   // host-driven steps (umcp_batch_step_host): the jobs' states packed in job
   // order, each job's offset into the pack, and the jobs' latest energies
   DevBuf d_pack, d_pack_off, d_pack_E;
@@ -508,7 +508,8 @@ extern "C" umcp_status umcp_batch_create(umcp_ctx *ctx, int precision, const umc
   UMCP_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   UMCP_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
   UMCP_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
-  UMCP_CUDA(b->d_next_tile.alloc(sizeof(int)));
+  UMCP_CUDA(b->d_next_tile.alloc(2 * sizeof(int)));
+  UMCP_CUDA(cudaMemsetAsync(b->d_next_tile.p, 0, 2 * sizeof(int), ctx->stream));
   b->ctx = ctx;
   b->precision = precision;
   if (opts) {

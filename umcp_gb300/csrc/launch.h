@@ -133,6 +133,7 @@ struct StepArgs {
   double gamma;
   uint64_t seed;
   uint32_t stream;
+  float mob_dt_f, sigma_f;  // kind 0: mob_dt and sigma rounded to FP32 (the precision form's increment)
 };
 // Gather fused with the vertex-local update (kind 0; kinds 1/2 with identity mass).
 // f (all NULL in the plain path) receives the FP32 positions of the new state.

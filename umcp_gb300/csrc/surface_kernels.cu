@@ -1134,6 +1134,24 @@ __device__ __forceinline__ void vertex_gradient(const T *__restrict__ partial, c
   }
 }
 
+// The same sum in the precision form, its compensated total rounded to FP32.
+__device__ __forceinline__ void vertex_gradient_f32(const float *__restrict__ partial, const int *__restrict__ loc,
+                                                    int v, float g[3]) {
+  const int base = loc[2 * (size_t)v], n = loc[2 * (size_t)v + 1];
+  float s3[3] = {0, 0, 0}, c3[3] = {0, 0, 0};
+  for (int k = 0; k < n; ++k) {
+    const size_t s = (size_t)base + 32 * (size_t)k;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float y = partial[3 * s + c] - c3[c], t = s3[c] + y;
+      c3[c] = (t - s3[c]) - y;
+      s3[c] = t;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) g[c] = s3[c] - c3[c];
+}
+
 template <typename T>
 __global__ void gather_kernel(int nv, const T *__restrict__ partial, const int *__restrict__ off,
                               double *__restrict__ g) {
@@ -1149,7 +1167,7 @@ __global__ void gather_kernel(int nv, const T *__restrict__ partial, const int *
 // Three unit normals per vertex from two Philox draws (Box-Muller). The
 // plain path transforms in FP64 (bit-for-bit the oracle's draws up to libm
 // rounding); the precision form in FP32 from 24-bit uniforms.
-__device__ __forceinline__ void normals3_f32(uint64_t seed, uint32_t stream, uint64_t step, int v, double n[3]) {
+__device__ __forceinline__ void normals3_f32(uint64_t seed, uint32_t stream, uint64_t step, int v, float n[3]) {
   philox_out o = philox4x32_10((uint32_t)v, (uint32_t)step, (uint32_t)(step >> 32), stream, (uint32_t)seed,
                                (uint32_t)(seed >> 32));
   const float k = 1.0f / 16777216.0f;
@@ -1160,6 +1178,13 @@ __device__ __forceinline__ void normals3_f32(uint64_t seed, uint32_t stream, uin
   n[0] = rad * cs;
   n[1] = rad * sn;
   n[2] = sqrtf(-2.0f * logf(u3)) * cospif(2.0f * u4);
+}
+__device__ __forceinline__ void normals3_f32(uint64_t seed, uint32_t stream, uint64_t step, int v, double n[3]) {
+  float f[3];
+  normals3_f32(seed, stream, step, v, f);
+  n[0] = f[0];
+  n[1] = f[1];
+  n[2] = f[2];
 }
 
 __device__ __forceinline__ void normals3(uint64_t seed, uint32_t stream, uint64_t step, int v, double n[3]) {
@@ -1217,6 +1242,30 @@ __device__ __forceinline__ void vertex_update(const StepArgs &a, const double gg
 // which finish_kernel has already advanced past this step.
 __device__ __forceinline__ uint64_t current_step(const uint64_t *cnt) { return cnt[0] + cnt[1] - 1; }
 
+// The precision form's overdamped BD step of one vertex: the gradient total
+// and the Box-Muller normals stay in FP32, and so does the increment
+// -(D dt / kT) g + sqrt(2 D dt) xi (about 2^-23 relative, 1e-9 A at a 0.02 A
+// step); it is added to the FP64 position, from which the FP32 copies are
+// then taken. The FP64 work is the position and its copies only: 8 operations
+// per coordinate instead of 14 on GB300's narrow FP64 pipe. Explicitly
+// rounded, so every kernel that inlines it rounds alike.
+__device__ __forceinline__ void bd_vertex_f32(const float *__restrict__ partial, const int *__restrict__ off, int v,
+                                              const StepArgs &a, uint64_t st, double *__restrict__ r,
+                                              float *__restrict__ rhi, float *__restrict__ rlo,
+                                              const double *__restrict__ r0, float *__restrict__ dsp) {
+  float g[3], n[3];
+  vertex_gradient_f32(partial, off, v, g);
+  normals3_f32(a.seed, a.stream, st, v, n);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t i = 3 * (size_t)v + c;
+    const float d = __fmaf_rn(-a.mob_dt_f, g[c], __fmul_rn(a.sigma_f, n[c]));
+    const double x = __dadd_rn(r[i], (double)d);
+    r[i] = x;
+    if (rhi) store_f32_position(i, x, rhi, rlo, r0, dsp);
+  }
+}
+
 // Gather fused with the vertex-local update (overdamped BD, or the leapfrog
 // kinds with identity mass).
 template <typename T>
@@ -1227,6 +1276,12 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
   if (*status) return;
   const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    if constexpr (sizeof(T) == 4) {
+      if (a.kind == 0) {
+        bd_vertex_f32((const float *)partial, off, v, a, st, r, rhi, rlo, r0, dsp);
+        continue;
+      }
+    }
     double gg[3], n[3];
     vertex_gradient(partial, off, v, gg);
     if constexpr (sizeof(T) == 8) normals3(a.seed, a.stream, st, v, n);
@@ -1651,6 +1706,12 @@ struct SharedSums {
   }
 };
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while the kernel before it on the stream finishes;
+// it waits here, before its first read of that kernel's results (a no-op
+// when it was launched without the attribute).
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Sum of q over the warp in a fixed (xor-tree) order.
 __device__ __forceinline__ double warp_sum(double q) {
 #pragma unroll
@@ -1726,18 +1787,20 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
 
 // Batched regular faces, precision form: a block takes a tile (faces of one
 // job), its warps 32 faces at a time; writes the tile's three energy sums.
+// counter[0] hands out the tiles; counter[1] counts the blocks that are done,
+// and the last of them zeroes both for the next launch.
 __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     batch_face_tpf_kernel(const BatchJob *__restrict__ jobs, int group, const BatchTile *__restrict__ tiles,
                           const int *__restrict__ counts, const double *__restrict__ basis,
                           const double *__restrict__ weight, double dudv_d, double *__restrict__ tile_sums,
-                          int *__restrict__ next_tile) {
+                          int *__restrict__ counter) {
   using namespace tpf;
   __shared__ Smem sm;
   __shared__ BatchFaceJob sj;
   __shared__ int s_active, s_tile;
+  tpf_stage(sm, basis, weight);  // constant tables: before the wait
+  grid_dependency_wait();        // positions, job states and the counter come from the kernels before
   const int ntiles = counts[group], tile_base = counts[3 + group];
-  if ((int)blockIdx.x >= ntiles) return;
-  tpf_stage(sm, basis, weight);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float dudv = (float)dudv_d;
   // Tiles are handed out by a counter (zeroed before the launch), so blocks
@@ -1745,7 +1808,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   // the results do not depend on which block took which tile.
   for (;;) {
     __syncthreads();  // the previous tile's readers of sj, s_tile and sm.red are done
-    if (threadIdx.x == 0) s_tile = atomicAdd(next_tile, 1);
+    if (threadIdx.x == 0) s_tile = (int)blockIdx.x < ntiles ? atomicAdd(&counter[0], 1) : ntiles;
     __syncthreads();
     const int t = s_tile;
     if (t >= ntiles) break;
@@ -1796,6 +1859,11 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
       tile_sums[3 * (size_t)(tile_base + t) + threadIdx.x] = s;
     }
   }
+  __threadfence();  // this block's last draw on counter[0] is ordered before its count on counter[1]
+  if (threadIdx.x == 0 && atomicAdd(&counter[1], 1) == (int)gridDim.x - 1) {
+    counter[0] = 0;  // every block has drawn its last tile: reset for the next launch
+    counter[1] = 0;
+  }
 }
 
 // Per job (one warp each): sum its tiles in listed order, record the step's
@@ -1806,6 +1874,7 @@ __global__ void batch_reduce_kernel(const BatchJob *__restrict__ jobs, const int
                                     const int *__restrict__ tile_off, const int *__restrict__ tile_idx,
                                     const double *__restrict__ tile_sums, int *__restrict__ live,
                                     unsigned long long *__restrict__ prog) {
+  grid_dependency_wait();
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (j >= counts[6]) return;
@@ -1847,6 +1916,7 @@ __global__ void batch_reduce_kernel(const BatchJob *__restrict__ jobs, const int
 template <typename T>
 __global__ void batch_gather_step_kernel(const BatchJob *__restrict__ jobs, const BatchTile *__restrict__ vtiles,
                                          const int *__restrict__ counts, const int *__restrict__ live) {
+  grid_dependency_wait();
   const int nvtiles = counts[7];
   for (int t = blockIdx.x; t < nvtiles; t += gridDim.x) {
     const BatchTile tile = vtiles[t];
@@ -1855,6 +1925,12 @@ __global__ void batch_gather_step_kernel(const BatchJob *__restrict__ jobs, cons
     const StepArgs &a = J.a;
     const int v = tile.first + threadIdx.x;
     const uint64_t st = J.f.cnt[0] + J.f.cnt[1] - 1;
+    if constexpr (sizeof(T) == 4) {
+      if (a.kind == 0) {
+        bd_vertex_f32((const float *)J.f.partial, J.off, v, a, st, J.r, J.rhi, J.rlo, J.r0, J.dsp);
+        continue;
+      }
+    }
     double gg[3], n[3];
     vertex_gradient((const T *)J.f.partial, J.off, v, gg);
     if constexpr (sizeof(T) == 8) normals3(a.seed, a.stream, st, v, n);
@@ -2748,6 +2824,24 @@ cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const doub
 
 namespace umcp {
 
+// Launch with programmatic stream serialization: the kernel may be scheduled
+// while the kernel before it on the stream drains, and waits for it in
+// grid_dependency_wait (which it calls before reading that kernel's results).
+template <typename... P, typename... A>
+static cudaError_t launch_after(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
+}
+
 template <typename T>
 int batch_face_blocks(int ncp, int npt) {
   if (sizeof(T) == 4 && ncp == 12 && npt == 15) {  // the batched thread-per-face kernel's own occupancy
@@ -2771,11 +2865,8 @@ cudaError_t launch_batch_faces(const BatchJob *jobs, int group, const BatchTile 
   if constexpr (sizeof(T) == 4) {
     if (ncp == 12 && npt == 15) {
       if (!next_tile) return cudaErrorInvalidValue;
-      const cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(int), s);
-      if (e != cudaSuccess) return e;
-      dev::batch_face_tpf_kernel<<<grid, dev::tpf::kThreads, 0, s>>>(
-          jobs, group, tiles, counts, basis, weight, dudv, tile_sums, next_tile);
-      return cudaGetLastError();
+      return launch_after(dev::batch_face_tpf_kernel, grid, dev::tpf::kThreads, 0, s, jobs, group, tiles, counts,
+                          basis, weight, dudv, tile_sums, next_tile);
     }
   }
   if (ncp == 12 && npt == 15)
@@ -2801,16 +2892,14 @@ template cudaError_t launch_batch_faces<float>(const BatchJob *, int, const Batc
 cudaError_t launch_batch_reduce(const BatchJob *jobs, const int *counts, int max_jobs, const int *tile_off,
                                 const int *tile_idx, const double *tile_sums, int *live, unsigned long long *prog,
                                 cudaStream_t s) {
-  dev::batch_reduce_kernel<<<grid_for(max_jobs * 32, 256), 256, 0, s>>>(jobs, counts, tile_off, tile_idx, tile_sums,
-                                                                        live, prog);
-  return cudaGetLastError();
+  return launch_after(dev::batch_reduce_kernel, grid_for(max_jobs * 32, 256), 256, 0, s, jobs, counts, tile_off,
+                      tile_idx, tile_sums, live, prog);
 }
 
 template <typename T>
 cudaError_t launch_batch_gather_step(const BatchJob *jobs, const BatchTile *vtiles, const int *counts,
                                      const int *live, int grid, cudaStream_t s) {
-  dev::batch_gather_step_kernel<T><<<grid, kVertexTile, 0, s>>>(jobs, vtiles, counts, live);
-  return cudaGetLastError();
+  return launch_after(dev::batch_gather_step_kernel<T>, grid, kVertexTile, 0, s, jobs, vtiles, counts, live);
 }
 template cudaError_t launch_batch_gather_step<double>(const BatchJob *, const BatchTile *, const int *, const int *,
                                                       int, cudaStream_t);
