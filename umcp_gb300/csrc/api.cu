@@ -1173,18 +1173,15 @@ static umcp_status run_steps(umcp_mesh *m, const umcp_integrator *it, uint64_t s
   UMCP_CUDA(cudaMemcpyAsync(m->cnt.p, m->h_cnt, 2 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
   UMCP_CUDA(cudaMemsetAsync(m->status.p, 0, sizeof(int), s));
   const int use_mass = (it->kind != 0 && it->use_mass) ? 1 : 0;
-  const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
-  if (full > 0) {
+  // kGraphChunk steps at a time, then the rest as one captured run per set bit
+  for (int left = n_steps; left > 0;) {
+    int len = kGraphChunk;
+    while (len > left) len >>= 1;
     cudaGraphExec_t g;
-    st = graph_for(m, a, use_mass, it->divergence_threshold, kGraphChunk, &g);
+    st = graph_for(m, a, use_mass, it->divergence_threshold, len, &g);
     if (st != UMCP_OK) return st;
-    for (int c = 0; c < full; ++c) UMCP_CUDA(cudaGraphLaunch(g, s));
-  }
-  if (rem > 0) {
-    cudaGraphExec_t g1;
-    st = graph_for(m, a, use_mass, it->divergence_threshold, 1, &g1);
-    if (st != UMCP_OK) return st;
-    for (int i = 0; i < rem; ++i) UMCP_CUDA(cudaGraphLaunch(g1, s));
+    UMCP_CUDA(cudaGraphLaunch(g, s));
+    left -= len;
   }
   return UMCP_OK;
 }

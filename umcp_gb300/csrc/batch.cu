@@ -74,8 +74,10 @@ struct umcp_batch {
   int counts[kCountWords] = {};
   unsigned long long *h_prog = nullptr;
   size_t prog_jobs = 0;  // jobs whose progress the latest run is copying to h_prog
-  // captured steps (kGraphChunk steps and 1 step) for the current capacities
-  cudaGraphExec_t g_chunk = nullptr, g_one = nullptr;
+  // captured steps for the current capacities: g_pow[i] runs 2^i steps (up to kGraphChunk)
+  static constexpr int kPows = 6;
+  static_assert(1 << (kPows - 1) == kGraphChunk, "one captured length per power of two up to kGraphChunk");
+  cudaGraphExec_t g_pow[kPows] = {};
   // The irregular face launches run on a second stream, forked from the
   // context's stream after the regular launch is queued and joined before the
   // per-job sums, so they fill the SMs the regular launch's tail leaves idle
@@ -83,9 +85,10 @@ struct umcp_batch {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   void drop_graphs() {
-    if (g_chunk) cudaGraphExecDestroy(g_chunk);
-    if (g_one) cudaGraphExecDestroy(g_one);
-    g_chunk = g_one = nullptr;
+    for (cudaGraphExec_t &g : g_pow) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   }
   ~umcp_batch() {
     drop_graphs();
@@ -620,14 +623,17 @@ extern "C" umcp_status umcp_batch_run(umcp_batch *b, int n_steps) {
     if ((st = autotune(b, faces)) != UMCP_OK) return st;
     b->tuned_faces = faces;
   }
-  const int full = n_steps / kGraphChunk, rem = n_steps % kGraphChunk;
-  if (full > 0) {
-    if (!b->g_chunk && (st = capture(b, kGraphChunk, &b->g_chunk)) != UMCP_OK) return st;
-    for (int c = 0; c < full; ++c) UMCP_CUDA(cudaGraphLaunch(b->g_chunk, s));
-  }
-  if (rem > 0) {
-    if (!b->g_one && (st = capture(b, 1, &b->g_one)) != UMCP_OK) return st;
-    for (int i = 0; i < rem; ++i) UMCP_CUDA(cudaGraphLaunch(b->g_one, s));
+  // kGraphChunk steps at a time, then the rest as one captured run per set bit
+  // (20 steps: 16 + 4), so short runs are a few graph launches, not one per
+  // step. All six lengths are captured together (at the first run and after a
+  // table outgrows its capacity), so no later run pays for a capture.
+  for (int i = 0; i < umcp_batch::kPows; ++i)
+    if (!b->g_pow[i] && (st = capture(b, 1 << i, &b->g_pow[i])) != UMCP_OK) return st;
+  for (int left = n_steps; left > 0;) {
+    int i = umcp_batch::kPows - 1;
+    while ((1 << i) > left) --i;
+    UMCP_CUDA(cudaGraphLaunch(b->g_pow[i], s));
+    left -= 1 << i;
   }
   UMCP_CUDA(cudaMemcpyAsync(b->h_prog, b->d_prog.p, 2 * b->jobs.size() * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, s));

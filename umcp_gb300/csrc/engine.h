@@ -124,7 +124,7 @@ struct umcp_mesh {
   int mrows = 0;
   umcp::DevBuf mrow, mcol, mval, alphas, mdense, min32;
   bool mass_dense = false, mass_f32 = false;
-  // captured step sequences, by length (1 and kGraphChunk steps)
+  // captured step sequences, by length (powers of two up to kGraphChunk steps)
   struct CachedGraph {
     cudaGraphExec_t exec = nullptr;
     int steps = 0;
