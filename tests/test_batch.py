@@ -156,11 +156,12 @@ def test_host_driven_steps_follow_the_resident_run(ctx, precision):
     array and come out after each call; the trajectory is the device-resident
     batch run's, bit for bit, and E holds each job's latest step energy. A
     state the caller changes between calls is the one the next step starts
-    from."""
+    from. Page-locked and pageable host buffers give the same states."""
+    torch = pytest.importorskip("torch")
     its = _integrators()[:2]
     names = ["ico2_plain", "ico3_deformed"]
     runs = []
-    for host in (False, True):
+    for host in (False, True, "pinned"):
         batch = U.Batch(ctx, precision)
         meshes = [_mesh(ctx, n, precision) for n in names]
         for k, m in enumerate(meshes):
@@ -168,8 +169,15 @@ def test_host_driven_steps_follow_the_resident_run(ctx, precision):
         if host:
             pack = np.concatenate([m.state_get()[0] for m in meshes])
             E = np.zeros(len(meshes))
-            for _ in range(20):
-                batch.step_host(pack, pack, E, 2)
+            if host == "pinned":
+                pack_t = torch.from_numpy(pack).pin_memory()
+                E_t = torch.zeros(len(meshes), dtype=torch.float64).pin_memory()
+                pack, E = pack_t.numpy(), E_t.numpy()  # views of the page-locked memory
+                for _ in range(20):
+                    batch.step_host(pack_t.data_ptr(), pack_t.data_ptr(), E_t.data_ptr(), 2)
+            else:
+                for _ in range(20):
+                    batch.step_host(pack, pack, E, 2)
             states = np.split(pack, np.cumsum([3 * m.nv + 3 for m in meshes])[:-1])
             assert all(np.array_equal(s, m.state_get()[0]) for s, m in zip(states, meshes))
             assert np.array_equal(E, [m.energies(40)[-1] for m in meshes])
@@ -177,8 +185,9 @@ def test_host_driven_steps_follow_the_resident_run(ctx, precision):
             batch.run(40)
             states = [m.state_get()[0] for m in meshes]
         runs.append(states)
-    for a, b in zip(*runs):
-        assert np.array_equal(a, b)
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            assert np.array_equal(a, b)
     # a changed state is picked up by the next call
     batch = U.Batch(ctx, precision)
     m = _mesh(ctx, "ico2_plain", precision)
@@ -224,3 +233,30 @@ def test_tuned_layout_is_cached_and_leaves_trajectories_unchanged(ctx, tmp_path)
         assert np.array_equal(a, b) and np.array_equal(a, c)
     for a, c in zip(e1, e3):
         assert np.max(np.abs(a - c) / np.abs(a)) <= E_TOL[U.FP32_CENTRED]
+
+
+def test_energy_call_between_runs_leaves_the_batch_trajectory(ctx):
+    """An energy evaluation of a batch job's mesh at other positions (which
+    takes the precision form's FP32 copies from those positions) between two
+    runs does not change the batch's trajectory, whether the next step is a
+    device-resident run or a host-driven step that passes the state back
+    unchanged (whose unpacking keeps the copies of unchanged coordinates)."""
+    it = _integrators()[0]
+    runs = []
+    for poke in (None, "run", "host"):
+        batch = U.Batch(ctx, U.FP32_CENTRED)
+        m = _mesh(ctx, "ico3_deformed", U.FP32_CENTRED)
+        batch.add(m, it, 0, 10)
+        batch.run(4)
+        r = m.state_get()[0]
+        if poke:
+            r2 = r.copy()
+            r2[:-3] += 0.3
+            m.energy(r2)
+        if poke == "host":
+            batch.step_host(r, r, None, 1)
+        else:
+            batch.run(1)
+        batch.run(5)
+        runs.append(m.state_get()[0])
+    assert np.array_equal(runs[0], runs[1]) and np.array_equal(runs[0], runs[2])

@@ -287,6 +287,19 @@ static umcp_status start_jobs(umcp_batch *b) {
   return UMCP_OK;
 }
 
+// The precision form's FP32 copies of every job's resident state: a mesh whose
+// copies were last taken from another state (an energy call at other
+// positions) gets them again before the batch reads them.
+static umcp_status resplit(umcp_batch *b) {
+  for (Job &J : b->jobs) {
+    umcp_mesh *m = J.m;
+    if (m->precision != UMCP_FP32_CENTRED || m->split_valid) continue;
+    UMCP_CUDA(launch_split_positions(3 * m->nv, m->r.as<double>(), m->f32pos(), b->ctx->stream));
+    m->split_valid = true;
+  }
+  return UMCP_OK;
+}
+
 template <typename T>
 static cudaError_t queue_faces_t(umcp_batch *b) {
   cudaStream_t s = b->ctx->stream;
@@ -614,6 +627,7 @@ extern "C" umcp_status umcp_batch_run(umcp_batch *b, int n_steps) {
   if ((st = harvest(b)) != UMCP_OK) return st;
   if (b->dirty && (st = rebuild(b)) != UMCP_OK) return st;
   if ((st = start_jobs(b)) != UMCP_OK) return st;
+  if ((st = resplit(b)) != UMCP_OK) return st;
   // The face launches' layout (tune cache or timing), at the first run and
   // again whenever the batch has grown fourfold in faces since (a few times
   // at most over a batch's life).
@@ -705,7 +719,12 @@ extern "C" umcp_status umcp_batch_step_host(umcp_batch *b, const double *r_in, d
   if ((st = harvest(b)) != UMCP_OK) return st;
   if (b->dirty && (st = rebuild(b)) != UMCP_OK) return st;
   if ((st = start_jobs(b)) != UMCP_OK) return st;
+  if ((st = resplit(b)) != UMCP_OK) return st;  // the unpacking keeps the copies of unchanged coordinates
   const size_t bytes = b->pack_doubles * sizeof(double);
+  // One copy each way through a device staging pack. (Reading and writing
+  // page-locked host memory in place from the (un)pack kernels, over the
+  // CPU-GPU link, was slower on GB300: 1.32 ms against 1.11 ms per 256-vesicle
+  // host step.)
   if (r_in) {
     UMCP_CUDA(cudaMemcpyAsync(b->d_pack.p, r_in, bytes, cudaMemcpyHostToDevice, s));
     UMCP_CUDA(launch_batch_unpack(b->d_jobs.as<BatchJob>(), b->d_vtiles.as<BatchTile>(), b->d_counts.as<int>(),

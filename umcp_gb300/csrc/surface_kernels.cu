@@ -2010,6 +2010,9 @@ __global__ void batch_unpack_kernel(const BatchJob *__restrict__ jobs, const Bat
       const size_t v = (size_t)(tile.first + threadIdx.x);
       for (int c = 0; c < 3; ++c) {
         const double x = src[3 * v + c];
+        // a coordinate the caller left as it was keeps its FP32 copies (compared
+        // bit for bit, on the integer pipe): most of the unpacking's FP64 work
+        if (__double_as_longlong(x) == __double_as_longlong(J.r[3 * v + c])) continue;
         J.r[3 * v + c] = x;
         if (J.rhi) store_f32_position(3 * v + c, x, J.rhi, J.rlo, J.r0, J.dsp);
       }
