@@ -105,7 +105,7 @@ def parse_args():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--e2e-groups", type=int, default=E2E_GROUPS,
                     help="independent batches (contexts, host threads) the e2e measurement drives the vesicles as")
-    ap.add_argument("--mode", default="bench", choices=["bench", "facepass", "massapply"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "facepass", "massapply", "geo"])
     ap.add_argument("--nx", type=int, default=512, help="facepass: planar membrane size")
     ap.add_argument("--ny", type=int, default=512)
     ap.add_argument("--icosphere", type=int, default=0, help="facepass: an icosahedral vesicle of this level instead")
@@ -892,6 +892,47 @@ def facepass_mode(args) -> None:
     print(f"faces={info.n_faces} points={info.n_points} E={E:.10g} face_pass_us={us:.1f}")
 
 
+def geo_mode(args) -> None:
+    """Energy and gradient of one vesicle (icosahedron subdivided --level times,
+    radius --radius) with and without the global area and volume restraints
+    (K_area 0.2, K_volume 0.01, the state's own targets), on the device: the
+    restraint kernels' cost, and a launch sequence for their ncu captures."""
+    import torch
+    import umcp_gb300 as U
+
+    prec = U.FP32_CENTRED if args.precision == "fp32" else U.FP64
+    ctx = U.Context(0)
+    prm = U.params(kc=U.kc_from_kT(20.0), KA=0.215, precision=prec)
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "v.mesh"
+        U.generate_icosphere(path, args.level, args.radius, 2.0, 7)
+        plan = U.Plan(path, prm)
+    mesh = U.Mesh(ctx, plan, prm)
+    d_r = torch.tensor(plan.positions(), dtype=torch.float64, device="cuda:0")
+    d_E = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    d_g = torch.zeros(d_r.numel(), dtype=torch.float64, device="cuda:0")
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda:0"))
+    torch.cuda.synchronize()
+
+    def timed() -> float:
+        mesh.energy_grad_device(d_r.data_ptr(), d_E.data_ptr(), d_g.data_ptr())  # untimed
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.repeat):
+            mesh.energy_grad_device(d_r.data_ptr(), d_E.data_ptr(), d_g.data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        ctx.synchronize()
+        return e0.elapsed_time(e1) * 1e3 / max(args.repeat, 1)
+
+    plain = timed()
+    mesh.restraints_set(K_area=0.2, K_volume=0.01)
+    restrained = timed()
+    A, V, Er = mesh.restraints_get()
+    print(f"vertices={plan.nv} faces={mesh.info().n_faces} energy_grad_us={plain:.1f} "
+          f"with_restraints_us={restrained:.1f} restraints_us={restrained - plain:.1f} A={A:.6f} V={V:.6f}")
+
+
 def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool) -> int:
     """Algorithmic bytes of one apply, out += M^-1 in on 3 components per row:
     CSR 8 per nonzero (FP32 value and column; 12 in FP64) plus, per row, the
@@ -947,6 +988,8 @@ def main() -> None:
         facepass_mode(args)
     elif args.mode == "massapply":
         massapply_mode(args)
+    elif args.mode == "geo":
+        geo_mode(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:
