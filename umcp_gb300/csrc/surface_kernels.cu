@@ -61,6 +61,12 @@ struct FaceSmem<float, NCP, NPT> {
 };
 
 // Error-free sum: s + e == a + b exactly (Knuth's two-sum).
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while the kernel before it on the stream finishes;
+// it waits here, before its first read of that kernel's results (a no-op
+// when it was launched without the attribute).
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = a + b;
   float bb = s - a;
@@ -473,6 +479,7 @@ __global__ void __launch_bounds__(FaceCfg<T>::threads, FaceCfg<T>::min_blocks)
   __shared__ S sm;
   stage_basis<T, NCP, NPT, NT>(sm, L.basis, L.weight);
   __syncthreads();
+  grid_dependency_wait();  // the state comes from the kernels before
 
   const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
   const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
@@ -1291,6 +1298,7 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
                                    const uint64_t *__restrict__ cnt, double *__restrict__ r, double *__restrict__ p,
                                    float *__restrict__ rhi, float *__restrict__ rlo, const double *__restrict__ r0,
                                    float *__restrict__ dsp, const int *__restrict__ status) {
+  grid_dependency_wait();  // the partials and the status come from the face launches
   if (*status) return;
   const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
@@ -1323,6 +1331,7 @@ __global__ void gather_step_kernel(int nv, const T *__restrict__ partial, const 
 
 __global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ cnt, double *__restrict__ p,
                             const double *__restrict__ g, const int *__restrict__ status) {
+  grid_dependency_wait();
   if (*status) return;
   const uint64_t st = current_step(cnt);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
@@ -1338,6 +1347,7 @@ __global__ void kick_kernel(int nv, StepArgs a, const uint64_t *__restrict__ cnt
 __global__ void drift_kernel(int nv, StepArgs a, double *__restrict__ r, double *__restrict__ p,
                              const double *__restrict__ qdot, float *__restrict__ rhi, float *__restrict__ rlo,
                              const double *__restrict__ r0, float *__restrict__ dsp, const int *__restrict__ status) {
+  grid_dependency_wait();
   if (*status) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * nv; i += gridDim.x * blockDim.x) {
     const double x = __dadd_rn(r[i], __dmul_rn(qdot[i], a.AK));
@@ -1724,12 +1734,6 @@ struct SharedSums {
   }
 };
 
-// Programmatic dependent launch: a kernel launched with programmatic stream
-// serialization may start while the kernel before it on the stream finishes;
-// it waits here, before its first read of that kernel's results (a no-op
-// when it was launched without the attribute).
-__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
 // Sum of q over the warp in a fixed (xor-tree) order.
 __device__ __forceinline__ double warp_sum(double q) {
 #pragma unroll
@@ -1751,6 +1755,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   extern __shared__ __align__(16) unsigned char tpf_dyn[];
   tpf_stage(sm, L.basis, L.weight);
   __syncthreads();
+  grid_dependency_wait();  // the state comes from the kernels before
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
   const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
@@ -2161,6 +2166,7 @@ __global__ void __launch_bounds__(kGeoThreads) geo_sums_kernel(GeoArgs G) {
   __shared__ double red[kGeoWords][kGeoThreads];
   stage_geo_basis<double>(G, sb);
   __syncthreads();
+  grid_dependency_wait();  // the state comes from the kernels before
   const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
   const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
   const double alpha[3] = {G.r[3 * (size_t)G.nv], G.r[3 * (size_t)G.nv + 1], G.r[3 * (size_t)G.nv + 2]};
@@ -2288,6 +2294,7 @@ __global__ void __launch_bounds__(kGeoThreads) geo_sums_ff_kernel(GeoArgs G) {
       c3s[gi][p] = FF{g.tab[2 * nrow + g.npt + p], g.tab[2 * nrow + 2 * g.npt + p]};
     }
   }
+  grid_dependency_wait();  // the state comes from the kernels before
   if (threadIdx.x < 3) {
     const double a = G.r[3 * (size_t)G.nv + threadIdx.x];
     alpha_s[threadIdx.x] = ff_of(a);
@@ -2408,6 +2415,7 @@ __global__ void __launch_bounds__(kGeoThreads) geo_sums_ff_kernel(GeoArgs G) {
 // contracted with the w, u, v rows (lanes = points, then lanes = control points).
 template <typename T>
 __global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__restrict__ partial) {
+  grid_dependency_wait();  // the coefficients come from the sums kernel, the partials from the face launches
   const double cA64 = G.gterm[kGeoCA], cV64 = G.gterm[kGeoCV];
   if (cA64 == 0.0 && cV64 == 0.0) return;
   __shared__ GeoBasis<T> sb;
@@ -2532,6 +2540,7 @@ __global__ void spmv_kernel(int nrow, const int *__restrict__ row_ptr, const int
                             const double *__restrict__ val, const double *__restrict__ scalev, double scale,
                             const double *__restrict__ alphas, const double *__restrict__ in, double *__restrict__ out,
                             int accumulate) {
+  grid_dependency_wait();
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -2581,6 +2590,7 @@ __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const i
                               const float *__restrict__ val, const double *__restrict__ scalev, double scale,
                               const double *__restrict__ alphas, const float4 *__restrict__ in4,
                               double *__restrict__ out, int accumulate) {
+  grid_dependency_wait();
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -2640,6 +2650,7 @@ __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const i
 
 // Rows of three doubles to float4 {x, y, z, 0}.
 __global__ void to_f32x4_kernel(int n, const double *__restrict__ in, float4 *__restrict__ out) {
+  grid_dependency_wait();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     out[i] = make_float4((float)in[3 * (size_t)i], (float)in[3 * (size_t)i + 1], (float)in[3 * (size_t)i + 2], 0.f);
 }
@@ -2656,6 +2667,24 @@ static int grid_for(int n, int per_block) {
 // device only, and the persistent grids follow each device's SM count, so
 // neither may be shared between the devices of one process.
 constexpr int kMaxDevices = 64;
+// Launch with programmatic stream serialization: the kernel may be scheduled
+// while the kernel before it on the stream drains, and waits for it in
+// grid_dependency_wait (which it calls before reading that kernel's results).
+template <typename... P, typename... A>
+static cudaError_t launch_after(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
+}
+
 struct PerDevice {
   std::once_flag once[kMaxDevices];
   int value[kMaxDevices] = {};
@@ -2736,15 +2765,13 @@ cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int
   const float *rhi = f.hi, *rlo = f.lo, *dsp = f.dsp;
   if constexpr (sizeof(T) == 4) {
     if (!rhi || !rlo || !dsp) return cudaErrorInvalidValue;
-    if (ncp == 12 && npt == 15) {
-      dev::face_tpf_kernel<<<grid, dev::tpf::kThreads, dev::tpf::kSumBytes, s>>>(L, dest, P, r, rhi, rlo, dsp,
-                                                                              partial, blockpart, status, fin);
-      return cudaGetLastError();
-    }
+    if (ncp == 12 && npt == 15)
+      return launch_after(dev::face_tpf_kernel, grid, dev::tpf::kThreads, dev::tpf::kSumBytes, s, L, dest, P, r, rhi,
+                          rlo, dsp, partial, blockpart, status, fin);
   }
   if (ncp == 12 && npt == 15)
-    dev::face_kernel<T, 12, 15><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status,
-                                                           fin);
+    return launch_after(dev::face_kernel<T, 12, 15>, grid, NT, 0, s, L, dest, P, r, rhi, rlo, dsp, partial, blockpart,
+                        status, fin);
   else if (ncp == 11 && npt == 16)
     dev::face_kernel<T, 11, 16><<<grid, NT, 0, s>>>(L, dest, P, r, rhi, rlo, dsp, partial, blockpart, status,
                                                            fin);
@@ -2791,9 +2818,8 @@ template cudaError_t launch_gather<float>(int, const float *, const int *, doubl
 template <typename T>
 cudaError_t launch_gather_step(int nv, const T *partial, const int *off, const StepArgs &a, const uint64_t *cnt,
                                double *r, double *p, const F32Pos &f, const int *status, cudaStream_t s) {
-  dev::gather_step_kernel<T><<<grid_for(nv, 256), 256, 0, s>>>(nv, partial, off, a, cnt, r, p, f.hi, f.lo, f.r0,
-                                                               f.dsp, status);
-  return cudaGetLastError();
+  return launch_after(dev::gather_step_kernel<T>, grid_for(nv, 256), 256, 0, s, nv, partial, off, a, cnt, r, p, f.hi,
+                      f.lo, f.r0, f.dsp, status);
 }
 template cudaError_t launch_gather_step<double>(int, const double *, const int *, const StepArgs &, const uint64_t *,
                                                 double *, double *, const F32Pos &, const int *, cudaStream_t);
@@ -2802,13 +2828,12 @@ template cudaError_t launch_gather_step<float>(int, const float *, const int *, 
 
 cudaError_t launch_kick(int nv, const StepArgs &a, const uint64_t *cnt, double *p, const double *g, const int *status,
                         cudaStream_t s) {
-  dev::kick_kernel<<<grid_for(nv, 256), 256, 0, s>>>(nv, a, cnt, p, g, status);
-  return cudaGetLastError();
+  return launch_after(dev::kick_kernel, grid_for(nv, 256), 256, 0, s, nv, a, cnt, p, g, status);
 }
 cudaError_t launch_drift(int nv, const StepArgs &a, double *r, double *p, const double *qdot, const F32Pos &f,
                          const int *status, cudaStream_t s) {
-  dev::drift_kernel<<<grid_for(3 * nv, 256), 256, 0, s>>>(nv, a, r, p, qdot, f.hi, f.lo, f.r0, f.dsp, status);
-  return cudaGetLastError();
+  return launch_after(dev::drift_kernel, grid_for(3 * nv, 256), 256, 0, s, nv, a, r, p, qdot, f.hi, f.lo, f.r0, f.dsp,
+                      status);
 }
 cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
                           double scale, const double *alphas, const float4 *in, double *out, int accumulate,
@@ -2817,16 +2842,14 @@ cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const fl
   int warps_per_block = 8;
   int grid = grid_for(nrow, warps_per_block);
   if (grid > 152 * 16) grid = 152 * 16;
-  dev::spmv32_kernel<<<grid, 32 * warps_per_block, 0, s>>>(nrow, row_ptr, col, val, scalev, scale, alphas, in, out,
-                                                          accumulate);
-  return cudaGetLastError();
+  return launch_after(dev::spmv32_kernel, grid, 32 * warps_per_block, 0, s, nrow, row_ptr, col, val, scalev, scale,
+                      alphas, in, out, accumulate);
 }
 
 cudaError_t launch_to_f32x4(int n, const double *in, float4 *out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int g = grid_for(n, 256);
-  dev::to_f32x4_kernel<<<g < 152 * 8 ? g : 152 * 8, 256, 0, s>>>(n, in, out);
-  return cudaGetLastError();
+  return launch_after(dev::to_f32x4_kernel, g < 152 * 8 ? g : 152 * 8, 256, 0, s, n, in, out);
 }
 
 cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const double *val, const double *scalev,
@@ -2836,32 +2859,13 @@ cudaError_t launch_spmv(int nrow, const int *row_ptr, const int *col, const doub
   int warps_per_block = 8;
   int grid = grid_for(nrow, warps_per_block);
   if (grid > 152 * 16) grid = 152 * 16;
-  dev::spmv_kernel<<<grid, 32 * warps_per_block, 0, s>>>(nrow, row_ptr, col, val, scalev, scale, alphas, in, out,
-                                                        accumulate);
-  return cudaGetLastError();
+  return launch_after(dev::spmv_kernel, grid, 32 * warps_per_block, 0, s, nrow, row_ptr, col, val, scalev, scale,
+                      alphas, in, out, accumulate);
 }
 
 }  // namespace umcp
 
 namespace umcp {
-
-// Launch with programmatic stream serialization: the kernel may be scheduled
-// while the kernel before it on the stream drains, and waits for it in
-// grid_dependency_wait (which it calls before reading that kernel's results).
-template <typename... P, typename... A>
-static cudaError_t launch_after(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
-}
 
 template <typename T>
 int batch_face_blocks(int ncp, int npt) {
@@ -2950,16 +2954,14 @@ cudaError_t launch_batch_pack(const BatchJob *jobs, const BatchTile *vtiles, con
 namespace umcp {
 
 cudaError_t launch_geo_sums(const GeoArgs &G, bool alpha64, cudaStream_t s) {
-  if (alpha64) dev::geo_sums_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
-  else dev::geo_sums_ff_kernel<<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G);
-  return cudaGetLastError();
+  return alpha64 ? launch_after(dev::geo_sums_kernel, geo_blocks(G.nfaces), kGeoThreads, 0, s, G)
+                 : launch_after(dev::geo_sums_ff_kernel, geo_blocks(G.nfaces), kGeoThreads, 0, s, G);
 }
 
 template <typename T>
 cudaError_t launch_geo_grad(const GeoArgs &G, T *partial, cudaStream_t s) {
   if (G.nfaces <= 0) return cudaSuccess;
-  dev::geo_grad_kernel<T><<<geo_blocks(G.nfaces), kGeoThreads, 0, s>>>(G, partial);
-  return cudaGetLastError();
+  return launch_after(dev::geo_grad_kernel<T>, geo_blocks(G.nfaces), kGeoThreads, 0, s, G, partial);
 }
 template cudaError_t launch_geo_grad<double>(const GeoArgs &, double *, cudaStream_t);
 template cudaError_t launch_geo_grad<float>(const GeoArgs &, float *, cudaStream_t);
