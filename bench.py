@@ -86,10 +86,10 @@ E2E_GROUPS = 3
 E2E_REPEATS = 3  # K-step e2e runs; the median is reported
 # DRAM bytes per face of the batched face launches, from the ncu capture of
 # the first 64 vesicles of the workload at 512-face tiles (dram__bytes_read.sum
-# + dram__bytes_write.sum of the regular and valence-5 launches: 86.26 +
-# 25.68 + 2.79 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
+# + dram__bytes_write.sum of the regular and valence-5 launches: 86.48 +
+# 26.64 + 2.79 + 0.01 MB over 392,960 faces); the benchmark's pass is scaled
 # from it by its face count.
-BATCH_FACE_DRAM_BYTES_PER_FACE = 114.74e6 / 392960
+BATCH_FACE_DRAM_BYTES_PER_FACE = 115.92e6 / 392960
 
 
 def parse_args():
