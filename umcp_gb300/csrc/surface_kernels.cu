@@ -2273,25 +2273,162 @@ __device__ __forceinline__ FF ff_of(double x) {
 // sums) and summed in float-float per thread; the area and the box-scale
 // derivatives from the FP32 leading parts with Kahan sums. FP64 enters only in
 // the per-block and final sums.
-__global__ void __launch_bounds__(kGeoThreads) geo_sums_ff_kernel(GeoArgs G) {
-  __shared__ float Bh[3][kGeoPt][3][kMaxCpDev], Bl[3][kGeoPt][3][kMaxCpDev];
-  __shared__ FF c3s[3][kGeoPt];
-  __shared__ float cws[3][kGeoPt];
-  __shared__ float Xh[kGeoHW][kMaxCpDev][3], Xl[kGeoHW][kMaxCpDev][3];
-  __shared__ double red[kGeoWords][kGeoThreads];
+//
+// One face per thread. Each thread keeps its face's
+// float-float local coordinates in its own columns of shared memory
+// (coordinate-major, control points padded to 16, the column 400 bytes, an
+// odd number of 16-byte chunks, so a warp's 16-byte reads do not conflict),
+// and walks the face's points; the value and derivative rows of the point
+// (hi and lo) are the same for every thread of a warp that is on the same
+// patch type, so they come out of shared memory as broadcasts. (A half-warp
+// form, lanes = points with per-lane row reads, took 177.6 us on a 40,962-vertex
+// vesicle against 154.5 us for this one, both issue-bound on the float-float
+// arithmetic.)
+namespace geo_tpf {
+constexpr int kThreads = 128;
+constexpr int kCp = 16;                  // control points, padded
+constexpr int kCol = 3 * kCp * 2 + 4;    // floats of a thread's column: hi [3][16], lo [3][16], pad
+struct Rows {
+  float4 r[3][kGeoPt][6][kCp / 4];       // [group][point][w hi, w lo, u hi, u lo, v hi, v lo][control points in fours]
+  float cw[3][kGeoPt];
+  FF c3[3][kGeoPt];
+};
+constexpr size_t kDynBytes = sizeof(float) * kCol * kThreads;
+}  // namespace geo_tpf
+
+template <int NCP, int NPT>
+__device__ __forceinline__ void geo_face_ff(const GeoArgs &G, const GeoGroup &g, const geo_tpf::Rows &rows, int gi,
+                                            int lf, const FF alpha[3], const float ialpha[3], float *col, FF &accV,
+                                            float ks[kGeoWords], float kc[kGeoWords]) {
+  using namespace geo_tpf;
+  auto kahan = [&](int q, float v) {
+    const float y = v - kc[q], t = ks[q] + y;
+    kc[q] = (t - ks[q]) - y;
+    ks[q] = t;
+  };
+  // ---- local coordinates (float-float, relative to the corner, in their images, times alpha)
+  const uint32_t *cp = g.cp + (size_t)lf * NCP;
+  float ahi[3], alo[3];
+  {
+    const int v0 = (int)(__ldg(&cp[0]) & kVertexMask);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { ahi[c] = G.rhi[3 * (size_t)v0 + c]; alo[c] = G.rlo[3 * (size_t)v0 + c]; }
+  }
+  FF X0[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) X0[c] = ff_mul(alpha[c], FF{ahi[c], alo[c]});  // the corner carries no image
+#pragma unroll
+  for (int j = 0; j < kCp; ++j) {
+    float xh[3] = {0.f, 0.f, 0.f}, xl[3] = {0.f, 0.f, 0.f};
+    if (j < NCP) {
+      const uint32_t packed = __ldg(&cp[j]);
+      const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
+      const int img[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float hi = G.rhi[3 * (size_t)v + c], lo = G.rlo[3 * (size_t)v + c];
+        float sh = 0.f, she = 0.f, shl = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          float t, e;
+          two_sum(sh, __fmul_rn((float)img[d], G.box_hi[d][c]), t, e);
+          sh = t;
+          she = __fadd_rn(she, e);
+          shl = __fadd_rn(shl, __fmul_rn((float)img[d], G.box_lo[d][c]));
+        }
+        float s1, e1, s2, e2;
+        two_sum(hi, sh, s1, e1);
+        two_sum(s1, -ahi[c], s2, e2);
+        const float res = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fsub_rn(lo, alo[c]), __fadd_rn(she, shl)));
+        const FF x = ff_mul(alpha[c], ff_fast_two_sum(s2, res));
+        xh[c] = x.hi;
+        xl[c] = x.lo;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      col[c * kCp + j] = xh[c];
+      col[3 * kCp + c * kCp + j] = xl[c];
+    }
+  }
+  // ---- the points
+#pragma unroll 1
+  for (int p = 0; p < NPT; ++p) {
+    FF R[3] = {{0, 0}, {0, 0}, {0, 0}}, Ru[3] = {{0, 0}, {0, 0}, {0, 0}}, Rv[3] = {{0, 0}, {0, 0}, {0, 0}};
+#pragma unroll
+    for (int q = 0; q < (NCP + 3) / 4; ++q) {
+      const float4 w4h = rows.r[gi][p][0][q], w4l = rows.r[gi][p][1][q], u4h = rows.r[gi][p][2][q],
+                   u4l = rows.r[gi][p][3][q], v4h = rows.r[gi][p][4][q], v4l = rows.r[gi][p][5][q];
+      const float wh[4] = {w4h.x, w4h.y, w4h.z, w4h.w}, wl[4] = {w4l.x, w4l.y, w4l.z, w4l.w};
+      const float uh[4] = {u4h.x, u4h.y, u4h.z, u4h.w}, ul[4] = {u4l.x, u4l.y, u4l.z, u4l.w};
+      const float vh[4] = {v4h.x, v4h.y, v4h.z, v4h.w}, vl[4] = {v4l.x, v4l.y, v4l.z, v4l.w};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float4 x4h = *reinterpret_cast<const float4 *>(&col[c * kCp + 4 * q]);
+        const float4 x4l = *reinterpret_cast<const float4 *>(&col[3 * kCp + c * kCp + 4 * q]);
+        const float xh[4] = {x4h.x, x4h.y, x4h.z, x4h.w}, xl[4] = {x4l.x, x4l.y, x4l.z, x4l.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          if (4 * q + jj >= NCP) break;
+          ff_acc(R[c], wh[jj], wl[jj], xh[jj], xl[jj]);
+          ff_acc(Ru[c], uh[jj], ul[jj], xh[jj], xl[jj]);
+          ff_acc(Rv[c], vh[jj], vl[jj], xh[jj], xl[jj]);
+        }
+      }
+    }
+    FF Ra[3], m[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Ru[c] = ff_norm(Ru[c]);
+      Rv[c] = ff_norm(Rv[c]);
+      Ra[c] = ff_add(X0[c], ff_norm(R[c]));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int a = (c + 1) % 3, b = (c + 2) % 3;
+      const FF t = ff_mul(Ru[b], Rv[a]);
+      m[c] = ff_add(ff_mul(Ru[a], Rv[b]), FF{-t.hi, -t.lo});
+    }
+    const FF dot = ff_add(ff_add(ff_mul(Ra[0], m[0]), ff_mul(Ra[1], m[1])), ff_mul(Ra[2], m[2]));
+    accV = ff_add(accV, ff_mul(rows.c3[gi][p], dot));
+    // area and box-scale derivatives from the leading parts
+    const float Rf[3] = {Ra[0].hi, Ra[1].hi, Ra[2].hi}, Uf[3] = {Ru[0].hi, Ru[1].hi, Ru[2].hi},
+                Vf[3] = {Rv[0].hi, Rv[1].hi, Rv[2].hi}, mf[3] = {m[0].hi, m[1].hi, m[2].hi};
+    const float gg2 = mf[0] * mf[0] + mf[1] * mf[1] + mf[2] * mf[2];
+    const float ig = rsqrtf(gg2), gg = gg2 * ig;
+    const float cwf = rows.cw[gi][p], c3f = rows.c3[gi][p].hi;
+    kahan(0, cwf * gg);
+    float n[3] = {mf[0] * ig, mf[1] * ig, mf[2] * ig}, a1[3], a2[3], v1[3], v2[3];
+    cross3(Vf, n, a1);
+    cross3(n, Uf, a2);
+    cross3(Vf, Rf, v1);
+    cross3(Rf, Uf, v2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      kahan(2 + k, cwf * (a1[k] * Uf[k] + a2[k] * Vf[k]) * ialpha[k]);
+      kahan(5 + k, c3f * (mf[k] * Rf[k] + v1[k] * Uf[k] + v2[k] * Vf[k]) * ialpha[k]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(geo_tpf::kThreads, 3) geo_sums_ff_tpf_kernel(GeoArgs G) {
+  using namespace geo_tpf;
+  __shared__ Rows rows;
   __shared__ FF alpha_s[3];
   __shared__ float ialpha_s[3];
-  for (int gi = 0; gi < G.ngroups; ++gi) {
+  extern __shared__ __align__(16) float geo_cols[];
+  for (int gi = 0; gi < G.ngroups; ++gi) {  // rows hi/lo, control points padded with zeros
     const GeoGroup &g = G.g[gi];
     const int nrow = g.npt * 3 * g.ncp;
-    for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
-      const int p = i / (3 * g.ncp), k = (i / g.ncp) % 3, x = i % g.ncp;
-      Bh[gi][p][k][x] = g.tab[i];
-      Bl[gi][p][k][x] = g.tab[nrow + i];
+    float *r = &rows.r[gi][0][0][0].x;
+    for (int i = threadIdx.x; i < g.npt * 6 * kCp; i += blockDim.x) {
+      const int p = i / (6 * kCp), k = (i / kCp) % 6, x = i % kCp;  // k: row (w, u, v) * 2 + lo
+      const int e = p * 3 * g.ncp + (k / 2) * g.ncp + x;
+      r[((size_t)p * 6 + k) * kCp + x] = x < g.ncp ? g.tab[(k & 1) * nrow + e] : 0.f;
     }
     for (int p = threadIdx.x; p < g.npt; p += blockDim.x) {
-      cws[gi][p] = g.tab[2 * nrow + p];
-      c3s[gi][p] = FF{g.tab[2 * nrow + g.npt + p], g.tab[2 * nrow + 2 * g.npt + p]};
+      rows.cw[gi][p] = g.tab[2 * nrow + p];
+      rows.c3[gi][p] = FF{g.tab[2 * nrow + g.npt + p], g.tab[2 * nrow + 2 * g.npt + p]};
     }
   }
   grid_dependency_wait();  // the state comes from the kernels before
@@ -2301,112 +2438,26 @@ __global__ void __launch_bounds__(kGeoThreads) geo_sums_ff_kernel(GeoArgs G) {
     ialpha_s[threadIdx.x] = 1.f / (float)a;
   }
   __syncthreads();
-  const int hw = threadIdx.x >> 4, lane = threadIdx.x & 15;
-  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
   const FF alpha[3] = {alpha_s[0], alpha_s[1], alpha_s[2]};
   const float ialpha[3] = {ialpha_s[0], ialpha_s[1], ialpha_s[2]};
-  // V in float-float; A and the box-scale derivatives with Kahan-compensated FP32 sums
+  float *col = geo_cols + (size_t)kCol * threadIdx.x;
   FF accV = {0, 0};
   float ks[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0}, kc[kGeoWords] = {0, 0, 0, 0, 0, 0, 0, 0};
-  auto kahan = [&](int q, float v) {
-    const float y = v - kc[q], t = ks[q] + y;
-    kc[q] = (t - ks[q]) - y;
-    ks[q] = t;
-  };
-  for (int f = blockIdx.x * kGeoHW + hw; f < G.nfaces; f += gridDim.x * kGeoHW) {
+  for (int f = blockIdx.x * kThreads + threadIdx.x; f < G.nfaces; f += gridDim.x * kThreads) {
     int lf;
     const int gi = geo_group(G, f, &lf);
     const GeoGroup &g = G.g[gi];
-    // ---- lanes = control points: local coordinates relative to the corner
-    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
-    int img[3] = {0, 0, 0};
-    if (lane < g.ncp) {
-      const uint32_t packed = __ldg(&g.cp[(size_t)lf * g.ncp + lane]);
-      const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
-      img[0] = code % 3 - 1; img[1] = (code / 3) % 3 - 1; img[2] = code / 9 - 1;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) { hi[c] = G.rhi[3 * (size_t)v + c]; lo[c] = G.rlo[3 * (size_t)v + c]; }
-    }
-    FF X0[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float ahi = __shfl_sync(hmask, hi[c], 0, 16), alo = __shfl_sync(hmask, lo[c], 0, 16);
-      float sh = 0.f, she = 0.f, shl = 0.f;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        float t, e;
-        two_sum(sh, __fmul_rn((float)img[d], G.box_hi[d][c]), t, e);
-        sh = t;
-        she = __fadd_rn(she, e);
-        shl = __fadd_rn(shl, __fmul_rn((float)img[d], G.box_lo[d][c]));
-      }
-      float s1, e1, s2, e2;
-      two_sum(hi[c], sh, s1, e1);
-      two_sum(s1, -ahi, s2, e2);
-      const float res = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fsub_rn(lo[c], alo), __fadd_rn(she, shl)));
-      const FF xl = ff_mul(alpha[c], ff_fast_two_sum(s2, res));
-      if (lane < g.ncp) { Xh[hw][lane][c] = xl.hi; Xl[hw][lane][c] = xl.lo; }
-      X0[c] = ff_mul(alpha[c], FF{ahi, alo});  // the corner carries no image
-    }
-    __syncwarp(hmask);
-    // ---- lanes = quadrature points
-    if (lane < g.npt) {
-      FF R[3] = {{0, 0}, {0, 0}, {0, 0}}, Ru[3] = {{0, 0}, {0, 0}, {0, 0}}, Rv[3] = {{0, 0}, {0, 0}, {0, 0}};
-#pragma unroll
-      for (int x = 0; x < kMaxCpDev; ++x) {
-        if (x < g.ncp) {
-          const float wh = Bh[gi][lane][0][x], wl = Bl[gi][lane][0][x], uh = Bh[gi][lane][1][x],
-                      ul = Bl[gi][lane][1][x], vh = Bh[gi][lane][2][x], vl = Bl[gi][lane][2][x];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const float xh = Xh[hw][x][c], xl = Xl[hw][x][c];
-            ff_acc(R[c], wh, wl, xh, xl);
-            ff_acc(Ru[c], uh, ul, xh, xl);
-            ff_acc(Rv[c], vh, vl, xh, xl);
-          }
-        }
-      }
-      FF Ra[3], m[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Ru[c] = ff_norm(Ru[c]);
-        Rv[c] = ff_norm(Rv[c]);
-        Ra[c] = ff_add(X0[c], ff_norm(R[c]));
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int a = (c + 1) % 3, b = (c + 2) % 3;
-        const FF q = ff_mul(Ru[b], Rv[a]);
-        m[c] = ff_add(ff_mul(Ru[a], Rv[b]), FF{-q.hi, -q.lo});
-      }
-      const FF dot = ff_add(ff_add(ff_mul(Ra[0], m[0]), ff_mul(Ra[1], m[1])), ff_mul(Ra[2], m[2]));
-      const FF vol = ff_mul(c3s[gi][lane], dot);
-      accV = ff_add(accV, vol);
-      // area and box-scale derivatives from the leading parts
-      const float Rf[3] = {Ra[0].hi, Ra[1].hi, Ra[2].hi}, Uf[3] = {Ru[0].hi, Ru[1].hi, Ru[2].hi},
-                  Vf[3] = {Rv[0].hi, Rv[1].hi, Rv[2].hi}, mf[3] = {m[0].hi, m[1].hi, m[2].hi};
-      const float gg2 = mf[0] * mf[0] + mf[1] * mf[1] + mf[2] * mf[2];
-      const float ig = rsqrtf(gg2), gg = gg2 * ig;
-      const float cwf = cws[gi][lane], c3f = c3s[gi][lane].hi;
-      kahan(0, cwf * gg);
-      float n[3] = {mf[0] * ig, mf[1] * ig, mf[2] * ig}, a1[3], a2[3], v1[3], v2[3];
-      cross3(Vf, n, a1);
-      cross3(n, Uf, a2);
-      cross3(Vf, Rf, v1);
-      cross3(Rf, Uf, v2);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        kahan(2 + k, cwf * (a1[k] * Uf[k] + a2[k] * Vf[k]) * ialpha[k]);
-        kahan(5 + k, c3f * (mf[k] * Rf[k] + v1[k] * Uf[k] + v2[k] * Vf[k]) * ialpha[k]);
-      }
-    }
-    __syncwarp(hmask);
+    if (g.ncp == 12) geo_face_ff<12, 15>(G, g, rows, gi, lf, alpha, ialpha, col, accV, ks, kc);
+    else if (g.ncp == 11) geo_face_ff<11, 16>(G, g, rows, gi, lf, alpha, ialpha, col, accV, ks, kc);
+    else geo_face_ff<13, 16>(G, g, rows, gi, lf, alpha, ialpha, col, accV, ks, kc);
   }
   double acc[kGeoWords];
 #pragma unroll
   for (int q = 0; q < kGeoWords; ++q) acc[q] = (double)ks[q] - (double)kc[q];
   acc[1] = (double)accV.hi + (double)accV.lo;
-  geo_finish(G, acc, red);
+  __syncthreads();  // every column is done with: the block sums reuse their space
+  static_assert(kDynBytes >= sizeof(double) * kGeoWords * kThreads, "block sums must fit in the columns");
+  geo_finish(G, acc, reinterpret_cast<double(*)[kThreads]>(geo_cols));
 }
 
 // partial[slot] += alpha * dE_r/dX for every (face, control point):
@@ -2954,8 +3005,15 @@ cudaError_t launch_batch_pack(const BatchJob *jobs, const BatchTile *vtiles, con
 namespace umcp {
 
 cudaError_t launch_geo_sums(const GeoArgs &G, bool alpha64, cudaStream_t s) {
-  return alpha64 ? launch_after(dev::geo_sums_kernel, geo_blocks(G.nfaces), kGeoThreads, 0, s, G)
-                 : launch_after(dev::geo_sums_ff_kernel, geo_blocks(G.nfaces), kGeoThreads, 0, s, G);
+  if (alpha64) return launch_after(dev::geo_sums_kernel, geo_blocks(G.nfaces), kGeoThreads, 0, s, G);
+  // the thread-per-face form: a grid that depends on the face count only (the sums' order is fixed)
+  const cudaError_t e = cudaFuncSetAttribute(dev::geo_sums_ff_tpf_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)dev::geo_tpf::kDynBytes);
+  if (e != cudaSuccess) return e;
+  const int per_block = dev::geo_tpf::kThreads, want = (G.nfaces + per_block - 1) / per_block;
+  const int grid = want < 1 ? 1 : (want < geo_blocks(G.nfaces) ? want : geo_blocks(G.nfaces));
+  return launch_after(dev::geo_sums_ff_tpf_kernel, grid, dev::geo_tpf::kThreads, dev::geo_tpf::kDynBytes, s, G);
 }
 
 template <typename T>
