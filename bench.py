@@ -519,7 +519,7 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
     if mi.dense:
         apply_bytes = 4.0 * plan.nv * plan.nv + 8.0 * n3 * 2 + 4.0 * n3
     else:
-        apply_bytes = 8.0 * mi.nnz_inverse + 4.0 * (plan.nv + 1) + 8.0 * n3 * 2 + 4.0 * n3
+        apply_bytes = (6.0 if plan.nv <= 65536 else 8.0) * mi.nnz_inverse + 4.0 * (plan.nv + 1) + 8.0 * n3 * 2 + 4.0 * n3
     gbs = apply_bytes / (ms_apply * 1e-3) / 1e9
     return {"workload": "Langevin with the limit-surface M^-1 on a 40,962-vertex vesicle (R 1000 A, noise 2 A, "
                         "kc 20 kT), area and volume restraints, gamma 1/ps, FP32 form",
@@ -534,7 +534,8 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
             "minv_dense": bool(mi.dense), "minv_nnz": int(mi.nnz_inverse),
             "minv_fill": mi.nnz_inverse / plan.nv ** 2,
             "minv_apply": {"ms": ms_apply, "bytes": apply_bytes, "gbs": gbs, "hbm_frac": gbs / peak_gbs,
-                           "storage": "FP32 values, int32 columns (CSR)" if not mi.dense else "FP32 dense"}}
+                           "storage": ("FP32 dense" if mi.dense else "FP32 values, %s columns (CSR)"
+                                       % ("uint16" if plan.nv <= 65536 else "int32"))}}
 
 
 def engine_arm(args) -> None:
@@ -939,11 +940,12 @@ def geo_mode(args) -> None:
 
 def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool) -> int:
     """Algorithmic bytes of one apply, out += M^-1 in on 3 components per row:
-    CSR 8 per nonzero (FP32 value and column; 12 in FP64) plus, per row, the
+    CSR 6 per nonzero (FP32 value and a 16-bit column, up to 65,536 rows; 8
+    with 32-bit columns; 12 in FP64) plus, per row, the
     row pointer (4), the input gathered at least once (16 as the packed FP32
     copy, 24 in FP64) and the output read and written (48); dense 4 (or 8) per
     entry plus the same per row."""
-    per_entry = (4 if fp32 else 8) if dense else (8 if fp32 else 12)
+    per_entry = (4 if fp32 else 8) if dense else ((6 if nrow <= 65536 else 8) if fp32 else 12)
     entries = nrow * nrow if dense else nnz
     per_row = (0 if dense else 4) + (16 if fp32 else 24) + 48
     return per_entry * entries + per_row * nrow

@@ -270,3 +270,35 @@ def test_tensor_core_face_kernel_matches_reference(ctx, name):
     prm.face_kernel = U.SIMT
     e_simt = U.Mesh(ctx, plan, prm).run(it, 0, 40)
     assert np.all(np.isfinite(e)) and np.max(np.abs(e - e_simt)) <= 1e-5 * np.max(np.abs(e_simt))
+
+
+def test_precision_form_mass_set_applies_in_fp32(ctx):
+    """A CSR installed on a mesh of the FP32 form (FP32 values, 16-bit columns)
+    applies within 1e-6 of sum_j |M_ij| |x_j| of the FP64 mesh's apply of the
+    same CSR, on rows of every length mod 4, and reads back as installed."""
+    plan, prm, _ = load_case("ico3_plain")
+    _, prm32, _ = load_case("ico3_plain", U.FP32_CENTRED)
+    m64, m32 = U.Mesh(ctx, plan, prm), U.Mesh(ctx, plan, prm32)
+    rng = np.random.default_rng(5)
+    rows, cols, vals = [], [], []
+    for i in range(plan.nv):  # row lengths 1 .. 9, every residue mod 4
+        js = np.unique(np.concatenate([[i], rng.choice(plan.nv, i % 9, replace=False)]))
+        rows.append(len(js))
+        cols.extend(js)
+        vals.extend(rng.normal(0, 1, len(js)) + (js == i) * 5.0)
+    rp = np.concatenate([[0], np.cumsum(rows)]).astype(np.int32)
+    cl, vl = np.array(cols, dtype=np.int32), np.array(vals)
+    assert len({int(n) % 4 for n in np.diff(rp)}) == 4
+    m64.mass_set(rp, cl, vl)
+    m32.mass_set(rp, cl, vl)
+    vin = rng.normal(0, 1, 3 * plan.nv)
+    base = rng.normal(0, 1, 3 * plan.nv)
+    dense = np.zeros((plan.nv, plan.nv))
+    for i in range(plan.nv):
+        for k in range(rp[i], rp[i + 1]):
+            dense[i, cl[k]] += vl[k]
+    bound = (np.abs(dense) @ np.abs(vin.reshape(-1, 3))).reshape(-1)
+    want = m64.mass_apply(vin, base.copy(), None, 1.0, (1, 1, 1))
+    got = m32.mass_apply(vin, base.copy(), None, 1.0, (1, 1, 1))
+    assert np.all(np.abs(got - want) <= 1e-6 * bound + 1e-12 * np.abs(base))
+    assert np.array_equal(m32.mass_get(), dense.astype(np.float32).astype(np.float64))

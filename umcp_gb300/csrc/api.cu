@@ -887,8 +887,10 @@ extern "C" umcp_status umcp_mass_set(umcp_mesh *m, int nrow, const int *row_ptr,
     if (col[k] < 0 || col[k] >= m->nv) return fail(UMCP_ERR_INVALID, "column index out of range");
   UMCP_CUDA(cudaSetDevice(m->ctx->device));
   UMCP_CUDA(upload(m->mrow, std::vector<int>(row_ptr, row_ptr + nrow + 1)));
-  UMCP_CUDA(upload(m->mcol, std::vector<int>(col, col + nnz)));
   m->mass_f32 = m->precision == UMCP_FP32_CENTRED;  // the precision form applies M^-1 in FP32
+  m->mcol16 = m->mass_f32 && nrow <= 65536;         // and stores its columns in 16 bits when they fit
+  if (m->mcol16) UMCP_CUDA(upload(m->mcol, std::vector<uint16_t>(col, col + nnz)));
+  else UMCP_CUDA(upload(m->mcol, std::vector<int>(col, col + nnz)));
   if (m->mass_f32) UMCP_CUDA(upload(m->mval, std::vector<float>(val, val + nnz)));
   else UMCP_CUDA(upload(m->mval, std::vector<double>(val, val + nnz)));
   UMCP_CUDA(m->min32.alloc(m->mass_f32 ? (size_t)nrow * sizeof(float4) : 0));

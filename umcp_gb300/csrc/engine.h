@@ -124,6 +124,9 @@ struct umcp_mesh {
   int mrows = 0;
   umcp::DevBuf mrow, mcol, mval, alphas, mdense, min32;
   bool mass_dense = false, mass_f32 = false;
+  // the FP32 CSR's column indices as uint16 (meshes of at most 65,536 vertices:
+  // 6 bytes per nonzero instead of 8 for an apply that HBM bounds)
+  bool mcol16 = false;
   // captured step sequences, by length (powers of two up to kGraphChunk steps)
   struct CachedGraph {
     cudaGraphExec_t exec = nullptr;

@@ -216,7 +216,7 @@ int batch_face_blocks(int ncp, int npt);
 // accumulate=0 overwrites out. alphas: device pointer to 3 doubles (or NULL = 1).
 // launch_spmv on FP32 values and an FP32 input packed as float4 {x, y, z, 0}
 // per row (spmv32_kernel).
-cudaError_t launch_spmv32(int nrow, const int *row_ptr, const int *col, const float *val, const double *scalev,
+cudaError_t launch_spmv32(int nrow, const int *row_ptr, const void *col, bool col16, const float *val, const double *scalev,
                           double scale, const double *alphas, const float4 *in, double *out, int accumulate,
                           cudaStream_t s);
 // out[i] = {(float)in[3i], (float)in[3i+1], (float)in[3i+2], 0}, i < n.

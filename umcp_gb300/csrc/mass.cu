@@ -270,9 +270,9 @@ __global__ void row_count_kernel(int n, const double *__restrict__ A, int *__res
 // CSR of the truncated inverse, columns ascending within each row (one warp
 // per row: a ballot over 32 columns at a time gives each kept entry its
 // place). V is double (plain path) or float (precision form, rounded once).
-template <typename V>
+template <typename V, typename C>  // C: int, or uint16_t for up to 65,536 columns
 __global__ void row_fill_kernel(int n, const double *__restrict__ A, const int *__restrict__ row_ptr,
-                                int *__restrict__ col, V *__restrict__ val) {
+                                C *__restrict__ col, V *__restrict__ val) {
   const int lane = threadIdx.x & 31;
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
     const double *row = A + (size_t)i * n;
@@ -283,7 +283,7 @@ __global__ void row_fill_kernel(int n, const double *__restrict__ A, const int *
       const unsigned keep = __ballot_sync(0xffffffffu, a != 0.0);
       if (a != 0.0) {
         const int at = w + __popc(keep & ((1u << lane) - 1u));
-        col[at] = j;
+        col[at] = (C)j;
         val[at] = (V)a;
       }
       w += __popc(keep);
@@ -304,7 +304,7 @@ cudaError_t umcp::queue_mass_apply(umcp_mesh *m, const double *scalev, double sc
     cudaError_t e = launch_to_f32x4(m->mrows, in, m->min32.as<float4>(), s);
     if (e != cudaSuccess) return e;
     if (!m->mass_dense)
-      return launch_spmv32(m->mrows, m->mrow.as<int>(), m->mcol.as<int>(), m->mval.as<float>(), scalev, scale, alphas,
+      return launch_spmv32(m->mrows, m->mrow.as<int>(), m->mcol.p, m->mcol16, m->mval.as<float>(), scalev, scale, alphas,
                            m->min32.as<float4>(), out, accumulate, s);
   }
   if (m->mass_dense) {
@@ -427,6 +427,7 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
       std::swap(m->mdense.bytes, A.bytes);
     }
     m->mass_dense = true;
+    m->mcol16 = false;
     UMCP_CUDA(m->mrow.alloc(0));
     UMCP_CUDA(m->mcol.alloc(0));
     UMCP_CUDA(m->mval.alloc(0));
@@ -444,14 +445,18 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
     for (int i = 0; i < n; ++i) rp[(size_t)i + 1] = rp[i] + cnt[i];
     if ((unsigned long long)rp[n] != kept) return fail(UMCP_ERR_CUDA, "M^-1 nonzero count mismatch between the truncation and the CSR pass");
     UMCP_CUDA(upload(m->mrow, rp));
-    UMCP_CUDA(m->mcol.alloc(kept * sizeof(int)));
+    m->mcol16 = f32 && n <= 65536;
+    UMCP_CUDA(m->mcol.alloc(kept * (m->mcol16 ? sizeof(uint16_t) : sizeof(int))));
     UMCP_CUDA(m->mval.alloc(kept * (f32 ? sizeof(float) : sizeof(double))));
-    if (f32)
-      row_fill_kernel<float><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
-                                                    m->mval.as<float>());
+    if (m->mcol16)
+      row_fill_kernel<float, uint16_t><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(),
+                                                              m->mcol.as<uint16_t>(), m->mval.as<float>());
+    else if (f32)
+      row_fill_kernel<float, int><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
+                                                         m->mval.as<float>());
     else
-      row_fill_kernel<double><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
-                                                     m->mval.as<double>());
+      row_fill_kernel<double, int><<<sms * 8, 256, 0, s>>>(n, A.as<double>(), m->mrow.as<int>(), m->mcol.as<int>(),
+                                                          m->mval.as<double>());
     UMCP_CUDA(cudaGetLastError());
     UMCP_CUDA(cudaStreamSynchronize(s));
     UMCP_CUDA(m->mdense.alloc(0));
@@ -500,7 +505,13 @@ extern "C" umcp_status umcp_mass_get(umcp_mesh *m, double *dense) {
   std::vector<int> cl((size_t)rp[n]);
   std::vector<double> vl((size_t)rp[n]);
   if (rp[n] > 0) {
-    UMCP_CUDA(cudaMemcpy(cl.data(), m->mcol.p, cl.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    if (m->mcol16) {
+      std::vector<uint16_t> c16(cl.size());
+      UMCP_CUDA(cudaMemcpy(c16.data(), m->mcol.p, c16.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < cl.size(); ++k) cl[k] = c16[k];
+    } else {
+      UMCP_CUDA(cudaMemcpy(cl.data(), m->mcol.p, cl.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    }
     if (m->mass_f32) {
       std::vector<float> v32(vl.size());
       UMCP_CUDA(cudaMemcpy(v32.data(), m->mval.p, v32.size() * sizeof(float), cudaMemcpyDeviceToHost));
