@@ -5,9 +5,8 @@ Tolerances (written here, used below):
   FP64 plain path: energy |dE|/|E| <= 1e-10; gradient max|dg|/max|g| <= 1e-10.
   FP32 face-centred form: energy |dE|/|E| <= 1e-6; gradient max|dg|/max|g| <= 1e-6
   and ||dg||/||g|| <= 1e-6.
-  FP32 form on the tensor-core kernel (an option, not the default): energy
-  <= 1e-6, gradient max|dg|/max|g| <= 3e-5 (its tangents carry fp16-split
-  rounding into the area strain).
+  FP32 form on the tensor-core kernel (an option, not the default): the same
+  bounds (energy 1e-6, gradient 1e-6 in both norms).
   Integrator steps (FP64, same Philox draws as the oracle): positions to 1e-12
   of the largest coordinate.
 """
@@ -24,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 E64, G64 = 1e-10, 1e-10
 E32, G32 = 1e-6, 1e-6
-GTC = 3e-5
+GTC = 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -262,7 +261,7 @@ def test_tensor_core_face_kernel_matches_reference(ctx, name):
     r = gold["r"]
     E, g = mesh.energy_grad(r)
     assert abs(E - gold["E"]) <= E32 * abs(gold["E"])
-    assert rel_inf(g[:-3], gold["grad"][:-3]) <= GTC
+    assert rel_inf(g[:-3], gold["grad"][:-3]) <= GTC and rel_l2(g[:-3], gold["grad"][:-3]) <= GTC
     E2, g2 = mesh.energy_grad(r)
     assert E2 == E and np.array_equal(g2, g)
     it = U.integrator(U.OVERDAMPED_BD, time_step=1.0, D=0.00125, seed=3)

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 # (energy, gradient) bounds, as in test_gpu_parity: FP64, the FP32 form, and
 # the FP32 form on the tensor-core kernel
 TOL = {(U.FP64, U.SIMT): (1e-10, 1e-10), (U.FP32_CENTRED, U.SIMT): (1e-6, 1e-6),
-       (U.FP32_CENTRED, U.TENSOR_CORES): (1e-6, 3e-5)}
+       (U.FP32_CENTRED, U.TENSOR_CORES): (1e-6, 1e-6)}
 
 
 def _mesh(precision, face_kernel):

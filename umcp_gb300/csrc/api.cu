@@ -697,7 +697,7 @@ static cudaError_t queue_faces(umcp_mesh *m, const double *d_r, const FinishArgs
     if constexpr (sizeof(T) == 4) {
       if (G->tc)
         e = launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, m->rhi.as<float>(), m->rlo.as<float>(),
-                            m->partial.as<float>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
+                            m->dsp.as<float>(), m->partial.as<float>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
                             fin ? *fin : none, on);
       else
         e = launch_faces<T>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, m->f32pos(), m->partial.as<T>(), m->blockpart.as<double>(), m->status.as<int>(), G->nblocks,
@@ -1314,7 +1314,7 @@ extern "C" umcp_status umcp_energy_grad_static(umcp_mesh *m, const double *d_r, 
     L.dudv = G->dudv;
     L.irregular = G->irregular;
     const FinishArgs &f = fin;  // every block of every launch counts toward the finish
-    cudaError_t e = (fp32 && G->tc) ? launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, rhi, rlo,
+    cudaError_t e = (fp32 && G->tc) ? launch_faces_tc(L, G->dest.as<int>(), m->P, d_r, rhi, rlo, f32.dsp,
                                                        (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)
                     : fp32 ? launch_faces<float>(L, G->dest.as<int>(), G->ncp, G->npt, m->P, d_r, f32,
                                                (float *)(base + off_partial), blockpart, status, G->nblocks, f, s)

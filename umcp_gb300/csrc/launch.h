@@ -103,8 +103,8 @@ cudaError_t launch_faces(const dev::FaceLaunch &L, const int *dest, int ncp, int
 // tiles; grid from face_blocks_tc.
 int face_blocks_tc(int nfaces);
 cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev::SurfaceParams &P, const double *r,
-                            const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
-                            int grid, const FinishArgs &fin, cudaStream_t s);
+                            const float *rhi, const float *rlo, const float *dsp, float *partial, double *blockpart,
+                            int *status, int grid, const FinishArgs &fin, cudaStream_t s);
 
 // The precision form's FP32 positions of r: f.hi[i] + f.lo[i] = r[i] to about
 // 2^-48 relative, f.dsp[i] = r[i] - f.r0[i].

@@ -596,6 +596,8 @@ struct Smem {
   uint4 B1[kChunks][kN1 * kK1 / 8];
   uint4 B2[kChunks][kN2 * kK2 / 8];
   float xmax[2][3][kFaces];       // per-row maxima exchanged between the two thread halves
+  float Dd[3][kNcp][kFaces];      // control points' change from the reference state (FP32, per face)
+  float Buv[kNpt][2][kNcp];       // basis rows u, v in FP32, for the area strain's tangent changes
   float W[16];
   uint64_t mbar;
   uint32_t tmem;
@@ -736,6 +738,10 @@ __device__ void setup(Smem &sm, const double *__restrict__ basis, const double *
     b2[(size_t)j * kN2 * kK2 + core_off(n, k, kSbo2) / 2] = v;
   }
   if (tid < 16) sm.W[tid] = tid < kNpt ? (float)weight[tid] : 0.f;
+  for (int e = tid; e < kNpt * 2 * kNcp; e += kThreads) {
+    const int p = e / (2 * kNcp), k = (e / kNcp) % 2, x = e % kNcp;
+    sm.Buv[p][k][x] = (float)basis[((size_t)p * 5 + k) * kNcp + x];
+  }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sm.mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -794,7 +800,8 @@ __device__ __forceinline__ void gather_d2(uint32_t tmem, uint32_t lane_base, int
 // One tile of up to 128 faces [first, first + count) of source S. Returns
 // false if a wait gave up (the CTA then stops).
 __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const float alpha[3], const float ialpha[3],
-                     const Moduli<float> &mod, float dudv, int first, int count, float *__restrict__ partial,
+                     const float am1[3], const Moduli<float> &mod, float dudv, int first, int count,
+                     float *__restrict__ partial,
                      HalfWarpSums<float> &acc, uint32_t &phase) {
   const int tid = threadIdx.x, fs = tid & (kFaces - 1), h = tid >> 7;
   const uint32_t tmem = sm.tmem, lane_base = (uint32_t)(32 * ((tid >> 5) & 3)) << 16;
@@ -811,13 +818,16 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       const uint32_t *cp = S.cp + (size_t)f * kNcp;
       // the corner (control point 0) is in the home image: coordinates are relative to its hi/lo pair
       const int v0 = (int)(__ldg(&cp[0]) & kVertexMask);
-      float chi[3], clo[3];
+      float chi[3], clo[3], cd[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         chi[c] = S.rhi[3 * (size_t)v0 + c];
         clo[c] = S.rlo[3 * (size_t)v0 + c];
+        cd[c] = S.dsp[3 * (size_t)v0 + c];
       }
-      auto local = [&](uint32_t packed, float out[3]) {
+      // out = alpha L; with d given, d = (alpha - 1) L + (dsp - dsp of the corner), the change from
+      // the reference state (as in the thread-per-face kernel)
+      auto local = [&](uint32_t packed, float out[3], float *d = nullptr) {
         const int v = (int)(packed & kVertexMask), code = (int)(packed >> kVertexBits);
         const int im[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
 #pragma unroll
@@ -835,7 +845,9 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
           const float hi = S.rhi[3 * (size_t)v + c], lo = S.rlo[3 * (size_t)v + c];
           two_sum(hi, sh, s1, e1);
           two_sum(s1, -chi[c], s2, e2);
-          out[c] = alpha[c] * (s2 + ((e1 + e2) + ((lo - clo[c]) + (she + shl))));
+          const float l = s2 + ((e1 + e2) + ((lo - clo[c]) + (she + shl)));
+          out[c] = alpha[c] * l;
+          if (d) d[c] = fmaf(am1[c], l, S.dsp[3 * (size_t)v + c] - cd[c]);
         }
       };
       local(__ldg(&cp[1]), Ev);  // lattice (0,1)
@@ -844,10 +856,13 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       for (int i = 0; i < 8; ++i) {
         if (i < nx) {
           const int x = 8 * h + i;
-          float xl[3];
-          local(__ldg(&cp[x]), xl);
+          float xl[3], dx[3];
+          local(__ldg(&cp[x]), xl, dx);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) xp[i][c] = xl[c] - (float)kLatU[x] * Eu[c] - (float)kLatV[x] * Ev[c];
+          for (int c = 0; c < 3; ++c) {
+            xp[i][c] = xl[c] - (float)kLatU[x] * Eu[c] - (float)kLatV[x] * Ev[c];
+            sm.Dd[c][x][fs] = dx[c];
+          }
         }
       }
       P2 = S.compf[3 * (size_t)f];
@@ -933,9 +948,18 @@ __device__ bool tile(Smem &sm, const FaceSrc &S, const SurfaceParams &P, const f
       K[q][1].x += Ev[0]; K[q][1].y += Ev[1]; K[q][1].z += Ev[2];
       Vec3<float> Kb[5], Kreg[2];
       if (active && p < kNpt) {
+        // the tangents' change from the reference state, for the area strain
+        Vec3<float> dR[2] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int x = 0; x < kNcp; ++x) {
+          const float bu = sm.Buv[p][0][x], bv = sm.Buv[p][1][x];
+          const float d0 = sm.Dd[0][x][fs], d1 = sm.Dd[1][x][fs], d2 = sm.Dd[2][x][fs];
+          dR[0].x = fmaf(bu, d0, dR[0].x); dR[0].y = fmaf(bu, d1, dR[0].y); dR[0].z = fmaf(bu, d2, dR[0].z);
+          dR[1].x = fmaf(bv, d0, dR[1].x); dR[1].y = fmaf(bv, d1, dR[1].y); dR[1].z = fmaf(bv, d2, dR[1].z);
+        }
         float ea = 0, ec = 0, er = 0;
         point_adjoint<float>(K[q], sm.W[p], g0[q], rr0[q], dudv, P2, Hbar, Pres, mod.kc, mod.KA, mod.kg, mod.k_reg,
-                             &ea, &ec, &er, Kb, Kreg);
+                             &ea, &ec, &er, Kb, Kreg, dR);
         e3[0] += ea; e3[1] += ec; e3[2] += er;
       } else {
 #pragma unroll
@@ -1040,22 +1064,24 @@ static_assert(sizeof(double) * 6 * kThreads <= sizeof(uint4) * 3 * kFaces * kK2 
 // Single mesh: persistent CTAs over the 128-face tiles of the regular group.
 __global__ void __launch_bounds__(tc::kThreads, 2)
     face_tc_kernel(FaceLaunch L, const int *__restrict__ dest, SurfaceParams P, const double *__restrict__ r,
-                   const float *__restrict__ rhi, const float *__restrict__ rlo, float *__restrict__ partial,
-                   double *__restrict__ blockpart, int *__restrict__ status, FinishArgs fin) {
+                   const float *__restrict__ rhi, const float *__restrict__ rlo, const float *__restrict__ dsp,
+                   float *__restrict__ partial, double *__restrict__ blockpart, int *__restrict__ status,
+                   FinishArgs fin) {
   extern __shared__ uint8_t tc_smem_raw[];
   tc::Smem &sm = *reinterpret_cast<tc::Smem *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~(uintptr_t)1023);
   tc::setup(sm, L.basis, L.weight);
   const float alpha[3] = {(float)r[3 * P.nv], (float)r[3 * P.nv + 1], (float)r[3 * P.nv + 2]};
   const float ialpha[3] = {1.f / alpha[0], 1.f / alpha[1], 1.f / alpha[2]};
+  const float am1[3] = {(float)(r[3 * P.nv] - 1.0), (float)(r[3 * P.nv + 1] - 1.0), (float)(r[3 * P.nv + 2] - 1.0)};
   const Moduli<float> mod(P);
-  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, nullptr, L.nfaces};
+  const FaceSrc src{L.cp, L.g0, L.rr0, L.comp, L.g0f, L.rr0f, L.compf, dest, r, rhi, rlo, dsp, L.nfaces};
   HalfWarpSums<float> acc;
   uint32_t phase = 0;
   bool ok = true;
   const int ntiles = (L.nfaces + tc::kFaces - 1) / tc::kFaces;
   for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     const int first = t * tc::kFaces;
-    ok = tc::tile(sm, src, P, alpha, ialpha, mod, (float)L.dudv, first, min(tc::kFaces, L.nfaces - first), partial,
+    ok = tc::tile(sm, src, P, alpha, ialpha, am1, mod, (float)L.dudv, first, min(tc::kFaces, L.nfaces - first), partial,
                   acc, phase);
   }
   if (!ok && threadIdx.x == 0) atomicOr(status, kStatusTimeout);
@@ -3042,12 +3068,13 @@ int face_blocks_tc(int nfaces) {
 }
 
 cudaError_t launch_faces_tc(const dev::FaceLaunch &L, const int *dest, const dev::SurfaceParams &P, const double *r,
-                            const float *rhi, const float *rlo, float *partial, double *blockpart, int *status,
-                            int grid, const FinishArgs &fin, cudaStream_t s) {
+                            const float *rhi, const float *rlo, const float *dsp, float *partial, double *blockpart,
+                            int *status, int grid, const FinishArgs &fin, cudaStream_t s) {
+  if (!dsp) return cudaErrorInvalidValue;
   const cudaError_t e = tc_opt_in();
   if (e != cudaSuccess) return e;
-  dev::face_tc_kernel<<<grid, dev::tc::kThreads, dev::tc::kSmemBytes, s>>>(L, dest, P, r, rhi, rlo, partial, blockpart,
-                                                                           status, fin);
+  dev::face_tc_kernel<<<grid, dev::tc::kThreads, dev::tc::kSmemBytes, s>>>(L, dest, P, r, rhi, rlo, dsp, partial,
+                                                                           blockpart, status, fin);
   return cudaGetLastError();
 }
 
