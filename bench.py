@@ -680,7 +680,7 @@ def engine_arm(args) -> None:
                   "path": f"umcp_batch_step_host once per step: every job's state (positions and box scales, "
                           f"packed) copied in from pinned host memory, one batched step, the new states and each "
                           f"job's energy copied back; the {len(meshes32)} vesicles as {ngroups} batches "
-                          f"(every {ngroups}th vesicle), each on its own context from its own host thread, so "
+                          f"(vesicle i in batch i mod {ngroups}), each on its own context from its own host thread, so "
                           f"one batch's copies overlap another's step; wall clock, median of {E2E_REPEATS} runs",
                   "groups": ngroups, "wall_s": e2e_wall, "wall_s_runs": walls}
     del groups
