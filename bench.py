@@ -502,7 +502,7 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
     sec = e0.elapsed_time(e1) / 1e3
     energies = mesh.energies(K)
     r1, _ = mesh.state_get()
-    # the M^-1 apply alone: 8 bytes per nonzero (FP32 value, column) plus the row pointers and vectors
+    # the M^-1 apply alone: the stored form's bytes (values, columns or runs, row pointers) and the vectors
     n3 = 3 * plan.nv
     a = torch.randn(n3, dtype=torch.float64, device="cuda")
     b = torch.zeros_like(a)
@@ -516,10 +516,7 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
     ctx.synchronize()
     torch.cuda.synchronize()
     ms_apply = e0.elapsed_time(e1) / reps
-    if mi.dense:
-        apply_bytes = 4.0 * plan.nv * plan.nv + 8.0 * n3 * 2 + 4.0 * n3
-    else:
-        apply_bytes = (6.0 if plan.nv <= 65536 else 8.0) * mi.nnz_inverse + 4.0 * (plan.nv + 1) + 8.0 * n3 * 2 + 4.0 * n3
+    apply_bytes = float(mass_apply_bytes(plan.nv, mi.nnz_inverse, bool(mi.dense), True, mi.column_bytes))
     gbs = apply_bytes / (ms_apply * 1e-3) / 1e9
     return {"workload": "Langevin with the limit-surface M^-1 on a 40,962-vertex vesicle (R 1000 A, noise 2 A, "
                         "kc 20 kT), area and volume restraints, gamma 1/ps, FP32 form",
@@ -535,7 +532,8 @@ def langevin_mass_variant(ctx, U, W, torch, stream, tmpdir: Path, K: int, peak_g
             "minv_fill": mi.nnz_inverse / plan.nv ** 2,
             "minv_apply": {"ms": ms_apply, "bytes": apply_bytes, "gbs": gbs, "hbm_frac": gbs / peak_gbs,
                            "storage": ("FP32 dense" if mi.dense else "FP32 values, %s columns (CSR)"
-                                       % ("uint16" if plan.nv <= 65536 else "int32"))}}
+                                       % ("uint16" if plan.nv <= 65536 else "int32")),
+                           "column_bytes": int(mi.column_bytes)}}
 
 
 def engine_arm(args) -> None:
@@ -938,17 +936,17 @@ def geo_mode(args) -> None:
           f"with_restraints_us={restrained:.1f} restraints_us={restrained - plain:.1f} A={A:.6f} V={V:.6f}")
 
 
-def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool) -> int:
+def mass_apply_bytes(nrow: int, nnz: int, dense: bool, fp32: bool, column_bytes: int) -> int:
     """Algorithmic bytes of one apply, out += M^-1 in on 3 components per row:
-    CSR 6 per nonzero (FP32 value and a 16-bit column, up to 65,536 rows; 8
-    with 32-bit columns; 12 in FP64) plus, per row, the
-    row pointer (4), the input gathered at least once (16 as the packed FP32
-    copy, 24 in FP64) and the output read and written (48); dense 4 (or 8) per
-    entry plus the same per row."""
-    per_entry = (4 if fp32 else 8) if dense else ((6 if nrow <= 65536 else 8) if fp32 else 12)
-    entries = nrow * nrow if dense else nnz
+    sparse, the values (4 per nonzero in FP32, 8 in FP64) and the stored
+    columns (column_bytes: 4 or 2 per nonzero) plus, per row, the row pointer (4), the input
+    gathered at least once (16 as the packed FP32 copy, 24 in FP64) and the
+    output read and written (48); dense 4 (or 8) per entry plus the same per
+    row without the pointer."""
     per_row = (0 if dense else 4) + (16 if fp32 else 24) + 48
-    return per_entry * entries + per_row * nrow
+    if dense:
+        return (4 if fp32 else 8) * nrow * nrow + per_row * nrow
+    return (4 if fp32 else 8) * nnz + column_bytes + per_row * nrow
 
 
 def massapply_mode(args) -> None:
@@ -981,9 +979,10 @@ def massapply_mode(args) -> None:
     e1.record(stream)
     e1.synchronize()
     us = e0.elapsed_time(e1) * 1e3 / max(args.repeat, 1)
-    nbytes = mass_apply_bytes(nrow, info.nnz_inverse, bool(info.dense), fp32)
+    nbytes = mass_apply_bytes(nrow, info.nnz_inverse, bool(info.dense), fp32, info.column_bytes)
     fill = info.nnz_inverse / float(nrow * nrow)
-    print(f"rows={nrow} nnz={info.nnz_inverse} fill={fill:.3f} {'dense' if info.dense else 'csr'} {args.precision} "
+    form = {1: "dense", 2: "csr"}[mesh.info().mass_form]
+    print(f"rows={nrow} nnz={info.nnz_inverse} fill={fill:.3f} {form} {args.precision} "
           f"apply {us:.1f} us bytes={nbytes} ({nbytes / (us * 1e-6) / 1e9:.0f} GB/s) "
           f"finite={bool(torch.isfinite(y).all().item())}")
 

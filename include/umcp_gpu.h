@@ -196,6 +196,7 @@ typedef struct {
   int precision;
   long long device_bytes;  /* device memory held by the mesh's buffers */
   long long h2d_bytes;     /* host-to-device bytes umcp_mesh_create copied (tables, bases, positions) */
+  int mass_form;           /* installed M^-1: 0 none, 1 dense, 2 CSR */
 } umcp_mesh_info;
 umcp_status umcp_mesh_info_get(const umcp_mesh *mesh, umcp_mesh_info *info);
 /* Device bytes umcp_mesh_create would allocate for this plan at this
@@ -249,6 +250,8 @@ typedef struct {
   double assembly_s;    /* wall time of the build: M assembled on the device, */
   double inverse_s;     /* its Cholesky inverse (potrf + potri), */
   double truncation_s;  /* symmetrising, truncation and the stored form */
+  long long column_bytes; /* bytes of the stored columns: CSR 4 per nonzero (2 in the precision form up to
+                          * 65,536 rows); 0 when dense */
 } umcp_mass_info;
 umcp_status umcp_mass_build(umcp_mesh *mesh, const umcp_plan *plan, const umcp_mass_opts *opts, umcp_mass_info *info);
 /* The installed M^-1 as a dense nv x nv row-major array. Meshes of the

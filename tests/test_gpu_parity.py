@@ -301,3 +301,64 @@ def test_precision_form_mass_set_applies_in_fp32(ctx):
     got = m32.mass_apply(vin, base.copy(), None, 1.0, (1, 1, 1))
     assert np.all(np.abs(got - want) <= 1e-6 * bound + 1e-12 * np.abs(base))
     assert np.array_equal(m32.mass_get(), dense.astype(np.float32).astype(np.float64))
+
+
+def _run_rows(nv: int, rng) -> tuple:
+    """CSR rows made of runs of consecutive columns, as a truncated inverse's
+    rows are: a single run of up to 2,400 nonzeros, 40 one-column runs ahead
+    of a long run, runs of random lengths in random order with a repeated
+    column, and empty rows."""
+    rows, cols = [], []
+    for i in range(nv):
+        kind = i % 4
+        if i % 16 == 3:
+            js = np.zeros(0, dtype=np.int64)
+        elif kind == 0:
+            n = 1 + (37 * i) % min(2400, nv - 1)
+            a = int(rng.integers(0, nv - n))
+            js = np.arange(a, a + n)
+        elif kind == 1:
+            a = int(rng.integers(0, nv - 400))
+            js = np.concatenate([a + 2 * np.arange(40), a + 81 + np.arange(300)])
+        else:
+            parts = []
+            for _ in range(int(rng.integers(2, 9))):
+                n = int(rng.integers(1, 71))
+                a = int(rng.integers(0, nv - n))
+                parts.append(np.arange(a, a + n))
+            parts.append(parts[0][:1])  # a repeated column
+            js = np.concatenate([parts[k] for k in rng.permutation(len(parts))])
+        rows.append(len(js))
+        cols.extend(js)
+    rp = np.concatenate([[0], np.cumsum(rows)]).astype(np.int32)
+    return rp, np.array(cols, dtype=np.int32)
+
+
+def test_precision_form_mass_apply_on_long_and_ragged_rows(ctx):
+    """A CSR of rows of 0 to 2,400 nonzeros in runs of consecutive columns,
+    installed on meshes of both forms: the FP32 apply (which asks L2 for the
+    lines of long rows ahead of its loads) stays within 1e-6 of
+    sum_j |M_ij| |x_j| of the FP64 apply, with and without the per-row scaling
+    and alphas, and the CSR reads back as installed."""
+    plan, prm, _ = load_case("ico4_plain")
+    _, prm32, _ = load_case("ico4_plain", U.FP32_CENTRED)
+    m64, m32 = U.Mesh(ctx, plan, prm), U.Mesh(ctx, plan, prm32)
+    rng = np.random.default_rng(11)
+    rp, cl = _run_rows(plan.nv, rng)
+    assert np.diff(rp).max() > 32 * 40 and np.diff(rp).min() == 0
+    vl = rng.normal(0, 1, len(cl))
+    m64.mass_set(rp, cl, vl)
+    m32.mass_set(rp, cl, vl)
+    assert m32.info().mass_form == 2 and m64.info().mass_form == 2
+    dense = np.zeros((plan.nv, plan.nv))
+    np.add.at(dense, (np.repeat(np.arange(plan.nv), np.diff(rp)), cl), vl.astype(np.float32).astype(np.float64))
+    vin = rng.normal(0, 1, 3 * plan.nv)
+    base = rng.normal(0, 1, 3 * plan.nv)
+    scalev = rng.uniform(0.5, 2.0, 3 * plan.nv)
+    bound = (np.abs(dense) @ np.abs(vin.reshape(-1, 3))).reshape(-1)
+    for sv, alphas in ((None, (1, 1, 1)), (scalev, (1.1, 0.9, 1.05))):
+        want = m64.mass_apply(vin, base.copy(), sv, 0.7, alphas)
+        got = m32.mass_apply(vin, base.copy(), sv, 0.7, alphas)
+        scale_bound = 0.7 * 2.0 / 0.81 * bound  # scale x max scalev / min alpha^2
+        assert np.all(np.abs(got - want) <= 1e-6 * scale_bound + 1e-12 * np.abs(base))
+    assert np.array_equal(m32.mass_get(), dense)

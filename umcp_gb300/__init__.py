@@ -64,7 +64,7 @@ class MeshInfo(C.Structure):
     _fields_ = [
         ("nv", C.c_int), ("n_faces", C.c_int), ("n_points", C.c_int), ("n_slots", C.c_int),
         ("kernels_per_step", C.c_int), ("kernels_per_step_mass", C.c_int), ("precision", C.c_int),
-        ("device_bytes", C.c_longlong), ("h2d_bytes", C.c_longlong),
+        ("device_bytes", C.c_longlong), ("h2d_bytes", C.c_longlong), ("mass_form", C.c_int),
     ]
 
 
@@ -112,6 +112,7 @@ class MassInfo(C.Structure):
         ("area0", C.c_double), ("mass_per_point", C.c_double), ("points", C.c_longlong),
         ("nnz_mass", C.c_longlong), ("nnz_inverse", C.c_longlong), ("dense", C.c_int),
         ("assembly_s", C.c_double), ("inverse_s", C.c_double), ("truncation_s", C.c_double),
+        ("column_bytes", C.c_longlong),
     ]
 
 

@@ -823,6 +823,7 @@ extern "C" umcp_status umcp_mesh_info_get(const umcp_mesh *m, umcp_mesh_info *in
                             &G->compf, &G->basis_w})
       h2d += (long long)x->bytes;
   info->h2d_bytes = h2d;
+  info->mass_form = !m->mrows ? 0 : m->mass_dense ? 1 : 2;
   return UMCP_OK;
 }
 

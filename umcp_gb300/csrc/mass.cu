@@ -11,9 +11,11 @@
 // inverted there (Cholesky: potrf + potri, as the reference
 // does with LAPACK), symmetrised and truncated at the reference's relative
 // tolerance (|M^-1_ij| / sqrt(|M^-1_ii M^-1_jj|) > rel_tol, src/modes.C:1893).
-// The reference's tolerance of 1e-20 keeps every entry, so M^-1 stays dense
-// and the apply is a dense FP64 matrix times the three Cartesian components;
-// a looser tolerance that leaves it sparse (under 30% fill) stores CSR.
+// At or above 30% fill M^-1 stays dense and the apply is a dense matrix times
+// the three Cartesian components; below it it is stored as CSR (the
+// reference's tolerance of 1e-20 leaves a 40,962-vertex vesicle's M^-1 24.7%
+// full). The precision form stores FP32 values, with 16-bit columns up to
+// 65,536 rows.
 //
 // The factorisation uses cuSOLVER's dense Cholesky routines, loaded at run
 // time so the engine does not depend on the library where no mass matrix is
@@ -187,7 +189,8 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
 // each row in flight (the matrix streams from HBM once, with an evict-first
 // hint, while the input stays cached). Kahan-compensated FP32 sums per lane
 // and row, then the lanes' sums in FP64 in a fixed butterfly order, and the
-// scaling in FP64.
+// scaling in FP64. (L2 prefetches 8 iterations ahead of each row's loads, as
+// the CSR apply makes, took 10,242 rows from 153.5 to 163.9 us.)
 constexpr int kDenseRows = 4;
 constexpr int kDenseAhead = 4;
 constexpr int kDenseThreads = 256;
@@ -477,6 +480,7 @@ extern "C" umcp_status umcp_mass_build(umcp_mesh *m, const umcp_plan *plan, cons
     info->nnz_mass = (long long)nnz_mass;
     info->nnz_inverse = (long long)kept;
     info->dense = m->mass_dense ? 1 : 0;
+    info->column_bytes = (long long)(m->mass_dense ? 0 : m->mcol.bytes);
     info->assembly_s = sec(t_start, t_assembled);
     info->inverse_s = sec(t_assembled, t_inverted);
     info->truncation_s = sec(t_inverted, t_end);
