@@ -1837,7 +1837,9 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
 // Batched regular faces, precision form: a block takes a tile (faces of one
 // job), its warps 32 faces at a time; writes the tile's three energy sums.
 // counter[0] hands out the tiles; counter[1] counts the blocks that are done,
-// and the last of them zeroes both for the next launch.
+// and the last of them zeroes both for the next launch. A block draws its next
+// tile while it works on the current one (the draw's round trip hides behind
+// the faces), and copies a job's header only when the tile's job changes.
 __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
     batch_face_tpf_kernel(const BatchJob *__restrict__ jobs, int group, const BatchTile *__restrict__ tiles,
                           const int *__restrict__ counts, const double *__restrict__ basis,
@@ -1846,7 +1848,7 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   using namespace tpf;
   __shared__ Smem sm;
   __shared__ BatchFaceJob sj;
-  __shared__ int s_active, s_tile;
+  __shared__ int s_active, s_tile[2];
   tpf_stage(sm, basis, weight);  // constant tables: before the wait
   grid_dependency_wait();        // positions, job states and the counter come from the kernels before
   const int ntiles = counts[group], tile_base = counts[3 + group];
@@ -1854,22 +1856,26 @@ __global__ void __launch_bounds__(tpf::kThreads, tpf::kMinBlocks)
   const float dudv = (float)dudv_d;
   // Tiles are handed out by a counter (zeroed before the launch), so blocks
   // that draw cheap tiles take more; each tile's sums go to its own row, so
-  // the results do not depend on which block took which tile.
-  for (;;) {
-    __syncthreads();  // the previous tile's readers of sj, s_tile and sm.red are done
-    if (threadIdx.x == 0) s_tile = (int)blockIdx.x < ntiles ? atomicAdd(&counter[0], 1) : ntiles;
-    __syncthreads();
-    const int t = s_tile;
+  // the results do not depend on which block took which tile. Draw k is read
+  // from s_tile[k & 1] after the barrier that opens iteration k and written
+  // during iteration k - 1, after that iteration's own barrier: its readers
+  // of the same slot (iteration k - 2) are done by then.
+  if (threadIdx.x == 0) s_tile[0] = (int)blockIdx.x < ntiles ? atomicAdd(&counter[0], 1) : ntiles;
+  int job = -1;
+  for (int k = 0;; ++k) {
+    __syncthreads();  // the previous tile's readers of sj, s_active and sm.red are done; draw k is visible
+    const int t = s_tile[k & 1];
     if (t >= ntiles) break;
     const BatchTile tile = tiles[tile_base + t];
-    {
+    if (tile.job != job) {  // the same for every thread of the block
       const int *src = reinterpret_cast<const int *>(&jobs[tile.job].f);
       int *dst = reinterpret_cast<int *>(&sj);
       for (int i = threadIdx.x; i < (int)(sizeof(BatchFaceJob) / sizeof(int)); i += kThreads) dst[i] = src[i];
+      if (threadIdx.x == 0) s_active = job_active(jobs[tile.job].f);
+      job = tile.job;
+      __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x == 0) s_active = job_active(sj);
-    __syncthreads();
+    if (threadIdx.x == 0) s_tile[(k + 1) & 1] = atomicAdd(&counter[0], 1);
     HalfWarpSums<float> acc;
     if (s_active) {
       const FaceSrc &src = sj.src[group];
