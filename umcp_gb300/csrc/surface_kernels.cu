@@ -2387,7 +2387,7 @@ __device__ __forceinline__ void geo_face_ff(const GeoArgs &G, const GeoGroup &g,
 #pragma unroll 1
   for (int p = 0; p < NPT; ++p) {
     FF R[3] = {{0, 0}, {0, 0}, {0, 0}}, Ru[3] = {{0, 0}, {0, 0}, {0, 0}}, Rv[3] = {{0, 0}, {0, 0}, {0, 0}};
-#pragma unroll
+#pragma unroll 1  // rolled: the unrolled body (about 1,900 instructions) missed in the instruction cache
     for (int q = 0; q < (NCP + 3) / 4; ++q) {
       const float4 w4h = rows.r[gi][p][0][q], w4l = rows.r[gi][p][1][q], u4h = rows.r[gi][p][2][q],
                    u4l = rows.r[gi][p][3][q], v4h = rows.r[gi][p][4][q], v4l = rows.r[gi][p][5][q];
@@ -2524,6 +2524,16 @@ __global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__r
     int lf;
     const int gi = geo_group(G, f, &lf);
     const GeoGroup &g = G.g[gi];
+    {  // the next face's control-point and slot rows into L1 while this face runs
+      const int fn = f + gridDim.x * kGeoHW;
+      if (lane < 2 && fn < G.nfaces) {
+        int lfn;
+        const GeoGroup &h = G.g[geo_group(G, fn, &lfn)];
+        const size_t at = (size_t)lfn * h.ncp + (lane ? h.ncp - 1 : 0);
+        tpf::prefetch_l1(h.cp + at);
+        tpf::prefetch_l1(h.dest + at);
+      }
+    }
     int dest = 0;
     T X0[3];
     if constexpr (sizeof(T) == 8) {
@@ -2566,6 +2576,12 @@ __global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__r
         X0[c] = alpha[c] * (ahi + alo);  // the corner carries no image (its shift is zero)
       }
     }
+    // this face's partial slots, read now so that the read-modify-write at the
+    // end does not wait on them (no other thread touches these slots)
+    T old[3] = {0, 0, 0};
+    if (lane < g.ncp)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) old[k] = partial[3 * (size_t)dest + k];
     __syncwarp(hmask);
     if (lane < g.npt) {
       T R[3] = {0, 0, 0}, Ru[3] = {0, 0, 0}, Rv[3] = {0, 0, 0};
@@ -2611,7 +2627,7 @@ __global__ void __launch_bounds__(kGeoThreads) geo_grad_kernel(GeoArgs G, T *__r
         for (int k = 0; k < 3; ++k) Gx[k] += w * Es[hw][p][k] + u * Es[hw][p][3 + k] + v * Es[hw][p][6 + k];
       }
 #pragma unroll
-      for (int k = 0; k < 3; ++k) partial[3 * (size_t)dest + k] += alpha[k] * Gx[k];
+      for (int k = 0; k < 3; ++k) partial[3 * (size_t)dest + k] = old[k] + alpha[k] * Gx[k];
     }
     __syncwarp(hmask);
   }
