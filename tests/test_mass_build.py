@@ -142,6 +142,9 @@ def test_precision_form_applies_the_inverse_in_fp32(rel_tol):
     m32 = U.Mesh(ctx, plan, prm32)
     i32 = m32.mass_build(plan, rel_tol=rel_tol)
     assert (i32.dense, i32.nnz_inverse) == (i64.dense, i64.nnz_inverse) and i32.dense == (rel_tol < 0.01)
+    # the stored form and its column bytes: none when dense, 16-bit columns in the FP32 CSR, 32-bit in FP64
+    assert m32.info().mass_form == m64.info().mass_form == (1 if i32.dense else 2)
+    assert (i32.column_bytes, i64.column_bytes) == ((0, 0) if i32.dense else (2 * i32.nnz_inverse, 4 * i64.nnz_inverse))
     g = m64.mass_get()
     assert np.array_equal(m32.mass_get(), g.astype(np.float32).astype(np.float64))
     rng = np.random.default_rng(3)
