@@ -190,7 +190,9 @@ __global__ void dense_apply_kernel(int n, const double *__restrict__ A, const do
 // hint, while the input stays cached). Kahan-compensated FP32 sums per lane
 // and row, then the lanes' sums in FP64 in a fixed butterfly order, and the
 // scaling in FP64. (L2 prefetches 8 iterations ahead of each row's loads, as
-// the CSR apply makes, took 10,242 rows from 153.5 to 163.9 us.)
+// the CSR apply makes, took 10,242 rows from 153.5 to 163.9 us; two warps per
+// nine rows, one per half of the columns, with twice the loads in flight per
+// SM, took 164-166 us.)
 constexpr int kDenseRows = 4;
 constexpr int kDenseAhead = 4;
 constexpr int kDenseThreads = 256;
