@@ -2688,7 +2688,7 @@ constexpr int kSpmvUnroll = 4;
 // spmv32_kernel streams each row's values and columns, kSpmvUnroll windows of
 // 32 nonzeros per warp iteration; a warp also asks L2 for the lines
 // kSpmvAhead windows ahead of the ones it loads, so that its loads find them
-// there (40,962-vertex M^-1, 415 M nonzeros: 546 -> 481 us per apply).
+// there (40,962-vertex M^-1, 415 M nonzeros: 546 -> about 475 us per apply).
 constexpr int kSpmvAhead = 32;
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 template <typename C>  // column index type: int, or uint16_t for up to 65,536 columns
@@ -2718,7 +2718,8 @@ __global__ void spmv32_kernel(int nrow, const int *__restrict__ row_ptr, const C
     for (int k0 = beg + lane; k0 < end; k0 += 32 * kSpmvUnroll) {
       if (lane < 2 * kSpmvUnroll) {  // lanes 0..3: value lines ahead; lanes 4..7: their columns
         const int w = k0 - lane, ahead = 32 * (kSpmvAhead + (lane % kSpmvUnroll));
-        if (ahead < end - w) prefetch_l2(lane < kSpmvUnroll ? (const void *)&val[w + ahead] : (const void *)&col[w + ahead]);
+        if (ahead < end - w)
+          prefetch_l2(lane < kSpmvUnroll ? (const void *)&val[w + ahead] : (const void *)&col[w + ahead]);
       }
       float v[kSpmvUnroll];
       int j[kSpmvUnroll];
