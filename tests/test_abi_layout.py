@@ -65,3 +65,16 @@ def test_sizes_and_field_offsets_match_the_header(tmp_path):
             assert C.sizeof(getattr(U, key)) == int(value), key
         seen += 1
     assert seen == len(PAIRS) + sum(len(getattr(U, py)._fields_) for py in PAIRS)
+
+
+def test_every_prototype_is_bound_with_its_arity():
+    """Each function the header declares is in the binding's signature table
+    with as many argument types as the prototype has parameters."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    protos = {}
+    for m in re.finditer(r"^[ \t]*(?:const\s+)?[A-Za-z_][\w ]*?[\s*]+(umcp_\w+)\s*\(([^;{]*?)\)\s*;", text, re.M | re.S):
+        args = " ".join(m.group(2).split())
+        protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    sigs = U._SIGNATURES
+    assert len(protos) > 60 and set(protos) == set(sigs)
+    assert {k: n for k, n in protos.items() if len(sigs[k]) != n} == {}
